@@ -1,0 +1,222 @@
+/*
+ * snncuda_gb300.h -- C ABI of the GB300 spiking-simulation backend.
+ *
+ * The backend advances a flattened SNNCuda Connectome tick by tick with the
+ * semantics of the reference CPU runtime (runtime::NetworkPropagator):
+ * timing-wheel spike delivery with spike-code offset expansion,
+ * synapse -> dendrite -> receptor integration, threshold and reset, pair STDP
+ * with a runtime toggle, and neuron / synapse temporal-pattern recording with
+ * cosine matching.
+ *
+ * Conventions
+ *  - Every call returns an int status (SNNCUDA_OK on success).  No C++
+ *    exception crosses this boundary.  snncuda_last_error() returns a
+ *    thread-local message describing the last failure.
+ *  - Neurons are dense 0-based indices in Connectome::neurons order.
+ *    Synapses are dense 0-based indices in Connectome::synapses order; that
+ *    order defines the outgoing/incoming list order of the reference
+ *    (NetworkPropagator.cpp:24-28) and therefore the event order.
+ *  - All input arrays are caller-owned and copied at create.
+ *  - A handle is used by one host thread at a time.
+ *  - After a device-side error (capacity overflow, wait timeout) the handle
+ *    is poisoned: later stepping calls return SNNCUDA_ERR_POISONED; readers
+ *    keep working.
+ */
+#ifndef SNNCUDA_GB300_H
+#define SNNCUDA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define SNNCUDA_OK 0
+#define SNNCUDA_ERR_INVALID_ARGUMENT 1 /* std::invalid_argument in the reference */
+#define SNNCUDA_ERR_OUT_OF_MEMORY 2
+#define SNNCUDA_ERR_CAPACITY 3         /* a fixed device capacity would overflow */
+#define SNNCUDA_ERR_DEVICE 4           /* CUDA runtime error (check_cuda in the reference) */
+#define SNNCUDA_ERR_TIMEOUT 5          /* a bounded device-side wait gave up */
+#define SNNCUDA_ERR_UNSUPPORTED 6      /* input outside the engine's stated limits */
+#define SNNCUDA_ERR_POISONED 7         /* an earlier device error left the handle unusable */
+
+/* ---- enumerations (snn/Synapse.h:9-21 in the reference) ----------------- */
+#define SNNCUDA_COMPARTMENT_SOMA 0
+#define SNNCUDA_COMPARTMENT_BASAL 1
+#define SNNCUDA_COMPARTMENT_APICAL 2
+#define SNNCUDA_COMPARTMENT_INHIBITORY 3
+
+#define SNNCUDA_RECEPTOR_AMPA 0
+#define SNNCUDA_RECEPTOR_NMDA 1
+#define SNNCUDA_RECEPTOR_GABA_A 2
+#define SNNCUDA_RECEPTOR_GABA_B 3
+
+/* ---- reference C ABI, kept unchanged ------------------------------------
+ * Replaces include/snncuda/c/SNNCudaC.h:7-8 (src/c/SNNCudaC.cpp:5-11).
+ * snncuda_cuda_available reports a usable device at run time (the reference
+ * reports the compile-time flag, core/Version.cpp:9-11). */
+const char* snncuda_version(void);
+int snncuda_cuda_available(void);
+
+/* Thread-local description of the last failing call ("" if none). */
+const char* snncuda_last_error(void);
+
+/* ---- network input -------------------------------------------------------
+ * Flattened declarative::Connectome (declarative/Connectome.h:13-37) with the
+ * per-neuron NeuronParamsIR (declarative/NetworkIR.h:14-19). */
+typedef struct snncuda_network {
+    uint32_t neuron_count;
+    const float* threshold;                  /* [neuron_count] */
+    const uint64_t* pattern_window_ticks;    /* [neuron_count] */
+    const float* similarity_threshold;       /* [neuron_count] */
+    const uint64_t* max_reference_patterns;  /* [neuron_count], >= 1 */
+
+    uint64_t synapse_count;
+    const uint32_t* source;                  /* [synapse_count] neuron index */
+    const uint32_t* target;                  /* [synapse_count] neuron index */
+    const float* weight;                     /* [synapse_count] */
+    const float* max_weight;                 /* [synapse_count] */
+    const uint32_t* delay_ticks;             /* [synapse_count] */
+    const uint8_t* compartment;              /* [synapse_count] SNNCUDA_COMPARTMENT_* */
+    const uint8_t* receptor;                 /* [synapse_count] SNNCUDA_RECEPTOR_* */
+    const uint8_t* plasticity_enabled;       /* [synapse_count] 0/1 */
+    /* Spike-code offsets as CSR: offsets of synapse s are
+     * code_offsets[code_offset_ptr[s] .. code_offset_ptr[s+1]).  An empty
+     * list means {0} (SynapseDendriteProcessor.cpp:68-70).  NULL pointers
+     * mean every synapse carries {0}. */
+    const uint64_t* code_offset_ptr;         /* [synapse_count + 1] or NULL */
+    const uint32_t* code_offsets;
+} snncuda_network;
+
+/* ---- processor configuration ---------------------------------------------
+ * SynapseDendriteConfig (runtime/SynapseDendriteProcessor.h:37-40) holding a
+ * learning::StdpConfig (learning/STDP.h:8-16), plus engine options. */
+typedef struct snncuda_config {
+    int32_t stdp_enabled;              /* StdpConfig::enabled, default 1 */
+    float ltp_amplitude;               /* 0.01 */
+    float ltd_amplitude;               /* 0.012 */
+    float ltp_tau_ticks;               /* 20 */
+    float ltd_tau_ticks;               /* 20 */
+    float min_weight;                  /* 0 */
+    float max_weight;                  /* 2 */
+    int32_t temporal_learning_enabled; /* 1 */
+
+    /* Engine options (0 = default). */
+    uint64_t timing_wheel_slots;       /* accepted for parity with the reference
+                                          constructor; must be nonzero
+                                          (SpikeScheduler.cpp:10-12) */
+    uint64_t slot_event_capacity;      /* events one wheel slot can hold */
+    uint64_t pattern_run_capacity;     /* per-neuron run storage for learned
+                                          temporal patterns */
+    uint64_t raster_capacity;          /* fire records kept for read-back;
+                                          0 disables capture */
+    void* cuda_stream;                 /* cudaStream_t to launch on; NULL =
+                                          the handle creates its own */
+} snncuda_config;
+
+/* Fills the reference defaults. */
+void snncuda_config_default(snncuda_config* config);
+
+typedef struct snncuda_sim snncuda_sim;
+
+/* Replaces NetworkPropagator(const Connectome&, NeuronStateStore&, size_t,
+ * size_t) (runtime/NetworkPropagator.h:16-20, NetworkPropagator.cpp:5-29):
+ * initial neuron state from the params, synapse runtime state from the
+ * Connectome (SynapseDendriteProcessor.cpp:59-75). */
+int snncuda_sim_create(const snncuda_network* network, const snncuda_config* config,
+                       snncuda_sim** out);
+int snncuda_sim_destroy(snncuda_sim* sim);
+
+/* Replaces NetworkPropagator::inject (NetworkPropagator.cpp:31-37), applied
+ * in array order.  A tick earlier than the next tick to process is clamped
+ * to it (SpikeScheduler.cpp:17-19). */
+int snncuda_sim_inject(snncuda_sim* sim, uint64_t count, const uint32_t* neurons,
+                       const uint64_t* ticks, const float* weights);
+
+/* Replaces NetworkPropagator::run_until (NetworkPropagator.cpp:39-43):
+ * processes every tick up to and including inclusive_tick that has not been
+ * processed yet.  Blocks until the device has finished. */
+int snncuda_sim_run_until(snncuda_sim* sim, uint64_t inclusive_tick);
+
+/* Runtime toggles: StdpRule::set_enabled (STDP.cpp:12-14) -- a disabled rule
+ * still clamps the weight (STDP.cpp:37-40) -- and
+ * SynapseDendriteConfig::temporal_learning_enabled. */
+int snncuda_sim_set_plasticity(snncuda_sim* sim, int32_t enabled);
+int snncuda_sim_set_temporal_learning(snncuda_sim* sim, int32_t enabled);
+
+typedef struct snncuda_counters {
+    uint64_t delivered_spikes;  /* NetworkPropagator::delivered_spike_count
+                                   (synaptic + external events) */
+    uint64_t fired_spikes;      /* NetworkPropagator::fired_spike_count */
+    uint64_t synaptic_events;   /* delivered (synapse, offset) events */
+    uint64_t external_events;   /* delivered injected events */
+    uint64_t next_tick;         /* first tick not yet processed */
+    uint64_t pending_events;    /* SpikeScheduler::pending_count */
+    uint64_t raster_count;      /* fire records captured so far */
+    uint64_t max_slot_events;   /* largest per-tick due list seen (engine stat) */
+} snncuda_counters;
+int snncuda_sim_counters(snncuda_sim* sim, snncuda_counters* out);
+
+/* NetworkPropagator::idle (NetworkPropagator.cpp:74-76). */
+int snncuda_sim_idle(snncuda_sim* sim, int32_t* out);
+
+/* NeuronState (runtime/NeuronStateCache.h:15-45) of every neuron.  Any
+ * pointer may be NULL.  Ticks that are std::nullopt in the reference read -1. */
+typedef struct snncuda_neuron_state {
+    float* membrane_potential;          /* [N] */
+    uint64_t* spike_count;              /* [N] */
+    int64_t* last_fired_tick;           /* [N] */
+    uint64_t* last_active_tick;         /* [N] */
+    float* compartment_current;         /* [N*4] soma, basal, apical, inhibitory */
+    uint64_t* compartment_last_update;  /* [N*4] */
+    float* compartment_tau;             /* [N*4] */
+    uint64_t* window_start_tick;        /* [N] temporal_pattern.window_start_tick */
+    uint64_t* offset_count;             /* [N] temporal_pattern.spike_offsets.size() */
+    uint64_t* learned_count;            /* [N] temporal_pattern.learned_patterns.size() */
+    uint64_t* match_count;              /* [N] */
+    uint8_t* last_match;                /* [N] */
+} snncuda_neuron_state;
+int snncuda_sim_read_neurons(snncuda_sim* sim, const snncuda_neuron_state* out);
+
+/* SynapseRuntimeState (runtime/SynapseDendriteProcessor.h:14-35) of every
+ * synapse, in Connectome order.  Any pointer may be NULL. */
+typedef struct snncuda_synapse_state {
+    float* weight;
+    int64_t* last_pre_spike_tick;
+    int64_t* last_post_spike_tick;
+    uint64_t* pre_spike_count;
+    uint64_t* plasticity_update_count;
+    float* last_weight_delta;
+    uint64_t* code_window_start_tick;
+    uint64_t* code_offset_count;
+    uint64_t* learned_code_count;
+    uint64_t* code_match_count;
+    uint8_t* last_code_match;
+} snncuda_synapse_state;
+int snncuda_sim_read_synapses(snncuda_sim* sim, const snncuda_synapse_state* out);
+
+/* One variable-length temporal list:
+ *   kind 0: neuron `index` temporal_pattern.spike_offsets
+ *   kind 1: neuron `index` learned_patterns[which]
+ *   kind 2: synapse `index` code_offsets
+ *   kind 3: synapse `index` learned_code_patterns[which]
+ * Writes min(len, capacity) values and the full length to *len. */
+int snncuda_sim_read_pattern(snncuda_sim* sim, int32_t kind, uint64_t index, uint64_t which,
+                             uint32_t* values, uint64_t capacity, uint64_t* len);
+
+/* 64-bit digests of the complete neuron and synapse state, defined over the
+ * reference field values (see the implementation of digest_neurons /
+ * digest_synapses); equal digests mean bit-identical state. */
+int snncuda_sim_state_digest(snncuda_sim* sim, uint64_t* neuron_digest, uint64_t* synapse_digest);
+
+/* Fire records in processing order: (tick, neuron).  Requires
+ * config.raster_capacity > 0. */
+int snncuda_sim_read_raster(snncuda_sim* sim, uint64_t first, uint64_t count, uint64_t* ticks,
+                            uint32_t* neurons);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SNNCUDA_GB300_H */

@@ -1,0 +1,221 @@
+// Device data layout and kernel interface of the GB300 tick engine.
+//
+// One simulation = one network resident in HBM:
+//   * neurons: NeuronRec (64 B, dynamic state), NeuronTp (32 B, temporal
+//     bookkeeping), NeuronParam (64 B, read-only) -- one per neuron;
+//   * synapses in target-major order (incoming lists of each target
+//     contiguous, Connectome order inside a list): SynA (32 B: weight, STDP
+//     state, static fields) and SynB (32 B: code-pattern state, counters);
+//   * pre-expanded outgoing events: for every source, its (synapse, code
+//     offset) events grouped by delivery delay class, each class in
+//     Connectome x offset order -- spike-code expansion is then a copy;
+//   * a timing wheel of W slots, each a buffer of 64-bit events in exact
+//     scheduling order (the reference bucket FIFO order).
+#pragma once
+
+#include <cstdint>
+
+namespace snngb {
+
+// Event word: low 32 bits = target neuron, bit 31 set for an external input;
+// high 32 bits = target-major synapse index, or the float weight bits of an
+// external input.
+constexpr uint32_t kExternalBit = 0x80000000u;
+
+// Status bits raised by kernels (host maps them to SNNCUDA_ERR_*).
+constexpr uint32_t kStatusSlotOverflow = 1u << 0;
+constexpr uint32_t kStatusRingOverflow = 1u << 1;
+constexpr uint32_t kStatusRasterOverflow = 1u << 2;
+constexpr uint32_t kStatusPostCountOverflow = 1u << 3;
+constexpr uint32_t kStatusRunOverflow = 1u << 4;
+constexpr uint32_t kStatusFireOverflow = 1u << 5;
+
+// SynA.meta bit fields.
+constexpr uint32_t kMetaDelayMask = 0xFFFFu;
+constexpr int kMetaCompShift = 16;      // 2 bits
+constexpr int kMetaRecShift = 18;       // 2 bits
+constexpr int kMetaPlasticBit = 20;     // 1 bit
+constexpr int kMetaExpectedShift = 21;  // 4 bits: max(2, #code offsets), <= 8
+
+constexpr int kMaxExpected = 8;
+
+struct alignas(32) SynA {
+    float weight;
+    uint32_t last_pre1;   // last_pre_spike_tick + 1, 0 = none
+    uint32_t last_post1;  // last_post_spike_tick + 1, 0 = none
+    uint32_t meta;
+    float clamp_hi;       // min(StdpConfig::max_weight, synapse max_weight)
+    uint32_t updates;     // plasticity_update_count
+    float last_delta;     // last_weight_delta
+    uint32_t post_cnt;    // target fires already applied at tick last_post1-1
+};
+
+struct alignas(32) SynB {
+    uint32_t pre_count;
+    uint32_t code_ws;       // code_window_start_tick
+    uint32_t code_matches;  // code_match_count
+    uint8_t code_len;       // code_offsets.size() (<= expected)
+    uint8_t last_code_match;
+    uint16_t learned_count; // learned_code_patterns.size()
+    uint16_t ring[kMaxExpected];  // code_offsets in order
+};
+
+struct alignas(64) NeuronRec {
+    float cur[4];          // soma, basal, apical, inhibitory current
+    uint32_t upd[4];       // compartment last_update_tick
+    float membrane;
+    uint32_t spike_count;
+    uint32_t last_fired1;  // last_fired_tick + 1, 0 = none
+    uint32_t last_active;
+    uint32_t flags;        // bits 0-7: 4 x 2-bit tau code; bit 8: temporal last_match
+    uint32_t match_count;
+    uint32_t ws;           // temporal window_start_tick
+    uint32_t len;          // spike_offsets.size()
+};
+
+struct alignas(32) NeuronTp {
+    unsigned long long cn;  // sum of squares of the current window's offsets
+    uint32_t nruns;         // runs in the current window's run list
+    uint32_t ref_head;      // FIFO index of the oldest learned pattern
+    uint32_t ref_count;
+    uint32_t ring_head;     // next free run slot of the learned-pattern run ring
+    uint32_t ring_used;
+    uint32_t pad;
+};
+
+struct alignas(64) NeuronParam {
+    float threshold;
+    uint32_t window;        // pattern_window_ticks
+    float similarity;
+    uint32_t max_refs;      // max_reference_patterns
+    uint32_t ring_cap;      // runs in the learned-pattern ring
+    uint32_t pad;
+    unsigned long long in_begin;    // first target-major synapse index
+    unsigned long long cand_base;   // run list of the current window (window+1 runs)
+    unsigned long long meta_base;   // max_refs RefMeta entries
+    unsigned long long ring_base;   // ring_cap runs
+    unsigned long long lcode_base;  // learned code patterns of the incoming synapses
+};
+
+// A learned temporal pattern: runs in the neuron's ring plus the running
+// prefix sums of its cosine against the current window.
+struct alignas(16) RefMeta {
+    unsigned long long dot, rn, cn;  // exact integer sums over min(len, window length)
+    uint32_t start;                  // first run (ring position)
+    uint32_t nruns;
+    uint32_t len;                    // pattern length
+    uint32_t cur_run;                // cursor into the pattern (run, position)
+    uint32_t cur_pos;
+    uint32_t match;                  // 0 no, 1 yes, 2 unknown (recompute from sums)
+};
+
+// A run of equal offsets: value in the low 16 bits, count in the high 48.
+__host__ __device__ inline uint32_t run_value(unsigned long long r) { return static_cast<uint32_t>(r & 0xFFFFu); }
+__host__ __device__ inline unsigned long long run_count(unsigned long long r) { return r >> 16; }
+
+// Per-tick scratch and counters that live on the device.
+struct TickState {
+    unsigned long long delivered;
+    unsigned long long external;
+    unsigned long long fired;
+    unsigned long long max_slot_events;
+    unsigned long long raster_count;
+    uint32_t status;
+    uint32_t tick;            // tick being processed
+    uint32_t n_due;           // events due this tick
+    uint32_t n_touched;       // targets with at least one due event
+    uint32_t n_fires;         // fires this tick
+    uint32_t n_fired_targets; // distinct targets that fired this tick
+    uint32_t expand_fires;    // fires whose events k_expand copies
+    uint32_t far_first_tick;  // delivery tick of far_idx[0] for the current run
+    uint32_t far_ticks;       // entries of far_idx minus one (0 = none)
+    int32_t stdp_enabled;     // StdpRule::enabled (runtime toggle)
+    int32_t temporal_enabled; // SynapseDendriteConfig::temporal_learning_enabled
+    uint32_t done_scan;       // "last block" counters
+    uint32_t done_fire_tile;
+    uint32_t done_fire_list;
+};
+
+struct Tables {
+    const float* decay;     // [4][decay_len]: expf(-e / tau_k), e = 0..decay_len-1
+    uint32_t decay_len;
+    const float* ltp;       // [stdp_len]: A+ expf(-dt / tau+)
+    const float* ltd;       // [stdp_len]: -A- expf(-dt / tau-)
+    uint32_t stdp_len;
+};
+
+// Everything a tick needs, passed by value to the kernels.
+struct Engine {
+    uint32_t N;
+    uint32_t W;             // wheel slots (power of two)
+    uint32_t wmask;
+    uint32_t D;             // delay classes
+    unsigned long long S;
+    unsigned long long slot_cap;
+    uint32_t code_stride;   // max expected over the network
+    unsigned long long raster_cap;
+    uint32_t fire_cap;
+    uint32_t fire_tiles_cap;
+    float min_weight;
+
+    // network
+    const unsigned long long* in_ptr;      // [N+1] target-major row pointers
+    const NeuronParam* nparam;             // [N]
+    NeuronRec* nrec;                       // [N]
+    NeuronTp* ntp;                         // [N]
+    unsigned long long* cand;              // run lists of current windows
+    RefMeta* refmeta;
+    unsigned long long* ring;              // learned-pattern runs
+    SynA* syna;                            // [S] target-major
+    SynB* synb;                            // [S]
+    uint16_t* lcode;                       // learned code patterns
+    const unsigned long long* pre_base;    // [N] first pre-expanded event of a source
+    const uint32_t* pre_off;               // [N*(D+1)] class offsets within a source
+    const unsigned long long* pre_ev;      // pre-expanded events
+    const uint32_t* cls_delta;             // [D] delivery delay of each class (>= 1)
+
+    // wheel
+    unsigned long long* wheel;             // [W * slot_cap]
+    uint32_t* slot_count;                  // [W]
+
+    // per-tick scratch
+    uint32_t* cnt;                         // [N] due events per target (zero between ticks)
+    uint32_t* seg_start;                   // [N]
+    uint32_t* tile_sum;                    // scan partials
+    uint32_t* tile_nz;
+    uint32_t* touched;                     // [N] target ids with due events, ascending
+    unsigned long long* grp;               // [slot_cap] (payload << 32) | (due index | ext << 31)
+    uint32_t* fire_bits;                   // [slot_cap/32] bitmap of due positions that fired
+    uint32_t* fire_at;                     // [slot_cap] firing neuron at a due position
+    uint32_t* fire_tile;                   // bitmap tile bases
+    uint32_t* fire_list;                   // [fire_cap] firing neurons in reference order
+    uint32_t* fired_tgt;                   // [N] targets that fired this tick
+    uint32_t* fired_cnt;                   // [N] their fire counts
+    uint32_t* xsum;                        // [fire_cap/8][D] events per (expansion block, class)
+    unsigned long long* xdst;              // [fire_cap/8][D] wheel position of each
+    uint32_t* xdst_ok;                     // [D] class destination fits its slot
+    uint32_t* raster;                      // [raster_cap * 2] (tick, neuron)
+
+    // far-future injections for the current run (see TickState)
+    const unsigned long long* far_ev;
+    const uint32_t* far_idx;
+
+    TickState* ts;
+    Tables tab;
+
+    // launch shapes
+    uint32_t grid_wide;
+    uint32_t grid_process;
+    uint32_t grid_fire;
+};
+
+constexpr int kScanTile = 4096;          // entries per scan tile (256 threads x 16)
+constexpr int kExpandFires = 8;          // fires per expansion block (one warp each)
+constexpr uint32_t kMaxClasses = 256;    // distinct delivery delays
+
+// Host-side launchers (kernels.cu).
+void launch_tick(const Engine& e, cudaStream_t stream);
+void launch_inject(const Engine& e, const unsigned long long* ev, const uint32_t* slot_of_group,
+                   const uint32_t* group_off, uint32_t groups, cudaStream_t stream);
+
+}  // namespace snngb

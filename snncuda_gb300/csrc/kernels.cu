@@ -1,0 +1,837 @@
+// Tick kernels of the GB300 engine (sm_103a).
+//
+// One tick t processes wheel slot t mod W, whose buffer holds the events due
+// at t in the exact order the reference scheduler would pop them
+// (SpikeScheduler.cpp:25-47: bucket FIFO order).  Per tick:
+//
+//  1. k_hist      count due events per target (and move far-future injects
+//                 that become reachable into the wheel)
+//  2. k_scan_tile exclusive scan of the per-target counts (+ last block
+//                 scans the tile sums)
+//  3. k_scan_out  segment starts and the ascending list of touched targets
+//  4. k_scatter   group the due events by target (unordered inside a group)
+//  5. k_process   one thread per touched target: restore due order inside its
+//                 group, then run the reference per-event physics in order
+//                 (SynapseDendriteProcessor.cpp:89-212, :294-365) and mark
+//                 fires in a due-position bitmap
+//  6. k_post      post-spike STDP over the in-rows of targets that fired
+//                 (SynapseDendriteProcessor.cpp:138-173) + fire tile counts
+//  7. k_fire_list fires in due order (= reference fire order), raster, class
+//                 sums; the last block scans destinations, finishes the tick
+//  8. k_expand    copy each fire's pre-expanded (synapse, offset) events into
+//                 their delivery slots, order-preserving
+//
+// Every wait is a kernel boundary or a "last block" hand-off (an atomic
+// counter, no spinning), so no kernel here can hang.
+// Float arithmetic uses explicitly rounded intrinsics so nothing is
+// contracted into an FMA: each operation rounds exactly as the reference's
+// separately evaluated float expressions.
+
+#include <cuda_runtime.h>
+
+#include "engine.h"
+
+namespace snngb {
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ float rec_gain(uint32_t r) { return r == 1 ? 0.55f : (r == 3 ? 0.65f : 1.0f); }
+__device__ __forceinline__ float rec_sign(uint32_t r) { return r >= 2 ? -1.0f : 1.0f; }
+
+__device__ __forceinline__ void raise_status(const Engine& e, uint32_t bit) { atomicOr(&e.ts->status, bit); }
+
+// ---------------------------------------------------------------------------
+// block-level helpers
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t n = __shfl_up_sync(0xffffffffu, v, d);
+        if (lane >= d) v += n;
+    }
+    return v;
+}
+
+// Exclusive block scan of one value per thread (blockDim.x == kThreads).
+// Returns the exclusive prefix; *total receives the block sum.
+__device__ uint32_t block_excl_scan(uint32_t v, uint32_t* total) {
+    __shared__ uint32_t warp_sums[kThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t incl = warp_incl_scan(v);
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t s = lane < kThreads / 32 ? warp_sums[lane] : 0;
+        s = warp_incl_scan(s);
+        if (lane < kThreads / 32) warp_sums[lane] = s;
+    }
+    __syncthreads();
+    const uint32_t base = warp > 0 ? warp_sums[warp - 1] : 0;
+    if (total) *total = warp_sums[kThreads / 32 - 1];
+    __syncthreads();
+    return base + incl - v;
+}
+
+// "Last block" hand-off: returns true in exactly one block, after every
+// block's prior global writes are visible.
+__device__ bool last_block(uint32_t* counter) {
+    __shared__ bool is_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t v = atomicAdd(counter, 1u);
+        is_last = (v == gridDim.x - 1);
+        if (is_last) *counter = 0;
+    }
+    __syncthreads();
+    if (is_last) __threadfence();
+    return is_last;
+}
+
+// Exclusive scan of n values in place, run by a single block (carry loop).
+__device__ void block_scan_inplace(uint32_t* data, uint32_t n, uint32_t* total_out) {
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < n; base += kThreads) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t v = i < n ? __ldcg(data + i) : 0;
+        uint32_t tot;
+        const uint32_t ex = block_excl_scan(v, &tot);
+        if (i < n) data[i] = carry + ex;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+    if (total_out && threadIdx.x == 0) *total_out = carry;
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// per-event physics
+// ---------------------------------------------------------------------------
+
+// float(dot / (sqrt(rn) * sqrt(cn))) >= sim for sim > 0
+// (TemporalPattern.cpp:35-60, :20-22).  dot, rn, cn are the exact integer
+// sums the reference accumulates in double.  A single-precision estimate
+// (relative error < 1e-6) decides every case farther than 2e-5 from the
+// threshold; the rest take the reference's exact double expression.
+__device__ bool cos_ge(unsigned long long dot, unsigned long long rn, unsigned long long cn, float sim) {
+    if (rn == 0 || cn == 0) return false;  // similarity 0.0f < sim
+    const float est = __fmul_rn(__fmul_rn(__ull2float_rn(dot), rsqrtf(__ull2float_rn(rn))),
+                                rsqrtf(__ull2float_rn(cn)));
+    if (est >= sim * 1.00002f) return true;
+    if (est <= sim * 0.99998f) return false;
+    const double q = __ddiv_rn(__ull2double_rn(dot),
+                               __dmul_rn(__dsqrt_rn(__ull2double_rn(rn)), __dsqrt_rn(__ull2double_rn(cn))));
+    return __double2float_rn(q) >= sim;
+}
+
+struct NState {
+    float cur[4];
+    uint32_t upd[4];
+    uint32_t flags;  // tau codes (2 bits each) | last_match << 8
+    float membrane;
+    uint32_t spikes, last_fired1, last_active, match_count, ws, len;
+    unsigned long long cn;
+    uint32_t nruns, ref_head, ref_count, ring_head, ring_used;
+};
+
+__device__ __forceinline__ float decay_factor(const Tables& tb, uint32_t code, uint32_t elapsed) {
+    const uint32_t i = elapsed < tb.decay_len ? elapsed : tb.decay_len - 1;
+    return tb.decay[code * tb.decay_len + i];
+}
+
+// SynapseDendriteProcessor.cpp:294-316 (+ :14-41), on the exact run-length
+// representation: offsets inside a window never decrease, so the window is
+// kept as runs (value, count); learned patterns are run lists in a per-neuron
+// ring, each with running integer sums of its cosine against the window.
+__device__ void temporal_update(NState& s, const NeuronParam& p, uint32_t t, const Engine& e, int enabled) {
+    if (!enabled) {
+        s.flags &= ~(1u << 8);
+        return;
+    }
+    unsigned long long* cand = e.cand + p.cand_base;
+    RefMeta* meta = e.refmeta + p.meta_base;
+    unsigned long long* ring = e.ring + p.ring_base;
+    if (s.len == 0 || t - s.ws > p.window) {
+        s.ws = t;
+        s.len = 0;
+        s.nruns = 0;
+        s.cn = 0;
+        for (uint32_t r = 0; r < s.ref_count; ++r) {
+            RefMeta& m = meta[(s.ref_head + r) % p.max_refs];
+            m.dot = 0;
+            m.rn = 0;
+            m.cn = 0;
+            m.cur_run = 0;
+            m.cur_pos = 0;
+            m.match = 2;
+        }
+    }
+    const uint32_t o = t - s.ws;
+    const unsigned long long oo = static_cast<unsigned long long>(o) * o;
+    if (s.nruns > 0 && run_value(cand[s.nruns - 1]) == o) {
+        cand[s.nruns - 1] += (1ull << 16);
+    } else {
+        if (s.nruns > p.window) {  // cannot happen: at most window+1 distinct offsets
+            raise_status(e, kStatusRunOverflow);
+            return;
+        }
+        cand[s.nruns++] = static_cast<unsigned long long>(o) | (1ull << 16);
+    }
+    s.len += 1;
+    s.cn += oo;
+    for (uint32_t r = 0; r < s.ref_count; ++r) {
+        RefMeta& m = meta[(s.ref_head + r) % p.max_refs];
+        if (s.len <= m.len) {
+            const unsigned long long run = ring[(m.start + m.cur_run) % p.ring_cap];
+            const unsigned long long v = run_value(run);
+            if (++m.cur_pos == run_count(run)) {
+                m.cur_run += 1;
+                m.cur_pos = 0;
+            }
+            m.dot += v * o;
+            m.rn += v * v;
+            m.cn += oo;
+            m.match = 2;
+        }
+    }
+    bool match = false;
+    if (s.ref_count > 0 && s.len >= 2) {
+        if (0.0f >= p.similarity) {
+            match = true;
+        } else {
+            for (uint32_t r = 0; r < s.ref_count && !match; ++r) {
+                RefMeta& m = meta[(s.ref_head + r) % p.max_refs];
+                if (m.match == 2) m.match = cos_ge(m.dot, m.rn, m.cn, p.similarity) ? 1 : 0;
+                match = m.match == 1;
+            }
+        }
+    }
+    if (match) {
+        s.flags |= (1u << 8);
+        s.match_count += 1;
+        return;
+    }
+    s.flags &= ~(1u << 8);
+    if (s.len < 2) return;
+    // learn_pattern: FIFO with max_reference_patterns entries.
+    if (s.ref_count >= p.max_refs) {
+        s.ring_used -= meta[s.ref_head].nruns;
+        s.ref_head = (s.ref_head + 1) % p.max_refs;
+        s.ref_count -= 1;
+    }
+    if (s.ring_used + s.nruns > p.ring_cap) {
+        raise_status(e, kStatusRingOverflow);
+        return;
+    }
+    const uint32_t idx = (s.ref_head + s.ref_count) % p.max_refs;
+    const uint32_t start = s.ring_head;
+    for (uint32_t j = 0; j < s.nruns; ++j) ring[(start + j) % p.ring_cap] = cand[j];
+    s.ring_head = (start + s.nruns) % p.ring_cap;
+    s.ring_used += s.nruns;
+    RefMeta& m = meta[idx];
+    m.dot = s.cn;
+    m.rn = s.cn;
+    m.cn = s.cn;
+    m.start = start;
+    m.nruns = s.nruns;
+    m.len = s.len;
+    m.cur_run = 0;
+    m.cur_pos = 0;
+    m.match = 2;
+    s.ref_count += 1;
+}
+
+// SynapseDendriteProcessor.cpp:175-229.  Returns whether the neuron fired.
+__device__ bool process_input(NState& s, const NeuronParam& p, uint32_t comp, uint32_t rec, float w,
+                              uint32_t t, const Engine& e, int temporal) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (t <= s.upd[k] || s.cur[k] == 0.0f) {
+            s.upd[k] = t;
+        } else {
+            const uint32_t code = (s.flags >> (2 * k)) & 3u;
+            s.cur[k] = __fmul_rn(s.cur[k], decay_factor(e.tab, code, t - s.upd[k]));
+            s.upd[k] = t;
+        }
+    }
+    const float applied = __fmul_rn(__fmul_rn(w, rec_gain(rec)), rec_sign(rec));
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (static_cast<uint32_t>(k) == comp) {
+            s.cur[k] = __fadd_rn(s.cur[k], applied);
+            s.upd[k] = t;
+            s.flags = (s.flags & ~(3u << (2 * k))) | (rec << (2 * k));
+        }
+    }
+    s.last_active = t;
+    temporal_update(s, p, t, e, temporal);
+    s.membrane = __fadd_rn(__fadd_rn(__fadd_rn(s.cur[0], s.cur[1]), s.cur[2]), s.cur[3]);
+    if (s.membrane >= p.threshold) {
+        s.membrane = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            s.cur[k] = 0.0f;
+            s.upd[k] = t;
+        }
+        // reset taus: soma AMPA, basal AMPA, apical NMDA, inhibitory GABA_A
+        s.flags = (s.flags & ~0xFFu) | (0u << 0) | (0u << 2) | (1u << 4) | (2u << 6);
+        s.last_fired1 = t + 1;
+        s.spikes += 1;
+        return true;
+    }
+    return false;
+}
+
+// StdpRule::weight_delta + apply (STDP.cpp:20-40) and the update bookkeeping
+// of SynapseDendriteProcessor.cpp:108-122 / :158-172.
+__device__ void stdp_apply(SynA& a, uint32_t pre, uint32_t post, const Engine& e, int stdp) {
+    const float before = a.weight;
+    float delta = 0.0f;
+    if (stdp) {
+        if (post > pre) {
+            const uint32_t dt = post - pre;
+            delta = e.tab.ltp[dt < e.tab.stdp_len ? dt : e.tab.stdp_len - 1];
+        } else if (post < pre) {
+            const uint32_t dt = pre - post;
+            delta = e.tab.ltd[dt < e.tab.stdp_len ? dt : e.tab.stdp_len - 1];
+        }
+    }
+    float v = __fadd_rn(a.weight, delta);
+    v = v < e.min_weight ? e.min_weight : (a.clamp_hi < v ? a.clamp_hi : v);
+    a.weight = v;
+    a.last_delta = __fsub_rn(v, before);
+    if (a.last_delta != 0.0f) a.updates += 1;
+}
+
+// apply_post_spike_plasticity for every target fire at tick t not yet
+// applied to this synapse (fires = target fires so far this tick).
+__device__ __forceinline__ bool post_catch_up(SynA& a, uint32_t t, uint32_t fires, const Engine& e, int stdp) {
+    const uint32_t applied = a.last_post1 == t + 1 ? a.post_cnt : 0u;
+    if (fires <= applied) return false;
+    const bool plastic = (a.meta >> kMetaPlasticBit) & 1u;
+    for (uint32_t k = applied; k < fires; ++k) {
+        a.last_post1 = t + 1;
+        if (plastic && a.last_pre1 != 0) stdp_apply(a, a.last_pre1 - 1, t, e, stdp);
+    }
+    a.post_cnt = fires;
+    return true;
+}
+
+// SynapseDendriteProcessor.cpp:318-365 on a fixed ring of `expected` offsets.
+__device__ void code_update(SynB& b, uint32_t meta, const NeuronParam& p, uint32_t t, uint16_t* lc,
+                            uint32_t stride, int enabled) {
+    if (!enabled) {
+        b.last_code_match = 0;
+        return;
+    }
+    if (b.code_len == 0 || t - b.code_ws > p.window) {
+        b.code_ws = t;
+        b.code_len = 0;
+    }
+    const uint16_t o = static_cast<uint16_t>(t - b.code_ws);
+    const uint32_t expected = (meta >> kMetaExpectedShift) & 15u;
+    if (b.code_len < expected) {
+        b.ring[b.code_len] = o;
+        b.code_len += 1;
+    } else {
+        for (uint32_t j = 0; j + 1 < expected; ++j) b.ring[j] = b.ring[j + 1];
+        b.ring[expected - 1] = o;
+    }
+    b.last_code_match = 0;
+    if (b.code_len < expected) return;
+    bool match = 0.0f >= p.similarity;
+    unsigned long long cn = 0;
+    for (uint32_t j = 0; j < expected; ++j) cn += static_cast<unsigned long long>(b.ring[j]) * b.ring[j];
+    for (uint32_t i = 0; i < b.learned_count && !match; ++i) {
+        const uint16_t* pat = lc + static_cast<size_t>(i) * stride;
+        unsigned long long dot = 0, rn = 0;
+        for (uint32_t j = 0; j < expected; ++j) {
+            dot += static_cast<unsigned long long>(pat[j]) * b.ring[j];
+            rn += static_cast<unsigned long long>(pat[j]) * pat[j];
+        }
+        match = cos_ge(dot, rn, cn, p.similarity);
+    }
+    if (match) {
+        b.code_matches += 1;
+        b.last_code_match = 1;
+        return;
+    }
+    if (b.learned_count >= p.max_refs) {
+        for (uint32_t i = 1; i < b.learned_count; ++i)
+            for (uint32_t j = 0; j < expected; ++j)
+                lc[static_cast<size_t>(i - 1) * stride + j] = lc[static_cast<size_t>(i) * stride + j];
+        b.learned_count -= 1;
+    }
+    for (uint32_t j = 0; j < expected; ++j) lc[static_cast<size_t>(b.learned_count) * stride + j] = b.ring[j];
+    b.learned_count += 1;
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+// Count due events per target; block 0 first moves far-future injections
+// whose delivery tick t + W - 1 just became addressable into the (empty)
+// slot of that tick.
+__global__ void k_hist(Engine e) {
+    const uint32_t t = e.ts->tick;
+    if (blockIdx.x == 0) {
+        const uint32_t ft = e.ts->far_ticks;
+        if (ft > 0) {
+            const long long rel = static_cast<long long>(t) + e.W - 1 - e.ts->far_first_tick;
+            if (rel >= 0 && rel < ft) {
+                const uint32_t b = e.far_idx[rel], en = e.far_idx[rel + 1];
+                const uint32_t slot = (t + e.W - 1) & e.wmask;
+                const uint32_t base = e.slot_count[slot];
+                if (base + (en - b) > e.slot_cap) {
+                    if (threadIdx.x == 0) raise_status(e, kStatusSlotOverflow);
+                } else {
+                    unsigned long long* dst = e.wheel + static_cast<size_t>(slot) * e.slot_cap + base;
+                    for (uint32_t i = threadIdx.x; i < en - b; i += blockDim.x) dst[i] = e.far_ev[b + i];
+                    __syncthreads();
+                    if (threadIdx.x == 0) e.slot_count[slot] = base + (en - b);
+                }
+            }
+        }
+    }
+    const uint32_t slot = t & e.wmask;
+    const uint32_t n = e.slot_count[slot];
+    const unsigned long long* ev = e.wheel + static_cast<size_t>(slot) * e.slot_cap;
+    uint32_t ext = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t lo = static_cast<uint32_t>(ev[i]);
+        atomicAdd(&e.cnt[lo & ~kExternalBit], 1u);
+        ext += lo >> 31;
+    }
+    ext = __reduce_add_sync(0xffffffffu, ext);
+    if ((threadIdx.x & 31) == 0 && ext) atomicAdd(&e.ts->external, static_cast<unsigned long long>(ext));
+    if (blockIdx.x == 0 && threadIdx.x == 0) e.ts->n_due = n;
+}
+
+// Phase 1 of the per-target scan: tile sums of counts and of touched targets;
+// the last block turns them into exclusive tile bases.
+__global__ void k_scan_tile(Engine e) {
+    const uint32_t tiles = (e.N + kScanTile - 1) / kScanTile;
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        uint32_t sum = 0, nz = 0;
+        const uint32_t base = tile * kScanTile + threadIdx.x * 16;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const uint32_t i = base + j;
+            const uint32_t c = i < e.N ? e.cnt[i] : 0;
+            sum += c;
+            nz += c != 0;
+        }
+        uint32_t ts_sum, ts_nz;
+        block_excl_scan(sum, &ts_sum);
+        block_excl_scan(nz, &ts_nz);
+        if (threadIdx.x == 0) {
+            e.tile_sum[tile] = ts_sum;
+            e.tile_nz[tile] = ts_nz;
+        }
+    }
+    if (last_block(&e.ts->done_scan)) {
+        block_scan_inplace(e.tile_sum, tiles, nullptr);
+        block_scan_inplace(e.tile_nz, tiles, &e.ts->n_touched);
+    }
+}
+
+// Phase 2: per-target segment starts and the ascending touched list.
+__global__ void k_scan_out(Engine e) {
+    const uint32_t tiles = (e.N + kScanTile - 1) / kScanTile;
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const uint32_t base = tile * kScanTile + threadIdx.x * 16;
+        uint32_t c[16];
+        uint32_t sum = 0, nz = 0;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const uint32_t i = base + j;
+            c[j] = i < e.N ? e.cnt[i] : 0;
+            sum += c[j];
+            nz += c[j] != 0;
+        }
+        uint32_t seg = __ldcg(e.tile_sum + tile) + block_excl_scan(sum, nullptr);
+        uint32_t pos = __ldcg(e.tile_nz + tile) + block_excl_scan(nz, nullptr);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const uint32_t i = base + j;
+            if (i < e.N && c[j] != 0) {
+                e.seg_start[i] = seg;
+                e.touched[pos++] = i;
+            }
+            seg += c[j];
+        }
+    }
+}
+
+// Group due events by target: each event takes a position inside its
+// target's segment (counts return to zero for the next tick).
+__global__ void k_scatter(Engine e) {
+    const uint32_t t = e.ts->tick;
+    const uint32_t slot = t & e.wmask;
+    const uint32_t n = e.ts->n_due;
+    const unsigned long long* ev = e.wheel + static_cast<size_t>(slot) * e.slot_cap;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned long long v = ev[i];
+        const uint32_t lo = static_cast<uint32_t>(v);
+        const uint32_t tgt = lo & ~kExternalBit;
+        const uint32_t pos = e.seg_start[tgt] + atomicSub(&e.cnt[tgt], 1u) - 1u;
+        e.grp[pos] = (v & 0xFFFFFFFF00000000ull) | (i | (lo & kExternalBit));
+    }
+}
+
+// One thread per touched target: the reference's sequential per-event loop
+// (NetworkPropagator.cpp:80-131) restricted to this target, which is exact
+// because every state an event reads or writes belongs to its target (the
+// target's neuron state and the target's incoming synapses).  Post-spike
+// STDP of a fire is applied lazily to synapses touched later in the tick
+// and in bulk by k_post for the rest.
+__global__ void __launch_bounds__(kThreads) k_process(Engine e) {
+    const uint32_t t = e.ts->tick;
+    const uint32_t n_touched = e.ts->n_touched;
+    const uint32_t n_due = e.ts->n_due;
+    const int stdp = e.ts->stdp_enabled;
+    const int temporal = e.ts->temporal_enabled;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n_touched; k += gridDim.x * blockDim.x) {
+        const uint32_t n = e.touched[k];
+        const uint32_t beg = e.seg_start[n];
+        const uint32_t end = k + 1 < n_touched ? e.seg_start[e.touched[k + 1]] : n_due;
+        unsigned long long* g = e.grp + beg;
+        const uint32_t len = end - beg;
+        // restore due order (keys are unique due indices)
+        for (uint32_t i = 1; i < len; ++i) {
+            const unsigned long long x = g[i];
+            const uint32_t key = static_cast<uint32_t>(x) & ~kExternalBit;
+            uint32_t j = i;
+            while (j > 0 && (static_cast<uint32_t>(g[j - 1]) & ~kExternalBit) > key) {
+                g[j] = g[j - 1];
+                --j;
+            }
+            g[j] = x;
+        }
+        const NeuronParam p = e.nparam[n];
+        NeuronRec r = e.nrec[n];
+        NeuronTp q = e.ntp[n];
+        NState s;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            s.cur[c] = r.cur[c];
+            s.upd[c] = r.upd[c];
+        }
+        s.flags = r.flags;
+        s.membrane = r.membrane;
+        s.spikes = r.spike_count;
+        s.last_fired1 = r.last_fired1;
+        s.last_active = r.last_active;
+        s.match_count = r.match_count;
+        s.ws = r.ws;
+        s.len = r.len;
+        s.cn = q.cn;
+        s.nruns = q.nruns;
+        s.ref_head = q.ref_head;
+        s.ref_count = q.ref_count;
+        s.ring_head = q.ring_head;
+        s.ring_used = q.ring_used;
+
+        uint32_t fires = 0;
+        for (uint32_t i = 0; i < len; ++i) {
+            const unsigned long long x = g[i];
+            const uint32_t due = static_cast<uint32_t>(x) & ~kExternalBit;
+            const uint32_t payload = static_cast<uint32_t>(x >> 32);
+            bool fired;
+            if (static_cast<uint32_t>(x) & kExternalBit) {
+                fired = process_input(s, p, 0u, 0u, __uint_as_float(payload), t, e, temporal);
+            } else {
+                const uint32_t tm = payload;
+                SynA a = e.syna[tm];
+                SynB b = e.synb[tm];
+                post_catch_up(a, t, fires, e, stdp);
+                const uint32_t delay = a.meta & kMetaDelayMask;
+                const uint32_t pre_tick = t >= delay ? t - delay : t;
+                const bool plastic = (a.meta >> kMetaPlasticBit) & 1u;
+                if (plastic && a.last_post1 != 0) stdp_apply(a, pre_tick, a.last_post1 - 1, e, stdp);
+                a.last_pre1 = pre_tick + 1;
+                b.pre_count += 1;
+                fired = process_input(s, p, (a.meta >> kMetaCompShift) & 3u, (a.meta >> kMetaRecShift) & 3u,
+                                      a.weight, t, e, temporal);
+                uint16_t* lc = e.lcode + p.lcode_base +
+                               static_cast<size_t>(tm - p.in_begin) * p.max_refs * e.code_stride;
+                code_update(b, a.meta, p, t, lc, e.code_stride, temporal);
+                e.syna[tm] = a;
+                e.synb[tm] = b;
+            }
+            if (fired) {
+                fires += 1;
+                atomicOr(&e.fire_bits[due >> 5], 1u << (due & 31));
+                e.fire_at[due] = n;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            r.cur[c] = s.cur[c];
+            r.upd[c] = s.upd[c];
+        }
+        r.flags = s.flags;
+        r.membrane = s.membrane;
+        r.spike_count = s.spikes;
+        r.last_fired1 = s.last_fired1;
+        r.last_active = s.last_active;
+        r.match_count = s.match_count;
+        r.ws = s.ws;
+        r.len = s.len;
+        q.cn = s.cn;
+        q.nruns = s.nruns;
+        q.ref_head = s.ref_head;
+        q.ref_count = s.ref_count;
+        q.ring_head = s.ring_head;
+        q.ring_used = s.ring_used;
+        e.nrec[n] = r;
+        e.ntp[n] = q;
+        if (fires > 0) {
+            const uint32_t j = atomicAdd(&e.ts->n_fired_targets, 1u);
+            e.fired_tgt[j] = n;
+            e.fired_cnt[j] = fires;
+        }
+    }
+}
+
+// Post-spike STDP over the incoming rows of every target that fired
+// (NetworkPropagator.cpp:95-102), one block per fired target, coalesced over
+// the target-major row; then popcounts of the fire bitmap tiles, whose last
+// block turns into exclusive tile bases.
+__global__ void k_post(Engine e) {
+    const uint32_t t = e.ts->tick;
+    const uint32_t nf = e.ts->n_fired_targets;
+    const int stdp = e.ts->stdp_enabled;
+    for (uint32_t j = blockIdx.x; j < nf; j += gridDim.x) {
+        const uint32_t n = e.fired_tgt[j];
+        const uint32_t fires = e.fired_cnt[j];
+        if (fires >= 0x10000u) {
+            if (threadIdx.x == 0) raise_status(e, kStatusPostCountOverflow);
+            continue;
+        }
+        const unsigned long long b = e.in_ptr[n], en = e.in_ptr[n + 1];
+        for (unsigned long long tm = b + threadIdx.x; tm < en; tm += blockDim.x) {
+            SynA a = e.syna[tm];
+            if (post_catch_up(a, t, fires, e, stdp)) e.syna[tm] = a;
+        }
+    }
+    // fire bitmap tile popcounts
+    const uint32_t words = (e.ts->n_due + 31) / 32;
+    const uint32_t tiles = (words + kScanTile - 1) / kScanTile;
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        uint32_t c = 0;
+        const uint32_t base = tile * kScanTile + threadIdx.x * 16;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            const uint32_t w = base + k;
+            c += w < words ? __popc(e.fire_bits[w]) : 0;
+        }
+        uint32_t tot;
+        block_excl_scan(c, &tot);
+        if (threadIdx.x == 0) e.fire_tile[tile] = tot;
+    }
+    if (last_block(&e.ts->done_fire_tile)) {
+        uint32_t total;
+        block_scan_inplace(e.fire_tile, tiles, &total);
+        if (threadIdx.x == 0) e.ts->n_fires = total;
+    }
+}
+
+// Fires in due order.  Each fire's rank r is its position in the reference's
+// fire order; the fire list, the raster and the per-(expansion block, delay
+// class) event counts are written here, the bitmap is cleared.  The last
+// block turns the class counts into destination offsets in the wheel and
+// finishes the tick.
+__global__ void k_fire_list(Engine e) {
+    const uint32_t t = e.ts->tick;
+    const uint32_t words = (e.ts->n_due + 31) / 32;
+    const uint32_t tiles = (words + kScanTile - 1) / kScanTile;
+    const uint32_t nfires = e.ts->n_fires;
+    const unsigned long long raster0 = e.ts->raster_count;
+    const uint32_t D = e.D;
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const uint32_t base = tile * kScanTile + threadIdx.x * 16;
+        uint32_t c = 0;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            const uint32_t w = base + k;
+            c += w < words ? __popc(e.fire_bits[w]) : 0;
+        }
+        uint32_t r = __ldcg(e.fire_tile + tile) + block_excl_scan(c, nullptr);
+        for (int k = 0; k < 16; ++k) {
+            const uint32_t w = base + k;
+            if (w >= words) break;
+            uint32_t bits = e.fire_bits[w];
+            if (bits == 0) continue;
+            e.fire_bits[w] = 0;
+            while (bits) {
+                const uint32_t bit = __ffs(bits) - 1;
+                bits &= bits - 1;
+                const uint32_t due = w * 32 + bit;
+                const uint32_t n = e.fire_at[due];
+                if (r < e.fire_cap) {
+                    e.fire_list[r] = n;
+                    const uint32_t* row = e.pre_off + static_cast<size_t>(n) * (D + 1);
+                    uint32_t* xs = e.xsum + static_cast<size_t>(r / kExpandFires) * D;
+                    for (uint32_t d = 0; d < D; ++d) {
+                        const uint32_t cnt = row[d + 1] - row[d];
+                        if (cnt) atomicAdd(xs + d, cnt);
+                    }
+                }
+                if (e.raster_cap > 0) {
+                    const unsigned long long pos = raster0 + r;
+                    if (pos < e.raster_cap) {
+                        e.raster[2 * pos] = t;
+                        e.raster[2 * pos + 1] = n;
+                    }
+                }
+                r += 1;
+            }
+        }
+    }
+    if (!last_block(&e.ts->done_fire_list)) return;
+    // --- tick finish (single block) ---
+    if (nfires > e.fire_cap && threadIdx.x == 0) raise_status(e, kStatusFireOverflow);
+    const uint32_t nf = nfires < e.fire_cap ? nfires : e.fire_cap;
+    const uint32_t blocks = (nf + kExpandFires - 1) / kExpandFires;
+    // per delay class: exclusive scan over expansion blocks, then absolute
+    // wheel positions; xsum is reset to zero for the next tick.
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (uint32_t d = warp; d < D; d += kThreads / 32) {
+        const uint32_t slot = (t + e.cls_delta[d]) & e.wmask;
+        const uint32_t start = e.slot_count[slot];
+        uint32_t carry = 0;
+        for (uint32_t b0 = 0; b0 < blocks; b0 += 32) {
+            const uint32_t b = b0 + lane;
+            const uint32_t v = b < blocks ? __ldcg(e.xsum + static_cast<size_t>(b) * D + d) : 0;
+            const uint32_t incl = warp_incl_scan(v);
+            if (b < blocks) {
+                e.xdst[static_cast<size_t>(b) * D + d] =
+                    static_cast<unsigned long long>(slot) * e.slot_cap + start + carry + incl - v;
+                e.xsum[static_cast<size_t>(b) * D + d] = 0;
+            }
+            carry += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if (lane == 0) {
+            if (static_cast<unsigned long long>(start) + carry > e.slot_cap) {
+                raise_status(e, kStatusSlotOverflow);
+                e.xdst_ok[d] = 0;
+            } else {
+                e.xdst_ok[d] = 1;
+                e.slot_count[slot] = start + carry;
+            }
+        }
+    }
+    if (threadIdx.x == 0) {
+        TickState* ts = e.ts;
+        const uint32_t due = ts->n_due;
+        ts->delivered += due;
+        ts->fired += nfires;
+        if (due > ts->max_slot_events) ts->max_slot_events = due;
+        if (e.raster_cap > 0) {
+            if (raster0 + nfires > e.raster_cap) raise_status(e, kStatusRasterOverflow);
+            ts->raster_count = raster0 + nfires;
+        }
+        ts->expand_fires = nf;
+        e.slot_count[t & e.wmask] = 0;
+        ts->n_touched = 0;
+        ts->n_fired_targets = 0;
+        ts->tick = t + 1;
+    }
+}
+
+// Spike-code offset expansion (NetworkPropagator.cpp:104-130): one warp per
+// fire copies the fire's pre-expanded events, class by class, to their
+// delivery slots.  Destinations were fixed by k_fire_list, so the wheel ends
+// up in exactly the reference's scheduling order.
+__global__ void __launch_bounds__(kThreads) k_expand(Engine e) {
+    __shared__ uint32_t s_row[kExpandFires][kMaxClasses + 1];
+    __shared__ unsigned long long s_dst[kExpandFires][kMaxClasses];
+    const uint32_t nf = e.ts->expand_fires;
+    const uint32_t blocks = (nf + kExpandFires - 1) / kExpandFires;
+    const uint32_t D = e.D;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (uint32_t blk = blockIdx.x; blk < blocks; blk += gridDim.x) {
+        const uint32_t r = blk * kExpandFires + warp;
+        const bool have = r < nf;
+        const uint32_t n = have ? e.fire_list[r] : 0;
+        if (have) {
+            const uint32_t* row = e.pre_off + static_cast<size_t>(n) * (D + 1);
+            for (uint32_t d = lane; d <= D; d += 32) s_row[warp][d] = row[d];
+        }
+        __syncthreads();
+        // destination of each class for this fire = block base + counts of the
+        // block's earlier fires
+        if (have) {
+            for (uint32_t d = lane; d < D; d += 32) {
+                unsigned long long dst = __ldcg(e.xdst + static_cast<size_t>(blk) * D + d);
+                for (int w = 0; w < warp; ++w) dst += s_row[w][d + 1] - s_row[w][d];
+                s_dst[warp][d] = dst;
+            }
+        }
+        __syncwarp();
+        if (have) {
+            const unsigned long long* src = e.pre_ev + e.pre_base[n];
+            const uint32_t total = s_row[warp][D];
+            for (uint32_t j = lane; j < total; j += 32) {
+                // class of event j: last d with s_row[d] <= j
+                uint32_t lo = 0, hi = D;
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (s_row[warp][mid] <= j) lo = mid; else hi = mid;
+                }
+                if (e.xdst_ok[lo]) e.wheel[s_dst[warp][lo] + (j - s_row[warp][lo])] = src[j];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_inject(Engine e, const unsigned long long* ev, const uint32_t* slot_of_group,
+                         const uint32_t* group_off, uint32_t groups) {
+    for (uint32_t gi = blockIdx.x; gi < groups; gi += gridDim.x) {
+        const uint32_t slot = slot_of_group[gi];
+        const uint32_t b = group_off[gi], en = group_off[gi + 1];
+        const uint32_t base = e.slot_count[slot];
+        if (static_cast<unsigned long long>(base) + (en - b) > e.slot_cap) {
+            if (threadIdx.x == 0) raise_status(e, kStatusSlotOverflow);
+            continue;
+        }
+        unsigned long long* dst = e.wheel + static_cast<size_t>(slot) * e.slot_cap + base;
+        for (uint32_t i = threadIdx.x; i < en - b; i += blockDim.x) dst[i] = ev[b + i];
+        __syncthreads();
+        if (threadIdx.x == 0) e.slot_count[slot] = base + (en - b);
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+void launch_tick(const Engine& e, cudaStream_t stream) {
+    const uint32_t tiles = (e.N + kScanTile - 1) / kScanTile;
+    const uint32_t wide = e.grid_wide;
+    const uint32_t scan_grid = tiles == 0 ? 1 : (tiles < wide ? tiles : wide);
+    k_hist<<<wide, kThreads, 0, stream>>>(e);
+    k_scan_tile<<<scan_grid, kThreads, 0, stream>>>(e);
+    k_scan_out<<<scan_grid, kThreads, 0, stream>>>(e);
+    k_scatter<<<wide, kThreads, 0, stream>>>(e);
+    k_process<<<e.grid_process, kThreads, 0, stream>>>(e);
+    k_post<<<wide, kThreads, 0, stream>>>(e);
+    k_fire_list<<<e.grid_fire, kThreads, 0, stream>>>(e);
+    k_expand<<<wide, kThreads, 0, stream>>>(e);
+}
+
+void launch_inject(const Engine& e, const unsigned long long* ev, const uint32_t* slot_of_group,
+                   const uint32_t* group_off, uint32_t groups, cudaStream_t stream) {
+    if (groups == 0) return;
+    k_inject<<<groups < 1024 ? groups : 1024, kThreads, 0, stream>>>(e, ev, slot_of_group, group_off, groups);
+}
+
+}  // namespace snngb

@@ -1,0 +1,1014 @@
+// Host side of the GB300 engine: the C ABI of include/snncuda_gb300.h.
+//
+// create    packs a flattened Connectome into the device layout of engine.h
+//           (replaces NetworkPropagator's constructor, NetworkPropagator.cpp:5-29
+//           and SynapseDendriteProcessor::initialize_synapse, :59-75)
+// inject    queues external inputs in call order (NetworkPropagator.cpp:31-37)
+// run_until places due injections into the wheel and replays a CUDA graph of
+//           the tick kernels once per tick (NetworkPropagator.cpp:39-43)
+// readers   copy state back and present it with the reference field meaning.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+#include "snncuda_gb300.h"
+
+using namespace snngb;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct Failure {
+    int code;
+    std::string message;
+};
+
+[[noreturn]] void throw_fail(int code, const std::string& msg) { throw Failure{code, msg}; }
+
+void check(cudaError_t err, const char* what) {
+    if (err == cudaSuccess) return;
+    if (err == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        throw_fail(SNNCUDA_ERR_OUT_OF_MEMORY, std::string(what) + ": " + cudaGetErrorString(err));
+    }
+    throw_fail(SNNCUDA_ERR_DEVICE, std::string(what) + ": " + cudaGetErrorString(err));
+}
+
+int set_error(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+constexpr float kTauValue[4] = {5.0F, 100.0F, 10.0F, 150.0F};  // receptor_decay_tau (:245-257)
+
+// exp table entries e = 0.. until std::exp(-e / tau) is 0 for every tau,
+// built with the host libm exactly as the reference evaluates
+// static_cast<float>(current * std::exp(-elapsed / tau)) (:220-221).
+std::vector<float> build_decay_table(uint32_t& len) {
+    uint32_t n = 1;
+    for (float tau : kTauValue) {
+        uint32_t e = 1;
+        while (std::exp(-static_cast<float>(e) / tau) != 0.0F) ++e;
+        n = std::max(n, e + 1);
+    }
+    len = n;
+    std::vector<float> t(4u * n);
+    for (int k = 0; k < 4; ++k)
+        for (uint32_t e = 0; e < n; ++e) t[k * n + e] = std::exp(-static_cast<float>(e) / kTauValue[k]);
+    return t;
+}
+
+// StdpRule::weight_delta (STDP.cpp:25-34) per |post - pre|, until the
+// exponential is 0; the last entry is the value for every larger distance.
+void build_stdp_tables(const snncuda_config& c, std::vector<float>& ltp, std::vector<float>& ltd) {
+    constexpr uint32_t kMax = 1u << 22;
+    uint32_t n = 2;
+    auto zero_at = [](float tau) {
+        uint32_t m = 1;
+        while (m < kMax && std::exp(-static_cast<float>(m) / tau) != 0.0F) ++m;
+        return m;
+    };
+    n = std::max({n, zero_at(c.ltp_tau_ticks) + 1, zero_at(c.ltd_tau_ticks) + 1});
+    if (n > kMax)
+        throw_fail(SNNCUDA_ERR_UNSUPPORTED, "STDP time constant too large for the delta tables");
+    ltp.assign(n, 0.0F);
+    ltd.assign(n, 0.0F);
+    for (uint32_t m = 1; m < n; ++m) {
+        const float dt = static_cast<float>(m);
+        ltp[m] = c.ltp_amplitude * std::exp(-dt / c.ltp_tau_ticks);
+        ltd[m] = -c.ltd_amplitude * std::exp(-dt / c.ltd_tau_ticks);
+    }
+}
+
+struct Digest {
+    uint64_t h{0xcbf29ce484222325ULL};
+    void word(uint64_t w) { h = (h ^ w) * 0x100000001b3ULL; }
+    void f32(float f) {
+        uint32_t b;
+        std::memcpy(&b, &f, 4);
+        word(b);
+    }
+};
+
+struct Pending {
+    uint64_t tick;  // clamped delivery
+    uint64_t event;
+};
+
+template <typename T>
+T* dalloc(std::vector<void*>& owned, size_t count) {
+    void* p = nullptr;
+    if (count == 0) count = 1;
+    check(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc");
+    owned.push_back(p);
+    return static_cast<T*>(p);
+}
+
+}  // namespace
+
+struct snncuda_sim {
+    Engine e{};
+    std::vector<void*> owned;
+    cudaStream_t stream{nullptr};
+    bool own_stream{false};
+    snncuda_config config{};
+    uint32_t N{0};
+    uint64_t S{0};
+    uint64_t next_tick{0};
+    bool poisoned{false};
+    int device{0};
+    std::vector<uint32_t> c_of_tm;     // Connectome index of each target-major slot
+    std::vector<uint32_t> tm_of_c;     // target-major slot of each Connectome index
+    std::vector<uint64_t> in_ptr;      // host copy of the row pointers
+    std::vector<NeuronParam> nparam;   // host copy
+    std::vector<Pending> pending;      // queued injections, call order
+    // far-future buffers (stable addresses while a graph uses them)
+    unsigned long long* far_ev{nullptr};
+    uint32_t* far_idx{nullptr};
+    size_t far_ev_cap{0}, far_idx_cap{0};
+    // injection staging
+    unsigned long long* inj_ev{nullptr};
+    uint32_t* inj_slot{nullptr};
+    uint32_t* inj_off{nullptr};
+    size_t inj_cap{0}, inj_groups_cap{0};
+    // graphs
+    cudaGraphExec_t graph_many{nullptr};
+    cudaGraphExec_t graph_one{nullptr};
+    static constexpr int kTicksPerGraph = 16;
+
+    ~snncuda_sim() {
+        if (graph_many) cudaGraphExecDestroy(graph_many);
+        if (graph_one) cudaGraphExecDestroy(graph_one);
+        if (stream) cudaStreamSynchronize(stream);
+        for (void* p : owned) cudaFree(p);
+        if (far_ev) cudaFree(far_ev);
+        if (far_idx) cudaFree(far_idx);
+        if (inj_ev) cudaFree(inj_ev);
+        if (inj_slot) cudaFree(inj_slot);
+        if (inj_off) cudaFree(inj_off);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+
+    void drop_graphs() {
+        if (graph_many) cudaGraphExecDestroy(graph_many);
+        if (graph_one) cudaGraphExecDestroy(graph_one);
+        graph_many = graph_one = nullptr;
+    }
+
+    cudaGraphExec_t capture(int ticks) {
+        cudaGraph_t g = nullptr;
+        check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        for (int i = 0; i < ticks; ++i) launch_tick(e, stream);
+        check(cudaStreamEndCapture(stream, &g), "end capture");
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t err = cudaGraphInstantiate(&exec, g, 0);
+        cudaGraphDestroy(g);
+        check(err, "graph instantiate");
+        return exec;
+    }
+
+    void ensure_far(size_t events, size_t idx) {
+        if (events > far_ev_cap) {
+            if (far_ev) cudaFree(far_ev);
+            far_ev = nullptr;
+            far_ev_cap = std::max<size_t>(events, 2 * far_ev_cap);
+            check(cudaMalloc(&far_ev, far_ev_cap * sizeof(unsigned long long)), "far events");
+            drop_graphs();
+        }
+        if (idx > far_idx_cap) {
+            if (far_idx) cudaFree(far_idx);
+            far_idx = nullptr;
+            far_idx_cap = std::max<size_t>(idx, 2 * far_idx_cap);
+            check(cudaMalloc(&far_idx, far_idx_cap * sizeof(uint32_t)), "far index");
+            drop_graphs();
+        }
+        e.far_ev = far_ev;
+        e.far_idx = far_idx;
+    }
+
+    void ensure_inject(size_t events, size_t groups) {
+        if (events > inj_cap) {
+            if (inj_ev) cudaFree(inj_ev);
+            inj_ev = nullptr;
+            inj_cap = std::max<size_t>(events, 2 * inj_cap);
+            check(cudaMalloc(&inj_ev, inj_cap * sizeof(unsigned long long)), "inject events");
+        }
+        if (groups + 1 > inj_groups_cap) {
+            if (inj_slot) cudaFree(inj_slot);
+            if (inj_off) cudaFree(inj_off);
+            inj_slot = nullptr;
+            inj_off = nullptr;
+            inj_groups_cap = std::max<size_t>(groups + 1, 2 * inj_groups_cap);
+            check(cudaMalloc(&inj_slot, inj_groups_cap * sizeof(uint32_t)), "inject slots");
+            check(cudaMalloc(&inj_off, inj_groups_cap * sizeof(uint32_t)), "inject offsets");
+        }
+    }
+
+    TickState read_ts() {
+        TickState ts;
+        check(cudaMemcpyAsync(&ts, e.ts, sizeof(ts), cudaMemcpyDeviceToHost, stream), "read tick state");
+        check(cudaStreamSynchronize(stream), "synchronize");
+        return ts;
+    }
+
+    template <typename T>
+    std::vector<T> d2h(const T* src, size_t count) {
+        std::vector<T> v(count);
+        if (count) {
+            check(cudaMemcpyAsync(v.data(), src, count * sizeof(T), cudaMemcpyDeviceToHost, stream), "copy back");
+            check(cudaStreamSynchronize(stream), "synchronize");
+        }
+        return v;
+    }
+};
+
+namespace {
+
+void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_sim* sim) {
+    const uint32_t N = net->neuron_count;
+    const uint64_t S = net->synapse_count;
+    if (cfg.timing_wheel_slots == 0)
+        throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "Spike scheduler timing wheel must have at least one slot");
+    if (N >= (1u << 31)) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "at most 2^31-1 neurons");
+    if (S >= 0xFFFFFFFFull) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "at most 2^32-2 synapses per simulation");
+    if (N > 0 && (!net->threshold || !net->pattern_window_ticks || !net->similarity_threshold ||
+                  !net->max_reference_patterns))
+        throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "neuron parameter arrays are required");
+    if (S > 0 && (!net->source || !net->target || !net->weight || !net->max_weight || !net->delay_ticks ||
+                  !net->compartment || !net->receptor || !net->plasticity_enabled))
+        throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "synapse arrays are required");
+    const bool has_codes = net->code_offset_ptr != nullptr && net->code_offsets != nullptr;
+
+    check(cudaGetDevice(&sim->device), "cudaGetDevice");
+    if (cfg.cuda_stream != nullptr) {
+        sim->stream = static_cast<cudaStream_t>(cfg.cuda_stream);
+    } else {
+        check(cudaStreamCreateWithFlags(&sim->stream, cudaStreamNonBlocking), "stream");
+        sim->own_stream = true;
+    }
+    sim->N = N;
+    sim->S = S;
+    sim->config = cfg;
+    Engine& e = sim->e;
+    e.N = N;
+    e.S = S;
+    e.min_weight = cfg.min_weight;
+
+    // ---- validation + target-major order (stable in Connectome order) ----
+    std::vector<uint64_t> in_ptr(static_cast<size_t>(N) + 1, 0);
+    uint32_t max_expected = 2;
+    for (uint64_t s = 0; s < S; ++s) {
+        if (net->source[s] >= N || net->target[s] >= N)
+            throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "synapse endpoint out of range");
+        if (net->compartment[s] > 3 || net->receptor[s] > 3)
+            throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "compartment/receptor out of range");
+        if (net->delay_ticks[s] > kMetaDelayMask)
+            throw_fail(SNNCUDA_ERR_UNSUPPORTED, "delays above 65535 ticks are not supported");
+        const uint64_t k = has_codes ? net->code_offset_ptr[s + 1] - net->code_offset_ptr[s] : 1;
+        if (k > static_cast<uint64_t>(kMaxExpected))
+            throw_fail(SNNCUDA_ERR_UNSUPPORTED, "more than 8 spike-code offsets per synapse");
+        max_expected = std::max<uint32_t>(max_expected, static_cast<uint32_t>(std::max<uint64_t>(2, k)));
+        in_ptr[net->target[s] + 1] += 1;
+    }
+    for (uint32_t n = 0; n < N; ++n) in_ptr[n + 1] += in_ptr[n];
+    std::vector<uint32_t> tm_of_c(S);
+    sim->c_of_tm.assign(S, 0);
+    {
+        std::vector<uint64_t> cursor(in_ptr.begin(), in_ptr.end() - 1);
+        for (uint64_t s = 0; s < S; ++s) {
+            const uint64_t tm = cursor[net->target[s]]++;
+            tm_of_c[s] = static_cast<uint32_t>(tm);
+            sim->c_of_tm[tm] = static_cast<uint32_t>(s);
+        }
+    }
+    e.code_stride = max_expected;
+    sim->tm_of_c = tm_of_c;
+
+    // ---- neuron parameters and temporal storage ----
+    sim->nparam.resize(N);
+    uint64_t cand_total = 0, meta_total = 0, ring_total = 0, lcode_total = 0;
+    const uint64_t run_budget = cfg.pattern_run_capacity ? cfg.pattern_run_capacity : 4096;
+    for (uint32_t n = 0; n < N; ++n) {
+        NeuronParam& p = sim->nparam[n];
+        std::memset(&p, 0, sizeof(p));
+        const uint64_t window = net->pattern_window_ticks[n];
+        const uint64_t refs = net->max_reference_patterns[n];
+        if (refs == 0) throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "max_reference_patterns must be >= 1");
+        if (window > 0xFFFE) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "pattern windows above 65534 ticks");
+        if (refs > 0xFFFF) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "more than 65535 reference patterns");
+        p.threshold = net->threshold[n];
+        p.window = static_cast<uint32_t>(window);
+        p.similarity = net->similarity_threshold[n];
+        p.max_refs = static_cast<uint32_t>(refs);
+        const uint64_t full = refs * (window + 1);
+        p.ring_cap = static_cast<uint32_t>(std::min<uint64_t>(full, std::max<uint64_t>(window + 1, run_budget)));
+        p.in_begin = in_ptr[n];
+        p.cand_base = cand_total;
+        cand_total += window + 1;
+        p.meta_base = meta_total;
+        meta_total += refs;
+        p.ring_base = ring_total;
+        ring_total += p.ring_cap;
+        p.lcode_base = lcode_total;
+        lcode_total += (in_ptr[n + 1] - in_ptr[n]) * refs * max_expected;
+    }
+
+    // ---- synapse records, target-major ----
+    std::vector<SynA> syna(S);
+    for (uint64_t s = 0; s < S; ++s) {
+        SynA& a = syna[tm_of_c[s]];
+        a.weight = net->weight[s];
+        a.last_pre1 = 0;
+        a.last_post1 = 0;
+        const uint64_t k = has_codes ? net->code_offset_ptr[s + 1] - net->code_offset_ptr[s] : 1;
+        const uint32_t expected = static_cast<uint32_t>(std::max<uint64_t>(2, k == 0 ? 1 : k));
+        a.meta = net->delay_ticks[s] | (static_cast<uint32_t>(net->compartment[s]) << kMetaCompShift) |
+                 (static_cast<uint32_t>(net->receptor[s]) << kMetaRecShift) |
+                 (static_cast<uint32_t>(net->plasticity_enabled[s] ? 1 : 0) << kMetaPlasticBit) |
+                 (expected << kMetaExpectedShift);
+        // std::min(config.max_weight, synapse.max_weight) (STDP.cpp:38)
+        a.clamp_hi = net->max_weight[s] < cfg.max_weight ? net->max_weight[s] : cfg.max_weight;
+        a.updates = 0;
+        a.last_delta = 0.0F;
+        a.post_cnt = 0;
+    }
+
+    // ---- pre-expanded outgoing events, grouped by delivery delay class ----
+    // delivery = tick + delay + offset, clamped to tick + 1 (SpikeScheduler.cpp:17-19)
+    std::vector<uint64_t> out_ptr(static_cast<size_t>(N) + 1, 0);
+    for (uint64_t s = 0; s < S; ++s) out_ptr[net->source[s] + 1] += 1;
+    for (uint32_t n = 0; n < N; ++n) out_ptr[n + 1] += out_ptr[n];
+    std::vector<uint64_t> out_list(S);
+    {
+        std::vector<uint64_t> cursor(out_ptr.begin(), out_ptr.end() - 1);
+        for (uint64_t s = 0; s < S; ++s) out_list[cursor[net->source[s]]++] = s;
+    }
+    auto codes_of = [&](uint64_t s, const uint32_t*& ptr, uint64_t& count) {
+        static const uint32_t zero = 0;
+        if (has_codes && net->code_offset_ptr[s + 1] > net->code_offset_ptr[s]) {
+            ptr = net->code_offsets + net->code_offset_ptr[s];
+            count = net->code_offset_ptr[s + 1] - net->code_offset_ptr[s];
+        } else {
+            ptr = &zero;
+            count = 1;
+        }
+    };
+    std::map<uint64_t, uint32_t> class_of;
+    uint64_t pre_total = 0;
+    for (uint64_t s = 0; s < S; ++s) {
+        const uint32_t* c;
+        uint64_t k;
+        codes_of(s, c, k);
+        for (uint64_t j = 0; j < k; ++j) {
+            const uint64_t d = std::max<uint64_t>(1, static_cast<uint64_t>(net->delay_ticks[s]) + c[j]);
+            class_of.emplace(d, 0);
+        }
+        pre_total += k;
+    }
+    if (class_of.size() > kMaxClasses)
+        throw_fail(SNNCUDA_ERR_UNSUPPORTED, "more than 256 distinct delivery delays");
+    const uint32_t D = static_cast<uint32_t>(class_of.size());
+    std::vector<uint32_t> cls_delta;
+    for (auto& kv : class_of) {
+        kv.second = static_cast<uint32_t>(cls_delta.size());
+        cls_delta.push_back(static_cast<uint32_t>(kv.first));
+    }
+    const uint64_t max_delta = cls_delta.empty() ? 1 : cls_delta.back();
+    uint32_t W = 2;
+    while (W <= max_delta) W <<= 1;
+    if (W > (1u << 20)) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "delivery delays above 2^20 ticks");
+    e.W = W;
+    e.wmask = W - 1;
+    e.D = D;
+    std::vector<unsigned long long> pre_base(N);
+    std::vector<uint32_t> pre_off(static_cast<size_t>(N) * (D + 1), 0);
+    std::vector<unsigned long long> pre_ev(pre_total > 0 ? pre_total : 1);
+    {
+        uint64_t pos = 0;
+        std::vector<uint32_t> cnt(D + 1);
+        for (uint32_t n = 0; n < N; ++n) {
+            pre_base[n] = pos;
+            std::fill(cnt.begin(), cnt.end(), 0);
+            for (uint64_t i = out_ptr[n]; i < out_ptr[n + 1]; ++i) {
+                const uint64_t s = out_list[i];
+                const uint32_t* c;
+                uint64_t k;
+                codes_of(s, c, k);
+                for (uint64_t j = 0; j < k; ++j)
+                    cnt[class_of[std::max<uint64_t>(1, static_cast<uint64_t>(net->delay_ticks[s]) + c[j])] + 1] += 1;
+            }
+            uint32_t* row = &pre_off[static_cast<size_t>(n) * (D + 1)];
+            for (uint32_t d = 0; d < D; ++d) row[d + 1] = row[d] + cnt[d + 1];
+            if (row[D] >= (1u << 30)) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "too many outgoing events per neuron");
+            std::vector<uint32_t> fill(row, row + D);
+            for (uint64_t i = out_ptr[n]; i < out_ptr[n + 1]; ++i) {
+                const uint64_t s = out_list[i];
+                const uint32_t* c;
+                uint64_t k;
+                codes_of(s, c, k);
+                for (uint64_t j = 0; j < k; ++j) {
+                    const uint32_t cls =
+                        class_of[std::max<uint64_t>(1, static_cast<uint64_t>(net->delay_ticks[s]) + c[j])];
+                    pre_ev[pos + fill[cls]++] =
+                        (static_cast<unsigned long long>(tm_of_c[s]) << 32) | net->target[s];
+                }
+            }
+            pos += row[D];
+        }
+    }
+
+    // ---- capacities ----
+    uint64_t slot_cap = cfg.slot_event_capacity;
+    if (slot_cap == 0) slot_cap = std::min<uint64_t>(1ull << 27, std::max<uint64_t>(1ull << 16, pre_total / 8));
+    if (slot_cap >= (1ull << 31)) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "slot capacity must be below 2^31");
+    slot_cap = (slot_cap + 31) & ~31ull;
+    e.slot_cap = slot_cap;
+    const uint64_t fire_cap = std::min<uint64_t>(slot_cap, std::max<uint64_t>(65536, 4ull * N));
+    e.fire_cap = static_cast<uint32_t>(fire_cap);
+    e.raster_cap = cfg.raster_capacity;
+    const uint64_t xblocks = (fire_cap + kExpandFires - 1) / kExpandFires;
+    const uint64_t bit_words = slot_cap / 32;
+    const uint64_t fire_tiles = (bit_words + kScanTile - 1) / kScanTile;
+    e.fire_tiles_cap = static_cast<uint32_t>(fire_tiles);
+
+    // ---- tables ----
+    uint32_t decay_len = 0;
+    const std::vector<float> decay = build_decay_table(decay_len);
+    std::vector<float> ltp, ltd;
+    build_stdp_tables(cfg, ltp, ltd);
+
+    // ---- device allocation ----
+    auto& own = sim->owned;
+    auto* d_in_ptr = dalloc<unsigned long long>(own, N + 1);
+    auto* d_nparam = dalloc<NeuronParam>(own, N);
+    e.nrec = dalloc<NeuronRec>(own, N);
+    e.ntp = dalloc<NeuronTp>(own, N);
+    e.cand = dalloc<unsigned long long>(own, cand_total);
+    e.refmeta = dalloc<RefMeta>(own, meta_total);
+    e.ring = dalloc<unsigned long long>(own, ring_total);
+    e.syna = dalloc<SynA>(own, S);
+    e.synb = dalloc<SynB>(own, S);
+    e.lcode = dalloc<uint16_t>(own, lcode_total);
+    auto* d_pre_base = dalloc<unsigned long long>(own, N);
+    auto* d_pre_off = dalloc<uint32_t>(own, static_cast<size_t>(N) * (D + 1));
+    auto* d_pre_ev = dalloc<unsigned long long>(own, pre_ev.size());
+    auto* d_cls = dalloc<uint32_t>(own, D);
+    e.wheel = dalloc<unsigned long long>(own, static_cast<size_t>(W) * slot_cap);
+    e.slot_count = dalloc<uint32_t>(own, W);
+    e.cnt = dalloc<uint32_t>(own, N);
+    e.seg_start = dalloc<uint32_t>(own, N);
+    const uint32_t scan_tiles = (N + kScanTile - 1) / kScanTile;
+    e.tile_sum = dalloc<uint32_t>(own, scan_tiles + 2);
+    e.tile_nz = dalloc<uint32_t>(own, scan_tiles + 2);
+    e.touched = dalloc<uint32_t>(own, N);
+    e.grp = dalloc<unsigned long long>(own, slot_cap);
+    e.fire_bits = dalloc<uint32_t>(own, bit_words);
+    e.fire_at = dalloc<uint32_t>(own, slot_cap);
+    e.fire_tile = dalloc<uint32_t>(own, fire_tiles + 2);
+    e.fire_list = dalloc<uint32_t>(own, fire_cap);
+    e.fired_tgt = dalloc<uint32_t>(own, N);
+    e.fired_cnt = dalloc<uint32_t>(own, N);
+    e.xsum = dalloc<uint32_t>(own, xblocks * std::max<uint32_t>(D, 1));
+    e.xdst = dalloc<unsigned long long>(own, xblocks * std::max<uint32_t>(D, 1));
+    e.xdst_ok = dalloc<uint32_t>(own, std::max<uint32_t>(D, 1));
+    e.raster = dalloc<uint32_t>(own, cfg.raster_capacity > 0 ? 2 * cfg.raster_capacity : 1);
+    e.ts = dalloc<TickState>(own, 1);
+    auto* d_decay = dalloc<float>(own, decay.size());
+    auto* d_ltp = dalloc<float>(own, ltp.size());
+    auto* d_ltd = dalloc<float>(own, ltd.size());
+
+    cudaStream_t st = sim->stream;
+    auto h2d = [&](void* dst, const void* src, size_t bytes) {
+        if (bytes) check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st), "copy to device");
+    };
+    auto zero = [&](void* dst, size_t bytes) {
+        if (bytes) check(cudaMemsetAsync(dst, 0, bytes, st), "memset");
+    };
+    h2d(d_in_ptr, in_ptr.data(), in_ptr.size() * sizeof(uint64_t));
+    h2d(d_nparam, sim->nparam.data(), sim->nparam.size() * sizeof(NeuronParam));
+    // NeuronState defaults (NeuronStateCache.h:15-45): every compartment tau 5 (code 0).
+    zero(e.nrec, sizeof(NeuronRec) * N);
+    zero(e.ntp, sizeof(NeuronTp) * N);
+    h2d(e.syna, syna.data(), syna.size() * sizeof(SynA));
+    zero(e.synb, sizeof(SynB) * S);
+    zero(e.lcode, sizeof(uint16_t) * lcode_total);
+    h2d(d_pre_base, pre_base.data(), pre_base.size() * sizeof(unsigned long long));
+    h2d(d_pre_off, pre_off.data(), pre_off.size() * sizeof(uint32_t));
+    h2d(d_pre_ev, pre_ev.data(), pre_ev.size() * sizeof(unsigned long long));
+    h2d(d_cls, cls_delta.data(), cls_delta.size() * sizeof(uint32_t));
+    zero(e.slot_count, sizeof(uint32_t) * W);
+    zero(e.cnt, sizeof(uint32_t) * N);
+    zero(e.fire_bits, sizeof(uint32_t) * bit_words);
+    zero(e.xsum, sizeof(uint32_t) * xblocks * std::max<uint32_t>(D, 1));
+    zero(e.tile_sum, sizeof(uint32_t) * (scan_tiles + 2));
+    zero(e.fire_tile, sizeof(uint32_t) * (fire_tiles + 2));
+    h2d(d_decay, decay.data(), decay.size() * sizeof(float));
+    h2d(d_ltp, ltp.data(), ltp.size() * sizeof(float));
+    h2d(d_ltd, ltd.data(), ltd.size() * sizeof(float));
+    TickState ts{};
+    ts.stdp_enabled = cfg.stdp_enabled ? 1 : 0;
+    ts.temporal_enabled = cfg.temporal_learning_enabled ? 1 : 0;
+    h2d(e.ts, &ts, sizeof(ts));
+    e.in_ptr = d_in_ptr;
+    e.nparam = d_nparam;
+    e.pre_base = d_pre_base;
+    e.pre_off = d_pre_off;
+    e.pre_ev = d_pre_ev;
+    e.cls_delta = d_cls;
+    e.tab.decay = d_decay;
+    e.tab.decay_len = decay_len;
+    e.tab.ltp = d_ltp;
+    e.tab.ltd = d_ltd;
+    e.tab.stdp_len = static_cast<uint32_t>(ltp.size());
+    sim->in_ptr = std::move(in_ptr);
+
+    int sms = 0;
+    check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sim->device), "device attribute");
+    e.grid_wide = static_cast<uint32_t>(std::max(1, sms * 2));
+    e.grid_process = static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>((N + 255) / 256, sms * 8ull)));
+    e.grid_fire = static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>(fire_tiles, sms * 2ull)));
+    sim->ensure_far(1, 2);
+    check(cudaStreamSynchronize(st), "create synchronize");
+}
+
+int status_to_error(uint32_t status, std::string& msg) {
+    msg.clear();
+    if (status & kStatusSlotOverflow) msg += "wheel slot capacity exceeded (raise slot_event_capacity); ";
+    if (status & kStatusRingOverflow) msg += "learned-pattern run storage exceeded (raise pattern_run_capacity); ";
+    if (status & kStatusRasterOverflow) msg += "raster capacity exceeded; ";
+    if (status & kStatusPostCountOverflow) msg += "a neuron fired 65536+ times in one tick; ";
+    if (status & kStatusRunOverflow) msg += "temporal run list overflow; ";
+    if (status & kStatusFireOverflow) msg += "fires per tick exceeded the fire capacity; ";
+    return SNNCUDA_ERR_CAPACITY;
+}
+
+void run_impl(snncuda_sim* sim, uint64_t T) {
+    const uint64_t p = sim->next_tick;
+    if (T < p) return;
+    if (T >= 0xFFFF0000ull) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "ticks beyond 2^32 - 2^16");
+    Engine& e = sim->e;
+    const uint64_t W = e.W;
+    // Injections in (delivery, call order).  Those due within W ticks go into
+    // their slots now, behind everything scheduled before this call; later
+    // ones are moved in by k_hist the tick their slot frees up; the rest wait.
+    std::stable_sort(sim->pending.begin(), sim->pending.end(),
+                     [](const Pending& a, const Pending& b) { return a.tick < b.tick; });
+    size_t a_end = 0;
+    while (a_end < sim->pending.size() && sim->pending[a_end].tick < p + W) ++a_end;
+    size_t b_end = a_end;
+    while (b_end < sim->pending.size() && sim->pending[b_end].tick <= T + W - 1) ++b_end;
+    cudaStream_t st = sim->stream;
+    if (a_end > 0) {
+        std::vector<unsigned long long> ev(a_end);
+        std::vector<uint32_t> slots, offs;
+        for (size_t i = 0; i < a_end; ++i) {
+            ev[i] = sim->pending[i].event;
+            const uint32_t slot = static_cast<uint32_t>(sim->pending[i].tick & (W - 1));
+            if (i == 0 || sim->pending[i].tick != sim->pending[i - 1].tick) {
+                slots.push_back(slot);
+                offs.push_back(static_cast<uint32_t>(i));
+            }
+        }
+        offs.push_back(static_cast<uint32_t>(a_end));
+        sim->ensure_inject(a_end, slots.size());
+        check(cudaMemcpyAsync(sim->inj_ev, ev.data(), a_end * 8, cudaMemcpyHostToDevice, st), "inject copy");
+        check(cudaMemcpyAsync(sim->inj_slot, slots.data(), slots.size() * 4, cudaMemcpyHostToDevice, st), "inject copy");
+        check(cudaMemcpyAsync(sim->inj_off, offs.data(), offs.size() * 4, cudaMemcpyHostToDevice, st), "inject copy");
+        launch_inject(e, sim->inj_ev, sim->inj_slot, sim->inj_off, static_cast<uint32_t>(slots.size()), st);
+        check(cudaGetLastError(), "inject launch");
+        check(cudaStreamSynchronize(st), "inject synchronize");
+    }
+    uint32_t far_first = static_cast<uint32_t>(p + W);
+    uint32_t far_ticks = 0;
+    if (b_end > a_end) {
+        far_ticks = static_cast<uint32_t>(T + W - 1 - (p + W) + 1);  // deliveries p+W .. T+W-1
+        const size_t n = b_end - a_end;
+        sim->ensure_far(n, static_cast<size_t>(far_ticks) + 1);
+        std::vector<unsigned long long> ev(n);
+        std::vector<uint32_t> idx(static_cast<size_t>(far_ticks) + 1, 0);
+        for (size_t i = 0; i < n; ++i) {
+            const Pending& q = sim->pending[a_end + i];
+            ev[i] = q.event;
+            idx[q.tick - far_first + 1] += 1;
+        }
+        for (size_t i = 1; i < idx.size(); ++i) idx[i] += idx[i - 1];
+        check(cudaMemcpyAsync(sim->far_ev, ev.data(), n * 8, cudaMemcpyHostToDevice, st), "far copy");
+        check(cudaMemcpyAsync(sim->far_idx, idx.data(), idx.size() * 4, cudaMemcpyHostToDevice, st), "far copy");
+    }
+    sim->pending.erase(sim->pending.begin(), sim->pending.begin() + static_cast<std::ptrdiff_t>(b_end));
+    // run parameters live in device memory so the captured graphs stay valid
+    check(cudaMemcpyAsync(reinterpret_cast<char*>(e.ts) + offsetof(TickState, far_first_tick), &far_first, 4,
+                          cudaMemcpyHostToDevice, st), "run params");
+    check(cudaMemcpyAsync(reinterpret_cast<char*>(e.ts) + offsetof(TickState, far_ticks), &far_ticks, 4,
+                          cudaMemcpyHostToDevice, st), "run params");
+    uint64_t ticks = T - p + 1;
+    if (ticks >= static_cast<uint64_t>(snncuda_sim::kTicksPerGraph) && sim->graph_many == nullptr)
+        sim->graph_many = sim->capture(snncuda_sim::kTicksPerGraph);
+    if (sim->graph_one == nullptr) sim->graph_one = sim->capture(1);
+    while (ticks >= static_cast<uint64_t>(snncuda_sim::kTicksPerGraph)) {
+        check(cudaGraphLaunch(sim->graph_many, st), "graph launch");
+        ticks -= snncuda_sim::kTicksPerGraph;
+    }
+    while (ticks > 0) {
+        check(cudaGraphLaunch(sim->graph_one, st), "graph launch");
+        ticks -= 1;
+    }
+    const uint32_t zero = 0;
+    check(cudaMemcpyAsync(reinterpret_cast<char*>(e.ts) + offsetof(TickState, far_ticks), &zero, 4,
+                          cudaMemcpyHostToDevice, st), "run params");
+    const TickState ts = sim->read_ts();
+    sim->next_tick = T + 1;
+    if (ts.tick != static_cast<uint32_t>(T + 1)) throw_fail(SNNCUDA_ERR_DEVICE, "device tick counter out of step");
+    if (ts.status != 0) {
+        sim->poisoned = true;
+        std::string msg;
+        const int code = status_to_error(ts.status, msg);
+        throw_fail(code, msg);
+    }
+}
+
+// Rebuild the offsets of a run list.
+void expand_runs(const unsigned long long* runs, uint32_t nruns, uint32_t cap, uint32_t start, uint64_t limit,
+                 std::vector<uint32_t>& out) {
+    out.clear();
+    for (uint32_t j = 0; j < nruns && out.size() < limit; ++j) {
+        const unsigned long long r = runs[(start + j) % cap];
+        for (unsigned long long c = 0; c < run_count(r) && out.size() < limit; ++c) out.push_back(run_value(r));
+    }
+}
+
+struct HostState {
+    std::vector<NeuronRec> nrec;
+    std::vector<NeuronTp> ntp;
+    std::vector<unsigned long long> cand, ring;
+    std::vector<RefMeta> meta;
+    std::vector<SynA> syna;
+    std::vector<SynB> synb;
+    std::vector<uint16_t> lcode;
+};
+
+void neuron_offsets(const snncuda_sim* sim, const HostState& h, uint32_t n, std::vector<uint32_t>& out) {
+    const NeuronParam& p = sim->nparam[n];
+    expand_runs(h.cand.data() + p.cand_base, h.ntp[n].nruns, p.window + 1, 0, h.nrec[n].len, out);
+}
+
+void neuron_learned(const snncuda_sim* sim, const HostState& h, uint32_t n, uint32_t which, std::vector<uint32_t>& out) {
+    const NeuronParam& p = sim->nparam[n];
+    const RefMeta& m = h.meta[p.meta_base + (h.ntp[n].ref_head + which) % p.max_refs];
+    expand_runs(h.ring.data() + p.ring_base, m.nruns, p.ring_cap, m.start, m.len, out);
+}
+
+uint32_t expected_of(const SynA& a) { return (a.meta >> kMetaExpectedShift) & 15u; }
+
+void synapse_learned(const snncuda_sim* sim, const HostState& h, uint64_t tm, uint32_t which, std::vector<uint32_t>& out) {
+    const uint32_t n = static_cast<uint32_t>(std::upper_bound(sim->in_ptr.begin(), sim->in_ptr.end(), tm) -
+                                             sim->in_ptr.begin() - 1);
+    const NeuronParam& p = sim->nparam[n];
+    const uint16_t* lc = h.lcode.data() + p.lcode_base + (tm - p.in_begin) * p.max_refs * sim->e.code_stride +
+                         static_cast<size_t>(which) * sim->e.code_stride;
+    out.assign(lc, lc + expected_of(h.syna[tm]));
+}
+
+HostState fetch_all(snncuda_sim* sim, bool temporal) {
+    HostState h;
+    Engine& e = sim->e;
+    h.nrec = sim->d2h(e.nrec, sim->N);
+    h.ntp = sim->d2h(e.ntp, sim->N);
+    h.syna = sim->d2h(e.syna, sim->S);
+    h.synb = sim->d2h(e.synb, sim->S);
+    if (temporal) {
+        uint64_t cand = 0, ring = 0, meta = 0, lcode = 0;
+        for (uint32_t n = 0; n < sim->N; ++n) {
+            const NeuronParam& p = sim->nparam[n];
+            cand += p.window + 1;
+            ring += p.ring_cap;
+            meta += p.max_refs;
+            lcode += (sim->in_ptr[n + 1] - sim->in_ptr[n]) * p.max_refs * e.code_stride;
+        }
+        h.cand = sim->d2h(e.cand, cand);
+        h.ring = sim->d2h(e.ring, ring);
+        h.meta = sim->d2h(e.refmeta, meta);
+        h.lcode = sim->d2h(e.lcode, lcode);
+    }
+    return h;
+}
+
+template <typename F>
+int guarded(F&& body) {
+    try {
+        body();
+        return SNNCUDA_OK;
+    } catch (const Failure& f) {
+        return set_error(f.code, f.message);
+    } catch (const std::bad_alloc&) {
+        return set_error(SNNCUDA_ERR_OUT_OF_MEMORY, "host allocation failed");
+    } catch (const std::exception& ex) {
+        return set_error(SNNCUDA_ERR_DEVICE, ex.what());
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* snncuda_version(void) { return "0.1.0-gb300"; }
+
+int snncuda_cuda_available(void) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return count > 0 ? 1 : 0;
+}
+
+const char* snncuda_last_error(void) { return g_last_error.c_str(); }
+
+void snncuda_config_default(snncuda_config* c) {
+    if (c == nullptr) return;
+    std::memset(c, 0, sizeof(*c));
+    c->stdp_enabled = 1;
+    c->ltp_amplitude = 0.01F;
+    c->ltd_amplitude = 0.012F;
+    c->ltp_tau_ticks = 20.0F;
+    c->ltd_tau_ticks = 20.0F;
+    c->min_weight = 0.0F;
+    c->max_weight = 2.0F;
+    c->temporal_learning_enabled = 1;
+    c->timing_wheel_slots = 4096;
+}
+
+int snncuda_sim_create(const snncuda_network* net, const snncuda_config* config, snncuda_sim** out) {
+    if (net == nullptr || out == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
+    snncuda_config def;
+    snncuda_config_default(&def);
+    const snncuda_config& cfg = config ? *config : def;
+    snncuda_sim* sim = nullptr;
+    try {
+        sim = new snncuda_sim();
+    } catch (const std::bad_alloc&) {
+        return set_error(SNNCUDA_ERR_OUT_OF_MEMORY, "host allocation failed");
+    }
+    const int rc = guarded([&] { create_impl(net, cfg, sim); });
+    if (rc != SNNCUDA_OK) {
+        delete sim;
+        return rc;
+    }
+    *out = sim;
+    return SNNCUDA_OK;
+}
+
+int snncuda_sim_destroy(snncuda_sim* sim) {
+    delete sim;
+    return SNNCUDA_OK;
+}
+
+int snncuda_sim_inject(snncuda_sim* sim, uint64_t count, const uint32_t* neurons, const uint64_t* ticks,
+                       const float* weights) {
+    if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
+    if (count > 0 && (!neurons || !ticks || !weights)) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null array");
+    for (uint64_t i = 0; i < count; ++i)
+        if (neurons[i] >= sim->N) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "inject neuron out of range");
+    return guarded([&] {
+        sim->pending.reserve(sim->pending.size() + count);
+        for (uint64_t i = 0; i < count; ++i) {
+            const uint64_t t = ticks[i] < sim->next_tick ? sim->next_tick : ticks[i];
+            uint32_t wbits;
+            std::memcpy(&wbits, &weights[i], 4);
+            sim->pending.push_back({t, (static_cast<unsigned long long>(wbits) << 32) | neurons[i] | kExternalBit});
+        }
+    });
+}
+
+int snncuda_sim_run_until(snncuda_sim* sim, uint64_t inclusive_tick) {
+    if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
+    if (sim->poisoned) return set_error(SNNCUDA_ERR_POISONED, "simulation poisoned by an earlier device error");
+    const int rc = guarded([&] { run_impl(sim, inclusive_tick); });
+    if (rc == SNNCUDA_ERR_DEVICE) sim->poisoned = true;
+    return rc;
+}
+
+static int set_flag(snncuda_sim* sim, size_t offset, int32_t v) {
+    if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
+    return guarded([&] {
+        check(cudaMemcpyAsync(reinterpret_cast<char*>(sim->e.ts) + offset, &v, 4, cudaMemcpyHostToDevice,
+                              sim->stream), "toggle");
+        check(cudaStreamSynchronize(sim->stream), "toggle");
+    });
+}
+
+int snncuda_sim_set_plasticity(snncuda_sim* sim, int32_t enabled) {
+    return set_flag(sim, offsetof(TickState, stdp_enabled), enabled ? 1 : 0);
+}
+
+int snncuda_sim_set_temporal_learning(snncuda_sim* sim, int32_t enabled) {
+    return set_flag(sim, offsetof(TickState, temporal_enabled), enabled ? 1 : 0);
+}
+
+int snncuda_sim_counters(snncuda_sim* sim, snncuda_counters* out) {
+    if (sim == nullptr || out == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        const TickState ts = sim->read_ts();
+        const std::vector<uint32_t> counts = sim->d2h(sim->e.slot_count, sim->e.W);
+        uint64_t pending = sim->pending.size();
+        for (uint32_t c : counts) pending += c;
+        out->delivered_spikes = ts.delivered;
+        out->fired_spikes = ts.fired;
+        out->external_events = ts.external;
+        out->synaptic_events = ts.delivered - ts.external;
+        out->next_tick = sim->next_tick;
+        out->pending_events = pending;
+        out->raster_count = ts.raster_count;
+        out->max_slot_events = ts.max_slot_events;
+    });
+}
+
+int snncuda_sim_idle(snncuda_sim* sim, int32_t* out) {
+    if (out == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
+    snncuda_counters c;
+    const int rc = snncuda_sim_counters(sim, &c);
+    if (rc == SNNCUDA_OK) *out = c.pending_events == 0 ? 1 : 0;
+    return rc;
+}
+
+int snncuda_sim_read_neurons(snncuda_sim* sim, const snncuda_neuron_state* o) {
+    if (sim == nullptr || o == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        const std::vector<NeuronRec> r = sim->d2h(sim->e.nrec, sim->N);
+        const std::vector<NeuronTp> q = sim->d2h(sim->e.ntp, sim->N);
+        for (uint32_t i = 0; i < sim->N; ++i) {
+            if (o->membrane_potential) o->membrane_potential[i] = r[i].membrane;
+            if (o->spike_count) o->spike_count[i] = r[i].spike_count;
+            if (o->last_fired_tick) o->last_fired_tick[i] = r[i].last_fired1 ? static_cast<int64_t>(r[i].last_fired1) - 1 : -1;
+            if (o->last_active_tick) o->last_active_tick[i] = r[i].last_active;
+            for (int k = 0; k < 4; ++k) {
+                if (o->compartment_current) o->compartment_current[i * 4 + k] = r[i].cur[k];
+                if (o->compartment_last_update) o->compartment_last_update[i * 4 + k] = r[i].upd[k];
+                if (o->compartment_tau) o->compartment_tau[i * 4 + k] = kTauValue[(r[i].flags >> (2 * k)) & 3u];
+            }
+            if (o->window_start_tick) o->window_start_tick[i] = r[i].ws;
+            if (o->offset_count) o->offset_count[i] = r[i].len;
+            if (o->learned_count) o->learned_count[i] = q[i].ref_count;
+            if (o->match_count) o->match_count[i] = r[i].match_count;
+            if (o->last_match) o->last_match[i] = (r[i].flags >> 8) & 1u;
+        }
+    });
+}
+
+int snncuda_sim_read_synapses(snncuda_sim* sim, const snncuda_synapse_state* o) {
+    if (sim == nullptr || o == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        const std::vector<SynA> a = sim->d2h(sim->e.syna, sim->S);
+        const std::vector<SynB> b = sim->d2h(sim->e.synb, sim->S);
+        for (uint64_t tm = 0; tm < sim->S; ++tm) {
+            const uint64_t i = sim->c_of_tm[tm];
+            if (o->weight) o->weight[i] = a[tm].weight;
+            if (o->last_pre_spike_tick) o->last_pre_spike_tick[i] = a[tm].last_pre1 ? static_cast<int64_t>(a[tm].last_pre1) - 1 : -1;
+            if (o->last_post_spike_tick) o->last_post_spike_tick[i] = a[tm].last_post1 ? static_cast<int64_t>(a[tm].last_post1) - 1 : -1;
+            if (o->pre_spike_count) o->pre_spike_count[i] = b[tm].pre_count;
+            if (o->plasticity_update_count) o->plasticity_update_count[i] = a[tm].updates;
+            if (o->last_weight_delta) o->last_weight_delta[i] = a[tm].last_delta;
+            if (o->code_window_start_tick) o->code_window_start_tick[i] = b[tm].code_ws;
+            if (o->code_offset_count) o->code_offset_count[i] = b[tm].code_len;
+            if (o->learned_code_count) o->learned_code_count[i] = b[tm].learned_count;
+            if (o->code_match_count) o->code_match_count[i] = b[tm].code_matches;
+            if (o->last_code_match) o->last_code_match[i] = b[tm].last_code_match;
+        }
+    });
+}
+
+int snncuda_sim_read_pattern(snncuda_sim* sim, int32_t kind, uint64_t index, uint64_t which, uint32_t* values,
+                             uint64_t capacity, uint64_t* len) {
+    if (sim == nullptr || len == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        std::vector<uint32_t> v;
+        if (kind == 0 || kind == 1) {
+            if (index >= sim->N) throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "neuron out of range");
+            const uint32_t n = static_cast<uint32_t>(index);
+            const NeuronParam& p = sim->nparam[n];
+            const NeuronRec r = sim->d2h(sim->e.nrec + n, 1)[0];
+            const NeuronTp q = sim->d2h(sim->e.ntp + n, 1)[0];
+            if (kind == 0) {
+                const auto cand = sim->d2h(sim->e.cand + p.cand_base, p.window + 1);
+                expand_runs(cand.data(), q.nruns, p.window + 1, 0, r.len, v);
+            } else {
+                if (which >= q.ref_count) throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "pattern index out of range");
+                const RefMeta m = sim->d2h(sim->e.refmeta + p.meta_base + (q.ref_head + which) % p.max_refs, 1)[0];
+                const auto ring = sim->d2h(sim->e.ring + p.ring_base, p.ring_cap);
+                expand_runs(ring.data(), m.nruns, p.ring_cap, m.start, m.len, v);
+            }
+        } else if (kind == 2 || kind == 3) {
+            if (index >= sim->S) throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "synapse out of range");
+            const uint64_t tm = sim->tm_of_c[index];
+            const SynA a = sim->d2h(sim->e.syna + tm, 1)[0];
+            const SynB b = sim->d2h(sim->e.synb + tm, 1)[0];
+            if (kind == 2) {
+                v.assign(b.ring, b.ring + b.code_len);
+            } else {
+                if (which >= b.learned_count) throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "pattern index out of range");
+                const uint32_t n = static_cast<uint32_t>(
+                    std::upper_bound(sim->in_ptr.begin(), sim->in_ptr.end(), tm) - sim->in_ptr.begin() - 1);
+                const NeuronParam& p = sim->nparam[n];
+                const uint64_t off = p.lcode_base + (tm - p.in_begin) * p.max_refs * sim->e.code_stride +
+                                     which * sim->e.code_stride;
+                const std::vector<uint16_t> lc = sim->d2h(sim->e.lcode + off, expected_of(a));
+                v.assign(lc.begin(), lc.end());
+            }
+        } else {
+            throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "unknown pattern kind");
+        }
+        *len = v.size();
+        for (uint64_t i = 0; i < v.size() && i < capacity; ++i) values[i] = v[i];
+    });
+}
+
+// Same digest definition as every other implementation of this ABI.
+int snncuda_sim_state_digest(snncuda_sim* sim, uint64_t* neuron_digest, uint64_t* synapse_digest) {
+    if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
+    return guarded([&] {
+        const HostState h = fetch_all(sim, true);
+        std::vector<uint32_t> v;
+        if (neuron_digest) {
+            Digest d;
+            for (uint32_t n = 0; n < sim->N; ++n) {
+                const NeuronRec& r = h.nrec[n];
+                d.f32(r.membrane);
+                d.word(r.spike_count);
+                d.word(r.last_fired1 ? static_cast<uint64_t>(r.last_fired1 - 1) : ~0ULL);
+                d.word(r.last_active);
+                for (int k = 0; k < 4; ++k) {
+                    d.f32(r.cur[k]);
+                    d.word(r.upd[k]);
+                    d.f32(kTauValue[(r.flags >> (2 * k)) & 3u]);
+                }
+                d.word(r.ws);
+                neuron_offsets(sim, h, n, v);
+                d.word(v.size());
+                for (uint32_t x : v) d.word(x);
+                d.word(h.ntp[n].ref_count);
+                for (uint32_t j = 0; j < h.ntp[n].ref_count; ++j) {
+                    neuron_learned(sim, h, n, j, v);
+                    d.word(v.size());
+                    for (uint32_t x : v) d.word(x);
+                }
+                d.word((r.flags >> 8) & 1u);
+                d.word(r.match_count);
+            }
+            *neuron_digest = d.h;
+        }
+        if (synapse_digest) {
+            const std::vector<uint32_t>& tm_of_c = sim->tm_of_c;
+            Digest d;
+            for (uint64_t c = 0; c < sim->S; ++c) {
+                const uint64_t tm = tm_of_c[c];
+                const SynA& a = h.syna[tm];
+                const SynB& b = h.synb[tm];
+                d.f32(a.weight);
+                d.word(a.last_pre1 ? static_cast<uint64_t>(a.last_pre1 - 1) : ~0ULL);
+                d.word(a.last_post1 ? static_cast<uint64_t>(a.last_post1 - 1) : ~0ULL);
+                d.word(b.pre_count);
+                d.word(a.updates);
+                d.f32(a.last_delta);
+                d.word(b.code_ws);
+                d.word(b.code_len);
+                for (uint32_t j = 0; j < b.code_len; ++j) d.word(b.ring[j]);
+                d.word(b.learned_count);
+                for (uint32_t j = 0; j < b.learned_count; ++j) {
+                    synapse_learned(sim, h, tm, j, v);
+                    d.word(v.size());
+                    for (uint32_t x : v) d.word(x);
+                }
+                d.word(b.code_matches);
+                d.word(b.last_code_match);
+            }
+            *synapse_digest = d.h;
+        }
+    });
+}
+
+int snncuda_sim_read_raster(snncuda_sim* sim, uint64_t first, uint64_t count, uint64_t* ticks, uint32_t* neurons) {
+    if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
+    return guarded([&] {
+        const TickState ts = sim->read_ts();
+        const uint64_t have = std::min<uint64_t>(ts.raster_count, sim->e.raster_cap);
+        if (first + count > have) throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "raster range out of bounds");
+        const std::vector<uint32_t> r = sim->d2h(sim->e.raster + 2 * first, 2 * count);
+        for (uint64_t i = 0; i < count; ++i) {
+            if (ticks) ticks[i] = r[2 * i];
+            if (neurons) neurons[i] = r[2 * i + 1];
+        }
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,366 @@
+"""Host-side API of the GB300 backend.
+
+`Simulation` is a thin owner of one `snncuda_sim` handle (C ABI in
+include/snncuda_gb300.h).  `NetworkPropagator` mirrors the reference
+runtime::NetworkPropagator interface (runtime/NetworkPropagator.h:14-47):
+`inject`, `run_until`, `state`, `spike_count`, `delivered_spike_count`,
+`fired_spike_count`, `synapse_state`, `idle`, with 1-based neuron and synapse
+ids, so code written against the reference reads the same.  Errors raise
+`SNNCudaError` (the reference throws std::invalid_argument /
+std::runtime_error).
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import pathlib
+from ctypes import c_float, c_int32, c_int64, c_uint8, c_uint32, c_uint64, c_void_p
+from dataclasses import dataclass
+from typing import Dict, List, Optional
+
+import numpy as np
+
+from . import _abi
+from .connectome import Connectome
+
+_LIB_DIR = pathlib.Path(__file__).resolve().parent / "_lib"
+BACKEND_LIBRARY = _LIB_DIR / "libsnncuda_gb300.so"
+
+_backend: Optional[ctypes.CDLL] = None
+
+
+class SNNCudaError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{_abi.STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def backend() -> ctypes.CDLL:
+    """The GPU backend library.  Raises if it has not been built: there is no
+    CPU fallback."""
+    global _backend
+    if _backend is None:
+        path = os.environ.get("SNNCUDA_GB300_LIBRARY", str(BACKEND_LIBRARY))
+        if not pathlib.Path(path).exists():
+            raise SNNCudaError(_abi.SNNCUDA_ERR_DEVICE,
+                               f"GPU backend library missing at {path}; run "
+                               "`python -c 'import __graft_entry__ as g; g.build()'`")
+        _backend = _abi.bind(path)
+    return _backend
+
+
+def default_config(lib: Optional[ctypes.CDLL] = None, **overrides) -> _abi.Config:
+    lib = lib or backend()
+    cfg = _abi.Config()
+    lib.snncuda_config_default(ctypes.byref(cfg))
+    for key, value in overrides.items():
+        if not hasattr(cfg, key):
+            raise AttributeError(f"unknown config field {key}")
+        setattr(cfg, key, value)
+    return cfg
+
+
+def _check(lib, status: int) -> None:
+    if status != _abi.SNNCUDA_OK:
+        raise SNNCudaError(status, lib.snncuda_last_error().decode("utf-8", "replace"))
+
+
+class Simulation:
+    """One simulation handle over a Connectome (0-based neuron indices)."""
+
+    def __init__(self, connectome: Connectome, config: Optional[_abi.Config] = None,
+                 lib: Optional[ctypes.CDLL] = None):
+        connectome.validate()
+        self.lib = lib or backend()
+        self.connectome = connectome
+        self.config = config if config is not None else default_config(self.lib)
+        c = connectome
+        self._keep = [np.ascontiguousarray(a) for a in (
+            c.threshold.astype(np.float32), c.pattern_window_ticks.astype(np.uint64),
+            c.similarity_threshold.astype(np.float32), c.max_reference_patterns.astype(np.uint64),
+            c.source.astype(np.uint32), c.target.astype(np.uint32), c.weight.astype(np.float32),
+            c.max_weight.astype(np.float32), c.delay_ticks.astype(np.uint32),
+            c.compartment.astype(np.uint8), c.receptor.astype(np.uint8),
+            c.plasticity_enabled.astype(np.uint8))]
+        (thr, win, sim, refs, src, tgt, w, mw, dly, comp, rec, pl) = self._keep
+        code_ptr = code = None
+        if c.code_offset_ptr is not None:
+            code_ptr = np.ascontiguousarray(c.code_offset_ptr.astype(np.uint64))
+            code = np.ascontiguousarray(c.code_offsets.astype(np.uint32))
+            if code.size == 0:
+                code = np.zeros(1, dtype=np.uint32)
+            self._keep += [code_ptr, code]
+        net = _abi.Network(
+            c.neuron_count, _abi.ptr(thr, c_float), _abi.ptr(win, c_uint64), _abi.ptr(sim, c_float),
+            _abi.ptr(refs, c_uint64), c.synapse_count, _abi.ptr(src, c_uint32),
+            _abi.ptr(tgt, c_uint32), _abi.ptr(w, c_float), _abi.ptr(mw, c_float),
+            _abi.ptr(dly, c_uint32), _abi.ptr(comp, c_uint8), _abi.ptr(rec, c_uint8),
+            _abi.ptr(pl, c_uint8), _abi.ptr(code_ptr, c_uint64), _abi.ptr(code, c_uint32))
+        handle = c_void_p()
+        _check(self.lib, self.lib.snncuda_sim_create(ctypes.byref(net), ctypes.byref(self.config),
+                                                     ctypes.byref(handle)))
+        self._keep = None  # arrays were copied by create
+        self.handle = handle
+        self.neuron_count = c.neuron_count
+        self.synapse_count = c.synapse_count
+
+    # -- lifecycle -----------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.snncuda_sim_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- stepping --------------------------------------------------------------
+    def inject(self, neurons, ticks, weights) -> None:
+        n = np.ascontiguousarray(np.asarray(neurons, dtype=np.uint32).ravel())
+        t = np.ascontiguousarray(np.asarray(ticks, dtype=np.uint64).ravel())
+        w = np.ascontiguousarray(np.asarray(weights, dtype=np.float32).ravel())
+        if not (n.size == t.size == w.size):
+            raise ValueError("inject arrays must have equal length")
+        if n.size == 0:
+            return
+        _check(self.lib, self.lib.snncuda_sim_inject(self.handle, n.size, _abi.ptr(n, c_uint32),
+                                                     _abi.ptr(t, c_uint64), _abi.ptr(w, c_float)))
+
+    def run_until(self, inclusive_tick: int) -> None:
+        _check(self.lib, self.lib.snncuda_sim_run_until(self.handle, int(inclusive_tick)))
+
+    def set_plasticity(self, enabled: bool) -> None:
+        _check(self.lib, self.lib.snncuda_sim_set_plasticity(self.handle, 1 if enabled else 0))
+
+    def set_temporal_learning(self, enabled: bool) -> None:
+        _check(self.lib, self.lib.snncuda_sim_set_temporal_learning(self.handle, 1 if enabled else 0))
+
+    # -- readers -----------------------------------------------------------------
+    def counters(self) -> Dict[str, int]:
+        out = _abi.Counters()
+        _check(self.lib, self.lib.snncuda_sim_counters(self.handle, ctypes.byref(out)))
+        return {name: int(getattr(out, name)) for name, _ in _abi.Counters._fields_}
+
+    def idle(self) -> bool:
+        out = c_int32()
+        _check(self.lib, self.lib.snncuda_sim_idle(self.handle, ctypes.byref(out)))
+        return bool(out.value)
+
+    def neurons(self) -> Dict[str, np.ndarray]:
+        n = self.neuron_count
+        arrays = {
+            "membrane_potential": np.zeros(n, np.float32), "spike_count": np.zeros(n, np.uint64),
+            "last_fired_tick": np.zeros(n, np.int64), "last_active_tick": np.zeros(n, np.uint64),
+            "compartment_current": np.zeros(n * 4, np.float32),
+            "compartment_last_update": np.zeros(n * 4, np.uint64),
+            "compartment_tau": np.zeros(n * 4, np.float32),
+            "window_start_tick": np.zeros(n, np.uint64), "offset_count": np.zeros(n, np.uint64),
+            "learned_count": np.zeros(n, np.uint64), "match_count": np.zeros(n, np.uint64),
+            "last_match": np.zeros(n, np.uint8),
+        }
+        types = dict(_abi.NeuronState._fields_)
+        view = _abi.NeuronState(**{k: _abi.ptr(v, types[k]._type_) for k, v in arrays.items()})
+        _check(self.lib, self.lib.snncuda_sim_read_neurons(self.handle, ctypes.byref(view)))
+        for k in ("compartment_current", "compartment_last_update", "compartment_tau"):
+            arrays[k] = arrays[k].reshape(n, 4)
+        return arrays
+
+    def synapses(self) -> Dict[str, np.ndarray]:
+        s = self.synapse_count
+        arrays = {
+            "weight": np.zeros(s, np.float32), "last_pre_spike_tick": np.zeros(s, np.int64),
+            "last_post_spike_tick": np.zeros(s, np.int64), "pre_spike_count": np.zeros(s, np.uint64),
+            "plasticity_update_count": np.zeros(s, np.uint64),
+            "last_weight_delta": np.zeros(s, np.float32),
+            "code_window_start_tick": np.zeros(s, np.uint64),
+            "code_offset_count": np.zeros(s, np.uint64), "learned_code_count": np.zeros(s, np.uint64),
+            "code_match_count": np.zeros(s, np.uint64), "last_code_match": np.zeros(s, np.uint8),
+        }
+        types = dict(_abi.SynapseState._fields_)
+        view = _abi.SynapseState(**{k: _abi.ptr(v, types[k]._type_) for k, v in arrays.items()})
+        _check(self.lib, self.lib.snncuda_sim_read_synapses(self.handle, ctypes.byref(view)))
+        return arrays
+
+    def pattern(self, kind: int, index: int, which: int = 0) -> List[int]:
+        length = c_uint64()
+        buf = np.zeros(64, dtype=np.uint32)
+        _check(self.lib, self.lib.snncuda_sim_read_pattern(
+            self.handle, kind, index, which, _abi.ptr(buf, c_uint32), buf.size, ctypes.byref(length)))
+        if length.value > buf.size:
+            buf = np.zeros(length.value, dtype=np.uint32)
+            _check(self.lib, self.lib.snncuda_sim_read_pattern(
+                self.handle, kind, index, which, _abi.ptr(buf, c_uint32), buf.size,
+                ctypes.byref(length)))
+        return [int(v) for v in buf[:length.value]]
+
+    def digest(self) -> tuple:
+        a, b = c_uint64(), c_uint64()
+        _check(self.lib, self.lib.snncuda_sim_state_digest(self.handle, ctypes.byref(a), ctypes.byref(b)))
+        return int(a.value), int(b.value)
+
+    def raster(self) -> tuple:
+        count = self.counters()["raster_count"]
+        ticks = np.zeros(count, np.uint64)
+        neurons = np.zeros(count, np.uint32)
+        if count:
+            _check(self.lib, self.lib.snncuda_sim_read_raster(
+                self.handle, 0, count, _abi.ptr(ticks, c_uint64), _abi.ptr(neurons, c_uint32)))
+        return ticks, neurons
+
+
+# ---------------------------------------------------------------------------
+# Reference-shaped interface
+# ---------------------------------------------------------------------------
+
+@dataclass
+class CompartmentState:
+    current: float
+    last_update_tick: int
+    decay_tau_ticks: float
+
+
+@dataclass
+class TemporalPatternState:
+    window_start_tick: int
+    spike_offsets: List[int]
+    learned_patterns: List[List[int]]
+    last_match: bool
+    match_count: int
+
+
+@dataclass
+class NeuronStateView:
+    """runtime::NeuronState (NeuronStateCache.h:15-45)."""
+    id: int
+    membrane_potential: float
+    threshold: float
+    last_active_tick: int
+    last_fired_tick: Optional[int]
+    spike_count: int
+    soma: CompartmentState
+    basal: CompartmentState
+    apical: CompartmentState
+    inhibitory: CompartmentState
+    temporal_pattern: TemporalPatternState
+
+
+@dataclass
+class SynapseStateView:
+    """runtime::SynapseRuntimeState (SynapseDendriteProcessor.h:14-35)."""
+    id: int
+    source: int
+    target: int
+    weight: float
+    max_weight: float
+    delay_ticks: int
+    spike_code_offsets: List[int]
+    plasticity_enabled: bool
+    last_pre_spike_tick: Optional[int]
+    last_post_spike_tick: Optional[int]
+    pre_spike_count: int
+    plasticity_update_count: int
+    last_weight_delta: float
+    code_window_start_tick: int
+    code_offsets: List[int]
+    learned_code_patterns: List[List[int]]
+    code_match_count: int
+    last_code_match: bool
+
+
+class NetworkPropagator:
+    """Drop-in for runtime::NetworkPropagator over the GPU backend.
+
+    `store` and `resident_neuron_capacity` are accepted for signature parity:
+    neuron state stays resident in device memory, so there is no LRU paging
+    (NeuronStateCache only moved state, never changed it).
+    """
+
+    def __init__(self, connectome: Connectome, store=None, resident_neuron_capacity: int = 65536,
+                 timing_wheel_slots: int = 4096, config: Optional[_abi.Config] = None,
+                 lib: Optional[ctypes.CDLL] = None):
+        if resident_neuron_capacity == 0:
+            raise SNNCudaError(_abi.SNNCUDA_ERR_INVALID_ARGUMENT, "LRU cache capacity must be nonzero")
+        lib = lib or backend()
+        cfg = config if config is not None else default_config(lib)
+        cfg.timing_wheel_slots = timing_wheel_slots
+        self.connectome = connectome
+        self.sim = Simulation(connectome, cfg, lib)
+        self._pending: List[tuple] = []
+
+    def _flush(self) -> None:
+        if self._pending:
+            n, t, w = zip(*self._pending)
+            self._pending = []
+            self.sim.inject(n, t, w)
+
+    def inject(self, target: int, delivery_tick: int, weight: float) -> None:
+        if not 1 <= target <= self.sim.neuron_count:
+            raise SNNCudaError(_abi.SNNCUDA_ERR_INVALID_ARGUMENT, f"unknown neuron id {target}")
+        self._pending.append((target - 1, delivery_tick, weight))
+
+    def run_until(self, inclusive_tick: int) -> None:
+        self._flush()
+        self.sim.run_until(inclusive_tick)
+
+    def set_plasticity(self, enabled: bool) -> None:
+        self.sim.set_plasticity(enabled)
+
+    def set_temporal_learning(self, enabled: bool) -> None:
+        self.sim.set_temporal_learning(enabled)
+
+    def state(self, neuron_id: int) -> NeuronStateView:
+        self._flush()
+        i = neuron_id - 1
+        a = self.sim.neurons()
+        comps = [CompartmentState(float(a["compartment_current"][i, k]),
+                                  int(a["compartment_last_update"][i, k]),
+                                  float(a["compartment_tau"][i, k])) for k in range(4)]
+        learned = [self.sim.pattern(1, i, j) for j in range(int(a["learned_count"][i]))]
+        tp = TemporalPatternState(int(a["window_start_tick"][i]), self.sim.pattern(0, i), learned,
+                                  bool(a["last_match"][i]), int(a["match_count"][i]))
+        lf = int(a["last_fired_tick"][i])
+        return NeuronStateView(neuron_id, float(a["membrane_potential"][i]),
+                               float(self.connectome.threshold[i]), int(a["last_active_tick"][i]),
+                               None if lf < 0 else lf, int(a["spike_count"][i]), *comps, tp)
+
+    def spike_count(self, neuron_id: int) -> int:
+        return int(self.sim.neurons()["spike_count"][neuron_id - 1])
+
+    def delivered_spike_count(self) -> int:
+        return self.sim.counters()["delivered_spikes"]
+
+    def fired_spike_count(self) -> int:
+        return self.sim.counters()["fired_spikes"]
+
+    def synapse_state(self, synapse_id: int) -> Optional[SynapseStateView]:
+        i = synapse_id - 1
+        if not 0 <= i < self.sim.synapse_count:
+            return None
+        a = self.sim.synapses()
+        c = self.connectome
+
+        def opt(v):
+            return None if int(v) < 0 else int(v)
+
+        learned = [self.sim.pattern(3, i, j) for j in range(int(a["learned_code_count"][i]))]
+        return SynapseStateView(
+            synapse_id, int(c.source[i]) + 1, int(c.target[i]) + 1, float(a["weight"][i]),
+            float(c.max_weight[i]), int(c.delay_ticks[i]), c.spike_codes(i),
+            bool(c.plasticity_enabled[i]), opt(a["last_pre_spike_tick"][i]),
+            opt(a["last_post_spike_tick"][i]), int(a["pre_spike_count"][i]),
+            int(a["plasticity_update_count"][i]), float(a["last_weight_delta"][i]),
+            int(a["code_window_start_tick"][i]), self.sim.pattern(2, i), learned,
+            int(a["code_match_count"][i]), bool(a["last_code_match"][i]))
+
+    def idle(self) -> bool:
+        self._flush()
+        return self.sim.idle()
