@@ -1,0 +1,358 @@
+"""Throughput benchmark: synaptic events/s of the per-tick SNN hot path.
+
+Workload (default `stdp_100k`, the 100,000-neuron / 1e8-synapse STDP
+network with 1-4 spike-code offsets per synapse, temporal-pattern matching,
+5 Hz Poisson drive, 10,000 ticks): one *step* is `--ticks-per-step` ticks
+(default 400) of the network; W warm-up steps then K timed steps cover the
+workload's 10,000 ticks.
+
+GPU arm (default)
+  value   synaptic events/s with the whole drive injected before the timed
+          region (inputs resident in HBM); CUDA events on the simulation's
+          stream bracket the K timed steps.
+  e2e     the same metric through the public API with host buffers: each step
+          injects that step's drive from pinned host memory, runs, and reads
+          back the step's fire raster and counters.
+  roofline  the dominant kernel from a per-kernel profile of 200 extra ticks
+          (graph event nodes around every kernel), algorithmic bytes per launch
+          / average launch time, against the measured HBM copy bandwidth.
+  cpu_baseline  the CPU oracle port on a bounded prefix of the same workload.
+Reference arm (--impl reference): the CPU oracle port (the reference's own
+runtime cannot be built on the GPU host) on a bounded prefix of the workload.
+
+Multi-GPU: replicas only (independent copies of the network, one per rank,
+no collective on the data path); value = all ranks' events / max time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "synaptic_events_per_s"
+UNIT = "events/s"
+ORACLE = ROOT / "oracle" / "_build" / "liboracle_port.so"
+
+# Per-unit algorithmic bytes of each kernel (device layout in
+# snncuda_gb300/csrc/engine.h).  See the design doc for the derivation.
+BYTES_PER_SYN_EVENT_PROCESS = 8 + 64 + 64       # grouped entry, SynA r+w, SynB r+w
+BYTES_PER_EXT_EVENT_PROCESS = 8
+BYTES_PER_TARGET_PROCESS = 64 + 128 + 64 + 8    # params, NeuronRec r+w, NeuronTp r+w, run append
+
+
+def load_peaks():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        d = json.loads(path.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        self.file.seek(0)
+        rows = [r.split(",") for r in self.file.read().strip().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def workload_from_args(args):
+    from snncuda_gb300 import synthetic
+    w = synthetic.WORKLOADS[args.workload]
+    if args.weight_scale is not None:
+        w = w.scaled(weight_scale=args.weight_scale)
+    return w
+
+
+def sim_config(lib, w, **extra):
+    from snncuda_gb300.simulation import default_config
+    cfg = default_config(lib, **extra)
+    cfg.stdp_enabled = 1 if w.stdp_enabled else 0
+    cfg.max_weight = w.max_weight
+    return cfg
+
+
+def cpu_sample(w, net, drive, budget_s: float, tick_chunk: int = 5, max_ticks: int = 400):
+    """Run the CPU oracle on a prefix of the workload for about budget_s."""
+    from snncuda_gb300 import _abi
+    from snncuda_gb300.simulation import Simulation
+    lib = _abi.bind(str(ORACLE))
+    sim = Simulation(net, sim_config(lib, w), lib)
+    n, t, wt = drive
+    keep = t < max_ticks
+    sim.inject(n[keep], t[keep], wt[keep])
+    start = time.perf_counter()
+    tick = 0
+    while tick < max_ticks:
+        tick += tick_chunk
+        sim.run_until(tick - 1)
+        if time.perf_counter() - start >= budget_s:
+            break
+    elapsed = time.perf_counter() - start
+    c = sim.counters()
+    sim.close()
+    return {"value": c["synaptic_events"] / elapsed, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"ticks 0..{tick - 1} of {w.name} ({c['synaptic_events']} synaptic events, "
+                      f"{elapsed:.1f} s, single-threaded oracle port)"}
+
+
+def run_reference(args, w):
+    from snncuda_gb300 import synthetic
+    net = synthetic.build_network(w)
+    drive = synthetic.build_drive(w, w.ticks)
+    sample = cpu_sample(w, net, drive, budget_s=args.cpu_seconds)
+    return {
+        "metric": METRIC, "value": sample["value"], "unit": UNIT, "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": config_block(args, w),
+        "cpu_baseline": sample,
+        "e2e": {"value": sample["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def config_block(args, w):
+    return {"workload": w.name, "neurons": w.neurons, "synapses": w.synapses, "fanout": w.fanout,
+            "weight_scale": w.weight_scale, "ticks": w.ticks, "ticks_per_step": args.ticks_per_step,
+            "stdp": w.stdp_enabled, "drive_hz": w.drive_rate_hz, "seed": w.seed,
+            "l2": "inputs larger than L2 (synapse state 64 B x 1e8 = 6.4 GB)",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    ap.add_argument("--workload", default="stdp_100k")
+    ap.add_argument("--ticks-per-step", type=int, default=400)
+    ap.add_argument("--weight-scale", type=float, default=None)
+    ap.add_argument("--profile-ticks", type=int, default=200)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    w = workload_from_args(args)
+    total_ticks = (args.warmup + args.steps) * args.ticks_per_step
+    if total_ticks > w.ticks:
+        w = w.scaled(ticks=total_ticks)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference(args, w)), flush=True)
+        return
+
+    import torch
+    import torch.distributed as dist
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    import __graft_entry__
+    if rank == 0 or world == 1:
+        __graft_entry__.build()
+    if world > 1:
+        dist.barrier()
+    from snncuda_gb300 import synthetic
+    from snncuda_gb300.simulation import Simulation, backend
+
+    lib = backend()
+    net = synthetic.build_network(w)
+    profile_end = total_ticks + args.profile_ticks
+    drive_all = synthetic.build_drive(w, profile_end)
+    dn, dt, dw = drive_all
+    main_mask = dt < total_ticks
+    drive = (dn[main_mask], dt[main_mask], dw[main_mask])
+    stream = torch.cuda.Stream(device=dev)
+
+    # ---- device-resident timing --------------------------------------------
+    sim = Simulation(net, sim_config(lib, w, cuda_stream=stream.cuda_stream), lib)
+    sim.inject(*drive)
+    tps = args.ticks_per_step
+    tick = 0
+    for _ in range(args.warmup):
+        tick += tps
+        sim.run_until(tick - 1)
+    c0 = sim.counters()
+    sampler = ClockSampler(local)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        tick += tps
+        sim.run_until(tick - 1)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    if world > 1:
+        dist.barrier()
+    c1 = sim.counters()
+    ms = ev0.elapsed_time(ev1)
+    events = c1["synaptic_events"] - c0["synaptic_events"]
+    fires = c1["fired_spikes"] - c0["fired_spikes"]
+    if world > 1:
+        t = torch.tensor([ms, float(events)], dtype=torch.float64, device=dev)
+        mx = t.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        ms_max, events_all = float(mx[0]), float(t[1])
+    else:
+        ms_max, events_all = ms, float(events)
+    value = events_all / (ms_max / 1e3)
+
+    # ---- per-kernel profile for the roofline -------------------------------
+    roofline = None
+    prof = None
+    if args.profile_ticks > 0:
+        extra = ~main_mask
+        sim.inject(dn[extra], dt[extra], dw[extra])
+        prof = sim.profile(profile_end - 1)
+        km = prof["kernel_ms"]
+        top = max(km, key=km.get)
+        launches = prof["ticks"]
+        peak, peak_kind = load_peaks()
+        if top == "k_process":
+            algo = (BYTES_PER_SYN_EVENT_PROCESS * prof["synaptic_events"] +
+                    BYTES_PER_EXT_EVENT_PROCESS * prof["external_events"] +
+                    BYTES_PER_TARGET_PROCESS * prof["touched_targets"]) / launches
+        else:
+            algo = None
+        avg_ms = km[top] / launches
+        achieved = algo / (avg_ms / 1e3) / 1e9 if algo else None
+        roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": (achieved / peak) if achieved else None, "traffic": None,
+                    "peak_source": peak_kind, "avg_launch_us": avg_ms * 1e3,
+                    "algorithmic_bytes_per_launch": algo,
+                    "kernel_share": {k: v / sum(km.values()) for k, v in km.items()}}
+    sim.close()
+    del sim
+
+    # ---- end to end through the public API ---------------------------------
+    e2e = None
+    if not args.no_e2e:
+        pin = lambda a, dt_: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+        pn, pt, pw = pin(drive[0], np.uint32), pin(drive[1], np.uint64), pin(drive[2], np.float32)
+        bounds = np.searchsorted(pt, np.arange(0, total_ticks + tps, tps))
+        sim2 = Simulation(net, sim_config(lib, w, cuda_stream=stream.cuda_stream,
+                                          raster_capacity=1 << 26), lib)
+        h2d = d2h = 0
+        raster_pos = 0
+        tick = 0
+        start = None
+        for step in range(args.warmup + args.steps):
+            if step == args.warmup:
+                torch.cuda.synchronize()
+                h2d = d2h = 0
+                start = time.perf_counter()
+                cs = sim2.counters()
+            a, b = bounds[step], bounds[step + 1]
+            sim2.inject(pn[a:b], pt[a:b], pw[a:b])
+            h2d += (b - a) * 16
+            tick += tps
+            sim2.run_until(tick - 1)
+            c = sim2.counters()
+            new = c["raster_count"] - raster_pos
+            sim2.raster(raster_pos, new)
+            d2h += new * 8 + 64
+            raster_pos = c["raster_count"]
+        elapsed = time.perf_counter() - start
+        ce = sim2.counters()
+        sim2.close()
+        e2e_events = ce["synaptic_events"] - cs["synaptic_events"]
+        e2e = {"value": e2e_events / elapsed, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
+               "d2h_bytes_per_step": int(d2h / args.steps)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_sample(w, net, drive_all, budget_s=args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_block(args, w),
+            "ticks_per_s": args.steps * tps / (ms_max / 1e3),
+            "fires_per_tick": fires / (args.steps * tps),
+            "events_per_tick": events / (args.steps * tps),
+            "gpu_launches": args.steps * tps * 8,
+            "clocks": clocks, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -215,6 +215,24 @@ int snncuda_sim_state_digest(snncuda_sim* sim, uint64_t* neuron_digest, uint64_t
 int snncuda_sim_read_raster(snncuda_sim* sim, uint64_t first, uint64_t count, uint64_t* ticks,
                             uint32_t* neurons);
 
+/* ---- engine extension: per-kernel device time ----------------------------
+ * No counterpart in the reference (which times the whole tick loop on the
+ * host clock, spike_throughput_benchmark.cpp:137-140).  Processes ticks like
+ * snncuda_sim_run_until, but launches one tick at a time from a graph whose
+ * event nodes bracket every kernel, and accumulates device time per kernel
+ * plus the work counters of the profiled ticks into *out (zero it first). */
+#define SNNCUDA_KERNEL_COUNT 8
+typedef struct snncuda_profile {
+    uint64_t ticks;
+    double kernel_ms[SNNCUDA_KERNEL_COUNT];
+    uint64_t synaptic_events;
+    uint64_t external_events;
+    uint64_t fires;
+    uint64_t touched_targets;   /* sum over ticks of targets with due events */
+} snncuda_profile;
+int snncuda_sim_profile(snncuda_sim* sim, uint64_t inclusive_tick, snncuda_profile* out);
+const char* snncuda_kernel_name(int32_t index);
+
 #ifdef __cplusplus
 }
 #endif

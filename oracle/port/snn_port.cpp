@@ -643,4 +643,22 @@ int snncuda_sim_read_raster(snncuda_sim* sim, uint64_t first, uint64_t count, ui
     return SNNCUDA_OK;
 }
 
+// Per-kernel device time does not exist on the CPU: only the work counters
+// of the processed ticks are filled.
+int snncuda_sim_profile(snncuda_sim* sim, uint64_t inclusive_tick, snncuda_profile* out) {
+    if (sim == nullptr || out == nullptr) return fail(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
+    snncuda_counters before, after;
+    snncuda_sim_counters(sim, &before);
+    const int rc = snncuda_sim_run_until(sim, inclusive_tick);
+    snncuda_sim_counters(sim, &after);
+    out->ticks += after.next_tick - before.next_tick;
+    out->synaptic_events += after.synaptic_events - before.synaptic_events;
+    out->external_events += after.external_events - before.external_events;
+    out->fires += after.fired_spikes - before.fired_spikes;
+    return rc;
+}
+
+const char* snncuda_kernel_name(int32_t) { return ""; }
+
 }  // extern "C"
+

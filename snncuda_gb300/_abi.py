@@ -112,6 +112,20 @@ class SynapseState(Structure):
     ]
 
 
+KERNEL_COUNT = 8
+
+
+class Profile(Structure):
+    _fields_ = [
+        ("ticks", c_uint64),
+        ("kernel_ms", ctypes.c_double * KERNEL_COUNT),
+        ("synaptic_events", c_uint64),
+        ("external_events", c_uint64),
+        ("fires", c_uint64),
+        ("touched_targets", c_uint64),
+    ]
+
+
 _SIGNATURES = {
     "snncuda_version": (c_char_p, []),
     "snncuda_cuda_available": (c_int, []),
@@ -133,6 +147,8 @@ _SIGNATURES = {
     "snncuda_sim_state_digest": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64)]),
     "snncuda_sim_read_raster": (c_int, [c_void_p, c_uint64, c_uint64, POINTER(c_uint64),
                                         POINTER(c_uint32)]),
+    "snncuda_sim_profile": (c_int, [c_void_p, c_uint64, POINTER(Profile)]),
+    "snncuda_kernel_name": (c_char_p, [c_int32]),
 }
 
 # Symbols every implementation of the ABI must export.

@@ -120,6 +120,7 @@ struct TickState {
     unsigned long long fired;
     unsigned long long max_slot_events;
     unsigned long long raster_count;
+    unsigned long long touched_total;  // sum of n_touched over ticks
     uint32_t status;
     uint32_t tick;            // tick being processed
     uint32_t n_due;           // events due this tick
@@ -214,7 +215,11 @@ constexpr int kExpandFires = 8;          // fires per expansion block (one warp 
 constexpr uint32_t kMaxClasses = 256;    // distinct delivery delays
 
 // Host-side launchers (kernels.cu).
-void launch_tick(const Engine& e, cudaStream_t stream);
+// `marks` (optional) holds 2 * kKernelCount events recorded around every
+// kernel (before, after) for profiling graphs.
+constexpr int kKernelCount = 8;
+void launch_tick(const Engine& e, cudaStream_t stream, cudaEvent_t* marks = nullptr);
+const char* kernel_name(int index);
 void launch_inject(const Engine& e, const unsigned long long* ev, const uint32_t* slot_of_group,
                    const uint32_t* group_off, uint32_t groups, cudaStream_t stream);
 

@@ -122,125 +122,85 @@ typedef struct snngen_spec {
     uint64_t seed;
 } snngen_spec;
 
+// Caller-allocated output arrays (the generator fills them in parallel).
+// code_offsets must hold neuron_count * fanout * codes_max entries; the
+// number written is returned in *code_count.
 typedef struct snngen_network {
-    uint32_t neuron_count;
-    uint64_t synapse_count;
-    uint64_t code_count;
-    float* threshold;
-    uint64_t* pattern_window_ticks;
-    float* similarity_threshold;
-    uint64_t* max_reference_patterns;
-    uint32_t* source;
-    uint32_t* target;
-    float* weight;
-    float* max_weight;
-    uint32_t* delay_ticks;
-    uint8_t* compartment;
-    uint8_t* receptor;
-    uint8_t* plasticity_enabled;
-    uint64_t* code_offset_ptr;
-    uint32_t* code_offsets;
+    float* threshold;                  // [N]
+    uint64_t* pattern_window_ticks;    // [N]
+    float* similarity_threshold;       // [N]
+    uint64_t* max_reference_patterns;  // [N]
+    uint32_t* source;                  // [S]
+    uint32_t* target;                  // [S]
+    float* weight;                     // [S]
+    float* max_weight;                 // [S]
+    uint32_t* delay_ticks;             // [S]
+    uint8_t* compartment;              // [S]
+    uint8_t* receptor;                 // [S]
+    uint8_t* plasticity_enabled;       // [S]
+    uint64_t* code_offset_ptr;         // [S+1]
+    uint32_t* code_offsets;            // [S * codes_max]
 } snngen_network;
 
-void snngen_free_network(snngen_network* n) {
-    if (n == nullptr) return;
-    delete[] n->threshold;
-    delete[] n->pattern_window_ticks;
-    delete[] n->similarity_threshold;
-    delete[] n->max_reference_patterns;
-    delete[] n->source;
-    delete[] n->target;
-    delete[] n->weight;
-    delete[] n->max_weight;
-    delete[] n->delay_ticks;
-    delete[] n->compartment;
-    delete[] n->receptor;
-    delete[] n->plasticity_enabled;
-    delete[] n->code_offset_ptr;
-    delete[] n->code_offsets;
-    std::memset(n, 0, sizeof(*n));
-}
-
-int snngen_build_network(const snngen_spec* spec, snngen_network* out) {
-    if (spec == nullptr || out == nullptr || spec->neuron_count == 0 || spec->delay_min > spec->delay_max ||
-        spec->codes_min == 0 || spec->codes_min > spec->codes_max || (spec->compartments != 2 && spec->compartments != 4))
+int snngen_fill_network(const snngen_spec* spec, const snngen_network* out, uint64_t* code_count) {
+    if (spec == nullptr || out == nullptr || code_count == nullptr || spec->neuron_count == 0 ||
+        spec->delay_min > spec->delay_max || spec->codes_min == 0 || spec->codes_min > spec->codes_max ||
+        (spec->compartments != 2 && spec->compartments != 4))
         return 1;
-    std::memset(out, 0, sizeof(*out));
     const uint32_t N = spec->neuron_count;
     const uint64_t S = static_cast<uint64_t>(N) * spec->fanout;
-    try {
-        out->neuron_count = N;
-        out->synapse_count = S;
-        out->threshold = new float[N];
-        out->pattern_window_ticks = new uint64_t[N];
-        out->similarity_threshold = new float[N];
-        out->max_reference_patterns = new uint64_t[N];
-        for (uint32_t i = 0; i < N; ++i) {
-            out->threshold[i] = spec->threshold;
-            out->pattern_window_ticks[i] = spec->pattern_window_ticks;
-            out->similarity_threshold[i] = spec->similarity_threshold;
-            out->max_reference_patterns[i] = spec->max_reference_patterns;
-        }
-        out->source = new uint32_t[S];
-        out->target = new uint32_t[S];
-        out->weight = new float[S];
-        out->max_weight = new float[S];
-        out->delay_ticks = new uint32_t[S];
-        out->compartment = new uint8_t[S];
-        out->receptor = new uint8_t[S];
-        out->plasticity_enabled = new uint8_t[S];
-        out->code_offset_ptr = new uint64_t[S + 1];
-        // Code counts per synapse first (stream 2*src+1), then a prefix sum.
-        std::vector<uint8_t> kcount(S);
-        parallel_for(N, [&](uint64_t src) {
-            Stream r(spec->seed, 2 * src + 1);
-            for (uint32_t j = 0; j < spec->fanout; ++j)
-                kcount[src * spec->fanout + j] = static_cast<uint8_t>(r.range(spec->codes_min, spec->codes_max));
-        });
-        out->code_offset_ptr[0] = 0;
-        for (uint64_t s = 0; s < S; ++s) out->code_offset_ptr[s + 1] = out->code_offset_ptr[s] + kcount[s];
-        out->code_count = out->code_offset_ptr[S];
-        out->code_offsets = new uint32_t[out->code_count > 0 ? out->code_count : 1];
-        parallel_for(N, [&](uint64_t src) {
-            Stream r(spec->seed, 2 * src);
-            Stream rc(spec->seed, 2 * src + 1);
-            for (uint32_t j = 0; j < spec->fanout; ++j) rc.next();  // skip the counts drawn above
-            const bool exc = src < spec->excitatory_count;
-            for (uint32_t j = 0; j < spec->fanout; ++j) {
-                const uint64_t s = src * spec->fanout + j;
-                out->source[s] = static_cast<uint32_t>(src);
-                out->target[s] = r.below(N);
-                float w;
-                if (spec->weight_kind == 0) {
-                    w = exc ? static_cast<float>(0.5 * r.uniform()) : static_cast<float>(-r.uniform());
-                    out->receptor[s] = 0;  // AMPA
-                    out->compartment[s] = exc ? static_cast<uint8_t>(1 + (j & 1)) : 3;
+    const uint32_t F = spec->fanout;
+    parallel_for(N, [&](uint64_t i) {
+        out->threshold[i] = spec->threshold;
+        out->pattern_window_ticks[i] = spec->pattern_window_ticks;
+        out->similarity_threshold[i] = spec->similarity_threshold;
+        out->max_reference_patterns[i] = spec->max_reference_patterns;
+    });
+    // Code counts per synapse (stream 2*src+1) into code_offset_ptr[s+1], then
+    // an in-place prefix sum.
+    out->code_offset_ptr[0] = 0;
+    parallel_for(N, [&](uint64_t src) {
+        Stream r(spec->seed, 2 * src + 1);
+        for (uint32_t j = 0; j < F; ++j) out->code_offset_ptr[src * F + j + 1] = r.range(spec->codes_min, spec->codes_max);
+    });
+    for (uint64_t s = 0; s < S; ++s) out->code_offset_ptr[s + 1] += out->code_offset_ptr[s];
+    *code_count = out->code_offset_ptr[S];
+    parallel_for(N, [&](uint64_t src) {
+        Stream r(spec->seed, 2 * src);
+        Stream rc(spec->seed, 2 * src + 1);
+        for (uint32_t j = 0; j < F; ++j) rc.next();  // skip the counts drawn above
+        const bool exc = src < spec->excitatory_count;
+        for (uint32_t j = 0; j < F; ++j) {
+            const uint64_t s = src * F + j;
+            out->source[s] = static_cast<uint32_t>(src);
+            out->target[s] = r.below(N);
+            float w;
+            if (spec->weight_kind == 0) {
+                w = exc ? static_cast<float>(0.5 * r.uniform()) : static_cast<float>(-r.uniform());
+                out->receptor[s] = 0;  // AMPA
+                out->compartment[s] = exc ? static_cast<uint8_t>(1 + (j & 1)) : 3;
+            } else {
+                const double z = det_normal(r);
+                w = static_cast<float>(det_exp(spec->lognormal_mu + spec->lognormal_sigma * z));
+                if (exc) {
+                    const uint8_t comp = spec->compartments == 4 ? static_cast<uint8_t>(r.below(3))
+                                                                 : static_cast<uint8_t>(1 + (j & 1));
+                    out->compartment[s] = comp;
+                    out->receptor[s] = comp == 2 ? 1 : 0;  // apical NMDA, else AMPA
                 } else {
-                    const double z = det_normal(r);
-                    w = static_cast<float>(det_exp(spec->lognormal_mu + spec->lognormal_sigma * z));
-                    if (exc) {
-                        const uint8_t comp = spec->compartments == 4 ? static_cast<uint8_t>(r.below(3))
-                                                                     : static_cast<uint8_t>(1 + (j & 1));
-                        out->compartment[s] = comp;
-                        out->receptor[s] = comp == 2 ? 1 : 0;  // apical NMDA, else AMPA
-                    } else {
-                        out->compartment[s] = 3;
-                        out->receptor[s] = 2;  // GABA_A, positive magnitude
-                    }
+                    out->compartment[s] = 3;
+                    out->receptor[s] = 2;  // GABA_A, positive magnitude
                 }
-                out->weight[s] = w * spec->weight_scale;
-                out->max_weight[s] = spec->max_weight;
-                out->delay_ticks[s] = r.range(spec->delay_min, spec->delay_max);
-                out->plasticity_enabled[s] = spec->plastic;
-                for (uint64_t k = out->code_offset_ptr[s]; k < out->code_offset_ptr[s + 1]; ++k)
-                    out->code_offsets[k] = rc.range(0, spec->code_offset_max);
             }
-        });
-        return 0;
-    } catch (const std::bad_alloc&) {
-        snngen_free_network(out);
-        return 2;
-    }
+            out->weight[s] = w * spec->weight_scale;
+            out->max_weight[s] = spec->max_weight;
+            out->delay_ticks[s] = r.range(spec->delay_min, spec->delay_max);
+            out->plasticity_enabled[s] = spec->plastic;
+            for (uint64_t k = out->code_offset_ptr[s]; k < out->code_offset_ptr[s + 1]; ++k)
+                out->code_offsets[k] = rc.range(0, spec->code_offset_max);
+        }
+    });
+    return 0;
 }
 
 typedef struct snngen_drive {

@@ -734,6 +734,7 @@ __global__ void k_fire_list(Engine e) {
         const uint32_t due = ts->n_due;
         ts->delivered += due;
         ts->fired += nfires;
+        ts->touched_total += ts->n_touched;
         if (due > ts->max_slot_events) ts->max_slot_events = due;
         if (e.raster_cap > 0) {
             if (raster0 + nfires > e.raster_cap) raise_status(e, kStatusRasterOverflow);
@@ -814,18 +815,29 @@ __global__ void k_inject(Engine e, const unsigned long long* ev, const uint32_t*
 
 }  // namespace
 
-void launch_tick(const Engine& e, cudaStream_t stream) {
+void launch_tick(const Engine& e, cudaStream_t stream, cudaEvent_t* marks) {
     const uint32_t tiles = (e.N + kScanTile - 1) / kScanTile;
     const uint32_t wide = e.grid_wide;
     const uint32_t scan_grid = tiles == 0 ? 1 : (tiles < wide ? tiles : wide);
-    k_hist<<<wide, kThreads, 0, stream>>>(e);
-    k_scan_tile<<<scan_grid, kThreads, 0, stream>>>(e);
-    k_scan_out<<<scan_grid, kThreads, 0, stream>>>(e);
-    k_scatter<<<wide, kThreads, 0, stream>>>(e);
-    k_process<<<e.grid_process, kThreads, 0, stream>>>(e);
-    k_post<<<wide, kThreads, 0, stream>>>(e);
-    k_fire_list<<<e.grid_fire, kThreads, 0, stream>>>(e);
-    k_expand<<<wide, kThreads, 0, stream>>>(e);
+    int k = 0;
+    auto mark = [&](bool after) {
+        if (marks) cudaEventRecordWithFlags(marks[2 * k + (after ? 1 : 0)], stream, cudaEventRecordExternal);
+        if (after) ++k;
+    };
+    mark(false); k_hist<<<wide, kThreads, 0, stream>>>(e); mark(true);
+    mark(false); k_scan_tile<<<scan_grid, kThreads, 0, stream>>>(e); mark(true);
+    mark(false); k_scan_out<<<scan_grid, kThreads, 0, stream>>>(e); mark(true);
+    mark(false); k_scatter<<<wide, kThreads, 0, stream>>>(e); mark(true);
+    mark(false); k_process<<<e.grid_process, kThreads, 0, stream>>>(e); mark(true);
+    mark(false); k_post<<<wide, kThreads, 0, stream>>>(e); mark(true);
+    mark(false); k_fire_list<<<e.grid_fire, kThreads, 0, stream>>>(e); mark(true);
+    mark(false); k_expand<<<wide, kThreads, 0, stream>>>(e); mark(true);
+}
+
+const char* kernel_name(int index) {
+    static const char* names[kKernelCount] = {"k_hist", "k_scan_tile", "k_scan_out", "k_scatter",
+                                              "k_process", "k_post", "k_fire_list", "k_expand"};
+    return index >= 0 && index < kKernelCount ? names[index] : "";
 }
 
 void launch_inject(const Engine& e, const unsigned long long* ev, const uint32_t* slot_of_group,

@@ -137,6 +137,10 @@ struct snncuda_sim {
     unsigned long long* far_ev{nullptr};
     uint32_t* far_idx{nullptr};
     size_t far_ev_cap{0}, far_idx_cap{0};
+    // pinned host staging for injected events and their slot/tick indices
+    unsigned long long* host_ev{nullptr};
+    uint32_t* host_idx{nullptr};
+    size_t host_ev_cap{0}, host_idx_cap{0};
     // injection staging
     unsigned long long* inj_ev{nullptr};
     uint32_t* inj_slot{nullptr};
@@ -145,11 +149,16 @@ struct snncuda_sim {
     // graphs
     cudaGraphExec_t graph_many{nullptr};
     cudaGraphExec_t graph_one{nullptr};
+    cudaGraphExec_t graph_prof{nullptr};
+    cudaEvent_t marks[2 * kKernelCount]{};
     static constexpr int kTicksPerGraph = 16;
 
     ~snncuda_sim() {
         if (graph_many) cudaGraphExecDestroy(graph_many);
         if (graph_one) cudaGraphExecDestroy(graph_one);
+        if (graph_prof) cudaGraphExecDestroy(graph_prof);
+        for (cudaEvent_t ev : marks)
+            if (ev) cudaEventDestroy(ev);
         if (stream) cudaStreamSynchronize(stream);
         for (void* p : owned) cudaFree(p);
         if (far_ev) cudaFree(far_ev);
@@ -157,19 +166,40 @@ struct snncuda_sim {
         if (inj_ev) cudaFree(inj_ev);
         if (inj_slot) cudaFree(inj_slot);
         if (inj_off) cudaFree(inj_off);
+        if (host_ev) cudaFreeHost(host_ev);
+        if (host_idx) cudaFreeHost(host_idx);
         if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+
+    // Pinned host buffers for the host->device copies of injected events.
+    void ensure_host(size_t events, size_t idx) {
+        if (events > host_ev_cap) {
+            if (host_ev) cudaFreeHost(host_ev);
+            host_ev = nullptr;
+            host_ev_cap = std::max<size_t>(events, 2 * host_ev_cap);
+            check(cudaMallocHost(&host_ev, host_ev_cap * sizeof(unsigned long long)), "pinned staging");
+        }
+        if (idx > host_idx_cap) {
+            if (host_idx) cudaFreeHost(host_idx);
+            host_idx = nullptr;
+            host_idx_cap = std::max<size_t>(idx, 2 * host_idx_cap);
+            check(cudaMallocHost(&host_idx, host_idx_cap * sizeof(uint32_t)), "pinned staging");
+        }
     }
 
     void drop_graphs() {
         if (graph_many) cudaGraphExecDestroy(graph_many);
         if (graph_one) cudaGraphExecDestroy(graph_one);
-        graph_many = graph_one = nullptr;
+        if (graph_prof) cudaGraphExecDestroy(graph_prof);
+        graph_many = graph_one = graph_prof = nullptr;
     }
 
-    cudaGraphExec_t capture(int ticks) {
+    cudaGraphExec_t capture(int ticks, bool profiled = false) {
         cudaGraph_t g = nullptr;
+        if (profiled && marks[0] == nullptr)
+            for (cudaEvent_t& ev : marks) check(cudaEventCreate(&ev), "event");
         check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-        for (int i = 0; i < ticks; ++i) launch_tick(e, stream);
+        for (int i = 0; i < ticks; ++i) launch_tick(e, stream, profiled ? marks : nullptr);
         check(cudaStreamEndCapture(stream, &g), "end capture");
         cudaGraphExec_t exec = nullptr;
         const cudaError_t err = cudaGraphInstantiate(&exec, g, 0);
@@ -553,7 +583,7 @@ int status_to_error(uint32_t status, std::string& msg) {
     return SNNCUDA_ERR_CAPACITY;
 }
 
-void run_impl(snncuda_sim* sim, uint64_t T) {
+void run_impl(snncuda_sim* sim, uint64_t T, snncuda_profile* prof = nullptr) {
     const uint64_t p = sim->next_tick;
     if (T < p) return;
     if (T >= 0xFFFF0000ull) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "ticks beyond 2^32 - 2^16");
@@ -570,10 +600,8 @@ void run_impl(snncuda_sim* sim, uint64_t T) {
     while (b_end < sim->pending.size() && sim->pending[b_end].tick <= T + W - 1) ++b_end;
     cudaStream_t st = sim->stream;
     if (a_end > 0) {
-        std::vector<unsigned long long> ev(a_end);
         std::vector<uint32_t> slots, offs;
         for (size_t i = 0; i < a_end; ++i) {
-            ev[i] = sim->pending[i].event;
             const uint32_t slot = static_cast<uint32_t>(sim->pending[i].tick & (W - 1));
             if (i == 0 || sim->pending[i].tick != sim->pending[i - 1].tick) {
                 slots.push_back(slot);
@@ -582,9 +610,15 @@ void run_impl(snncuda_sim* sim, uint64_t T) {
         }
         offs.push_back(static_cast<uint32_t>(a_end));
         sim->ensure_inject(a_end, slots.size());
-        check(cudaMemcpyAsync(sim->inj_ev, ev.data(), a_end * 8, cudaMemcpyHostToDevice, st), "inject copy");
-        check(cudaMemcpyAsync(sim->inj_slot, slots.data(), slots.size() * 4, cudaMemcpyHostToDevice, st), "inject copy");
-        check(cudaMemcpyAsync(sim->inj_off, offs.data(), offs.size() * 4, cudaMemcpyHostToDevice, st), "inject copy");
+        sim->ensure_host(a_end, 2 * slots.size() + 1);
+        for (size_t i = 0; i < a_end; ++i) sim->host_ev[i] = sim->pending[i].event;
+        std::copy(slots.begin(), slots.end(), sim->host_idx);
+        std::copy(offs.begin(), offs.end(), sim->host_idx + slots.size());
+        check(cudaMemcpyAsync(sim->inj_ev, sim->host_ev, a_end * 8, cudaMemcpyHostToDevice, st), "inject copy");
+        check(cudaMemcpyAsync(sim->inj_slot, sim->host_idx, slots.size() * 4, cudaMemcpyHostToDevice, st),
+              "inject copy");
+        check(cudaMemcpyAsync(sim->inj_off, sim->host_idx + slots.size(), offs.size() * 4, cudaMemcpyHostToDevice,
+                              st), "inject copy");
         launch_inject(e, sim->inj_ev, sim->inj_slot, sim->inj_off, static_cast<uint32_t>(slots.size()), st);
         check(cudaGetLastError(), "inject launch");
         check(cudaStreamSynchronize(st), "inject synchronize");
@@ -595,16 +629,19 @@ void run_impl(snncuda_sim* sim, uint64_t T) {
         far_ticks = static_cast<uint32_t>(T + W - 1 - (p + W) + 1);  // deliveries p+W .. T+W-1
         const size_t n = b_end - a_end;
         sim->ensure_far(n, static_cast<size_t>(far_ticks) + 1);
-        std::vector<unsigned long long> ev(n);
-        std::vector<uint32_t> idx(static_cast<size_t>(far_ticks) + 1, 0);
+        sim->ensure_host(n, static_cast<size_t>(far_ticks) + 1);
+        uint32_t* idx = sim->host_idx;
+        std::fill(idx, idx + far_ticks + 1, 0u);
         for (size_t i = 0; i < n; ++i) {
             const Pending& q = sim->pending[a_end + i];
-            ev[i] = q.event;
+            sim->host_ev[i] = q.event;
             idx[q.tick - far_first + 1] += 1;
         }
-        for (size_t i = 1; i < idx.size(); ++i) idx[i] += idx[i - 1];
-        check(cudaMemcpyAsync(sim->far_ev, ev.data(), n * 8, cudaMemcpyHostToDevice, st), "far copy");
-        check(cudaMemcpyAsync(sim->far_idx, idx.data(), idx.size() * 4, cudaMemcpyHostToDevice, st), "far copy");
+        for (size_t i = 1; i <= far_ticks; ++i) idx[i] += idx[i - 1];
+        check(cudaMemcpyAsync(sim->far_ev, sim->host_ev, n * 8, cudaMemcpyHostToDevice, st), "far copy");
+        check(cudaMemcpyAsync(sim->far_idx, idx, (static_cast<size_t>(far_ticks) + 1) * 4, cudaMemcpyHostToDevice,
+                              st), "far copy");
+        check(cudaStreamSynchronize(st), "far copy");
     }
     sim->pending.erase(sim->pending.begin(), sim->pending.begin() + static_cast<std::ptrdiff_t>(b_end));
     // run parameters live in device memory so the captured graphs stay valid
@@ -613,9 +650,29 @@ void run_impl(snncuda_sim* sim, uint64_t T) {
     check(cudaMemcpyAsync(reinterpret_cast<char*>(e.ts) + offsetof(TickState, far_ticks), &far_ticks, 4,
                           cudaMemcpyHostToDevice, st), "run params");
     uint64_t ticks = T - p + 1;
+    if (prof != nullptr) {
+        const TickState before = sim->read_ts();
+        if (sim->graph_prof == nullptr) sim->graph_prof = sim->capture(1, true);
+        for (uint64_t i = 0; i < ticks; ++i) {
+            check(cudaGraphLaunch(sim->graph_prof, st), "graph launch");
+            check(cudaStreamSynchronize(st), "profile synchronize");
+            for (int k = 0; k < kKernelCount; ++k) {
+                float ms = 0.0F;
+                check(cudaEventElapsedTime(&ms, sim->marks[2 * k], sim->marks[2 * k + 1]), "event time");
+                prof->kernel_ms[k] += ms;
+            }
+        }
+        const TickState after = sim->read_ts();
+        prof->ticks += ticks;
+        prof->synaptic_events += (after.delivered - after.external) - (before.delivered - before.external);
+        prof->external_events += after.external - before.external;
+        prof->fires += after.fired - before.fired;
+        prof->touched_targets += after.touched_total - before.touched_total;
+        ticks = 0;
+    }
     if (ticks >= static_cast<uint64_t>(snncuda_sim::kTicksPerGraph) && sim->graph_many == nullptr)
         sim->graph_many = sim->capture(snncuda_sim::kTicksPerGraph);
-    if (sim->graph_one == nullptr) sim->graph_one = sim->capture(1);
+    if (ticks > 0 && sim->graph_one == nullptr) sim->graph_one = sim->capture(1);
     while (ticks >= static_cast<uint64_t>(snncuda_sim::kTicksPerGraph)) {
         check(cudaGraphLaunch(sim->graph_many, st), "graph launch");
         ticks -= snncuda_sim::kTicksPerGraph;
@@ -996,6 +1053,16 @@ int snncuda_sim_state_digest(snncuda_sim* sim, uint64_t* neuron_digest, uint64_t
         }
     });
 }
+
+int snncuda_sim_profile(snncuda_sim* sim, uint64_t inclusive_tick, snncuda_profile* out) {
+    if (sim == nullptr || out == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
+    if (sim->poisoned) return set_error(SNNCUDA_ERR_POISONED, "simulation poisoned by an earlier device error");
+    const int rc = guarded([&] { run_impl(sim, inclusive_tick, out); });
+    if (rc == SNNCUDA_ERR_DEVICE) sim->poisoned = true;
+    return rc;
+}
+
+const char* snncuda_kernel_name(int32_t index) { return kernel_name(index); }
 
 int snncuda_sim_read_raster(snncuda_sim* sim, uint64_t first, uint64_t count, uint64_t* ticks, uint32_t* neurons) {
     if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");

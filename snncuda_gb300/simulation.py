@@ -202,18 +202,30 @@ class Simulation:
                 ctypes.byref(length)))
         return [int(v) for v in buf[:length.value]]
 
+    def profile(self, inclusive_tick: int) -> Dict[str, object]:
+        """Run to `inclusive_tick` one tick at a time with per-kernel device
+        timing (engine extension; CPU implementations fill only counters)."""
+        out = _abi.Profile()
+        _check(self.lib, self.lib.snncuda_sim_profile(self.handle, int(inclusive_tick), ctypes.byref(out)))
+        names = [self.lib.snncuda_kernel_name(k).decode() for k in range(_abi.KERNEL_COUNT)]
+        return {"ticks": int(out.ticks), "kernel_ms": dict(zip(names, list(out.kernel_ms))),
+                "synaptic_events": int(out.synaptic_events), "external_events": int(out.external_events),
+                "fires": int(out.fires), "touched_targets": int(out.touched_targets)}
+
     def digest(self) -> tuple:
         a, b = c_uint64(), c_uint64()
         _check(self.lib, self.lib.snncuda_sim_state_digest(self.handle, ctypes.byref(a), ctypes.byref(b)))
         return int(a.value), int(b.value)
 
-    def raster(self) -> tuple:
-        count = self.counters()["raster_count"]
+    def raster(self, first: int = 0, count: Optional[int] = None) -> tuple:
+        """Fire records [first, first+count) as (ticks, neurons); all by default."""
+        if count is None:
+            count = self.counters()["raster_count"] - first
         ticks = np.zeros(count, np.uint64)
         neurons = np.zeros(count, np.uint32)
         if count:
             _check(self.lib, self.lib.snncuda_sim_read_raster(
-                self.handle, 0, count, _abi.ptr(ticks, c_uint64), _abi.ptr(neurons, c_uint32)))
+                self.handle, first, count, _abi.ptr(ticks, c_uint64), _abi.ptr(neurons, c_uint32)))
         return ticks, neurons
 
 

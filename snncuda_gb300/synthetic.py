@@ -59,7 +59,6 @@ class _Spec(Structure):
 
 class _Net(Structure):
     _fields_ = [
-        ("neuron_count", c_uint32), ("synapse_count", c_uint64), ("code_count", c_uint64),
         ("threshold", POINTER(c_float)), ("pattern_window_ticks", POINTER(c_uint64)),
         ("similarity_threshold", POINTER(c_float)), ("max_reference_patterns", POINTER(c_uint64)),
         ("source", POINTER(c_uint32)), ("target", POINTER(c_uint32)), ("weight", POINTER(c_float)),
@@ -85,9 +84,8 @@ def _lib():
         if not pathlib.Path(path).exists():
             raise RuntimeError(f"generator library missing at {path}; run __graft_entry__.build()")
         _gen = ctypes.CDLL(path)
-        _gen.snngen_build_network.argtypes = [POINTER(_Spec), POINTER(_Net)]
-        _gen.snngen_build_network.restype = c_int
-        _gen.snngen_free_network.argtypes = [POINTER(_Net)]
+        _gen.snngen_fill_network.argtypes = [POINTER(_Spec), POINTER(_Net), POINTER(c_uint64)]
+        _gen.snngen_fill_network.restype = c_int
         _gen.snngen_build_drive.argtypes = [
             c_uint32, c_uint32, c_uint64, c_double, c_float, c_uint32, c_uint32, c_uint32, c_uint32,
             c_uint32, c_uint32, c_float, c_uint64, POINTER(_Drive)]
@@ -150,9 +148,13 @@ WORKLOADS = {w.name: w for w in (PLAIN_1K, STDP_100K, RECOG_1M)}
 
 
 def _view(ptr, n, dtype):
+    """Copy n elements of a generator-owned C array into a numpy array."""
+    dtype = np.dtype(dtype)
     if n == 0:
         return np.zeros(0, dtype=dtype)
-    return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
+    addr = ctypes.cast(ptr, ctypes.c_void_p).value
+    raw = (ctypes.c_char * (int(n) * dtype.itemsize)).from_address(addr)
+    return np.frombuffer(raw, dtype=dtype).copy()
 
 
 def build_network(w: Workload) -> Connectome:
@@ -161,29 +163,26 @@ def build_network(w: Workload) -> Connectome:
         w.weight_scale, w.lognormal[0], w.lognormal[1], w.max_weight, w.delay[0], w.delay[1],
         w.codes[0], w.codes[1], w.code_offset_max, w.compartments, 1 if w.plastic else 0,
         w.threshold, w.pattern_window_ticks, w.similarity_threshold, w.max_reference_patterns, w.seed)
-    net = _Net()
-    lib = _lib()
-    rc = lib.snngen_build_network(ctypes.byref(spec), ctypes.byref(net))
+    n, s = w.neurons, w.neurons * w.fanout
+    a = dict(threshold=np.empty(n, np.float32), pattern_window_ticks=np.empty(n, np.uint64),
+             similarity_threshold=np.empty(n, np.float32), max_reference_patterns=np.empty(n, np.uint64),
+             source=np.empty(s, np.uint32), target=np.empty(s, np.uint32), weight=np.empty(s, np.float32),
+             max_weight=np.empty(s, np.float32), delay_ticks=np.empty(s, np.uint32),
+             compartment=np.empty(s, np.uint8), receptor=np.empty(s, np.uint8),
+             plasticity_enabled=np.empty(s, np.uint8), code_offset_ptr=np.empty(s + 1, np.uint64),
+             code_offsets=np.empty(max(1, s * w.codes[1]), np.uint32))
+    types = dict(_Net._fields_)
+    net = _Net(**{k: v.ctypes.data_as(types[k]) for k, v in a.items()})
+    count = c_uint64()
+    rc = _lib().snngen_fill_network(ctypes.byref(spec), ctypes.byref(net), ctypes.byref(count))
     if rc != 0:
         raise RuntimeError(f"network generation failed ({rc})")
-    try:
-        n, s, k = net.neuron_count, net.synapse_count, net.code_count
-        single = w.codes == (1, 1) and w.code_offset_max == 0
-        return Connectome(
-            threshold=_view(net.threshold, n, np.float32),
-            pattern_window_ticks=_view(net.pattern_window_ticks, n, np.uint64),
-            similarity_threshold=_view(net.similarity_threshold, n, np.float32),
-            max_reference_patterns=_view(net.max_reference_patterns, n, np.uint64),
-            source=_view(net.source, s, np.uint32), target=_view(net.target, s, np.uint32),
-            weight=_view(net.weight, s, np.float32), max_weight=_view(net.max_weight, s, np.float32),
-            delay_ticks=_view(net.delay_ticks, s, np.uint32),
-            compartment=_view(net.compartment, s, np.uint8), receptor=_view(net.receptor, s, np.uint8),
-            plasticity_enabled=_view(net.plasticity_enabled, s, np.uint8),
-            code_offset_ptr=None if single else _view(net.code_offset_ptr, s + 1, np.uint64),
-            code_offsets=None if single else _view(net.code_offsets, k, np.uint32),
-        )
-    finally:
-        lib.snngen_free_network(ctypes.byref(net))
+    single = w.codes == (1, 1) and w.code_offset_max == 0
+    if single:
+        a["code_offset_ptr"] = a["code_offsets"] = None
+    else:
+        a["code_offsets"] = a["code_offsets"][:count.value]
+    return Connectome(**a)
 
 
 def build_drive(w: Workload, ticks: Optional[int] = None):

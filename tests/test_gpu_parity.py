@@ -50,7 +50,7 @@ def _compare(gpu_lib, port_lib, net, drive, ticks, cfg, *, toggles=()):
     return cg
 
 
-@pytest.mark.parametrize("neurons,fanout,ticks,g", [(20_000, 200, 300, 0.05), (5_000, 1000, 200, 0.02)])
+@pytest.mark.parametrize("neurons,fanout,ticks,g", [(20_000, 200, 300, 0.05), (5_000, 1000, 200, 0.01)])
 def test_stdp_network_matches_oracle(gpu_lib, port_lib, neurons, fanout, ticks, g):
     w = synthetic.STDP_100K.scaled(neurons=neurons, fanout=fanout, weight_scale=g, seed=21)
     net = synthetic.build_network(w)
