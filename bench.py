@@ -126,7 +126,7 @@ def sim_config(lib, w, **extra):
     from snncuda_gb300.simulation import default_config
     cfg = default_config(lib, **extra)
     cfg.stdp_enabled = 1 if w.stdp_enabled else 0
-    cfg.max_weight = w.max_weight
+    cfg.max_weight = 1.0  # StdpConfig clip [0, 1]; synapses carry their own max_weight
     return cfg
 
 

@@ -112,7 +112,7 @@ class SynapseState(Structure):
     ]
 
 
-KERNEL_COUNT = 8
+KERNEL_COUNT = 9
 
 
 class Profile(Structure):

@@ -138,6 +138,8 @@ struct NState {
     uint32_t spikes, last_fired1, last_active, match_count, ws, len;
     unsigned long long cn;
     uint32_t nruns, ref_head, ref_count, ring_head, ring_used;
+    unsigned long long last_run;  // cand[nruns-1], kept in a register while nruns > 0
+    RefMeta one;                  // the learned pattern when max_reference_patterns == 1
 };
 
 __device__ __forceinline__ float decay_factor(const Tables& tb, uint32_t code, uint32_t elapsed) {
@@ -149,6 +151,9 @@ __device__ __forceinline__ float decay_factor(const Tables& tb, uint32_t code, u
 // representation: offsets inside a window never decrease, so the window is
 // kept as runs (value, count); learned patterns are run lists in a per-neuron
 // ring, each with running integer sums of its cosine against the window.
+// kOne: max_reference_patterns == 1, the single pattern's sums live in
+// registers (s.one) for the whole of the target's events in a tick.
+template <bool kOne>
 __device__ void temporal_update(NState& s, const NeuronParam& p, uint32_t t, const Engine& e, int enabled) {
     if (!enabled) {
         s.flags &= ~(1u << 8);
@@ -157,13 +162,20 @@ __device__ void temporal_update(NState& s, const NeuronParam& p, uint32_t t, con
     unsigned long long* cand = e.cand + p.cand_base;
     RefMeta* meta = e.refmeta + p.meta_base;
     unsigned long long* ring = e.ring + p.ring_base;
+    auto ref = [&](uint32_t r) -> RefMeta& {
+        if constexpr (kOne) {
+            return s.one;
+        } else {
+            return meta[(s.ref_head + r) % p.max_refs];
+        }
+    };
     if (s.len == 0 || t - s.ws > p.window) {
         s.ws = t;
         s.len = 0;
         s.nruns = 0;
         s.cn = 0;
         for (uint32_t r = 0; r < s.ref_count; ++r) {
-            RefMeta& m = meta[(s.ref_head + r) % p.max_refs];
+            RefMeta& m = ref(r);
             m.dot = 0;
             m.rn = 0;
             m.cn = 0;
@@ -174,19 +186,21 @@ __device__ void temporal_update(NState& s, const NeuronParam& p, uint32_t t, con
     }
     const uint32_t o = t - s.ws;
     const unsigned long long oo = static_cast<unsigned long long>(o) * o;
-    if (s.nruns > 0 && run_value(cand[s.nruns - 1]) == o) {
-        cand[s.nruns - 1] += (1ull << 16);
+    if (s.nruns > 0 && run_value(s.last_run) == o) {
+        s.last_run += (1ull << 16);
     } else {
         if (s.nruns > p.window) {  // cannot happen: at most window+1 distinct offsets
             raise_status(e, kStatusRunOverflow);
             return;
         }
-        cand[s.nruns++] = static_cast<unsigned long long>(o) | (1ull << 16);
+        if (s.nruns > 0) cand[s.nruns - 1] = s.last_run;
+        s.last_run = static_cast<unsigned long long>(o) | (1ull << 16);
+        s.nruns += 1;
     }
     s.len += 1;
     s.cn += oo;
     for (uint32_t r = 0; r < s.ref_count; ++r) {
-        RefMeta& m = meta[(s.ref_head + r) % p.max_refs];
+        RefMeta& m = ref(r);
         if (s.len <= m.len) {
             const unsigned long long run = ring[(m.start + m.cur_run) % p.ring_cap];
             const unsigned long long v = run_value(run);
@@ -206,7 +220,7 @@ __device__ void temporal_update(NState& s, const NeuronParam& p, uint32_t t, con
             match = true;
         } else {
             for (uint32_t r = 0; r < s.ref_count && !match; ++r) {
-                RefMeta& m = meta[(s.ref_head + r) % p.max_refs];
+                RefMeta& m = ref(r);
                 if (m.match == 2) m.match = cos_ge(m.dot, m.rn, m.cn, p.similarity) ? 1 : 0;
                 match = m.match == 1;
             }
@@ -221,7 +235,7 @@ __device__ void temporal_update(NState& s, const NeuronParam& p, uint32_t t, con
     if (s.len < 2) return;
     // learn_pattern: FIFO with max_reference_patterns entries.
     if (s.ref_count >= p.max_refs) {
-        s.ring_used -= meta[s.ref_head].nruns;
+        s.ring_used -= ref(0).nruns;
         s.ref_head = (s.ref_head + 1) % p.max_refs;
         s.ref_count -= 1;
     }
@@ -229,12 +243,12 @@ __device__ void temporal_update(NState& s, const NeuronParam& p, uint32_t t, con
         raise_status(e, kStatusRingOverflow);
         return;
     }
-    const uint32_t idx = (s.ref_head + s.ref_count) % p.max_refs;
+    cand[s.nruns - 1] = s.last_run;
     const uint32_t start = s.ring_head;
     for (uint32_t j = 0; j < s.nruns; ++j) ring[(start + j) % p.ring_cap] = cand[j];
     s.ring_head = (start + s.nruns) % p.ring_cap;
     s.ring_used += s.nruns;
-    RefMeta& m = meta[idx];
+    RefMeta& m = ref(s.ref_count);
     m.dot = s.cn;
     m.rn = s.cn;
     m.cn = s.cn;
@@ -248,6 +262,7 @@ __device__ void temporal_update(NState& s, const NeuronParam& p, uint32_t t, con
 }
 
 // SynapseDendriteProcessor.cpp:175-229.  Returns whether the neuron fired.
+template <bool kOne>
 __device__ bool process_input(NState& s, const NeuronParam& p, uint32_t comp, uint32_t rec, float w,
                               uint32_t t, const Engine& e, int temporal) {
 #pragma unroll
@@ -270,7 +285,7 @@ __device__ bool process_input(NState& s, const NeuronParam& p, uint32_t comp, ui
         }
     }
     s.last_active = t;
-    temporal_update(s, p, t, e, temporal);
+    temporal_update<kOne>(s, p, t, e, temporal);
     s.membrane = __fadd_rn(__fadd_rn(__fadd_rn(s.cur[0], s.cur[1]), s.cur[2]), s.cur[3]);
     if (s.membrane >= p.threshold) {
         s.membrane = 0.0f;
@@ -486,13 +501,138 @@ __global__ void k_scatter(Engine e) {
     }
 }
 
-// One thread per touched target: the reference's sequential per-event loop
-// (NetworkPropagator.cpp:80-131) restricted to this target, which is exact
-// because every state an event reads or writes belongs to its target (the
-// target's neuron state and the target's incoming synapses).  Post-spike
-// STDP of a fire is applied lazily to synapses touched later in the tick
-// and in bulk by k_post for the rest.
+constexpr int kSegCache = 24;  // due events per target sorted in shared memory
+
+// The events of one target in due order, then the reference's sequential
+// per-event loop (NetworkPropagator.cpp:80-131) restricted to this target.
+// Synapse records of the next event are loaded while the current one is
+// processed; a repeat of the same synapse takes the just-updated record.
+template <bool kOne>
+__device__ __forceinline__ void process_target(const Engine& e, uint32_t n, const unsigned long long* g,
+                                               uint32_t len, uint32_t stride, uint32_t t, int stdp,
+                                               int temporal) {
+    const NeuronParam p = e.nparam[n];
+    const NeuronRec r = e.nrec[n];
+    const NeuronTp q = e.ntp[n];
+    NState s;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        s.cur[c] = r.cur[c];
+        s.upd[c] = r.upd[c];
+    }
+    s.flags = r.flags;
+    s.membrane = r.membrane;
+    s.spikes = r.spike_count;
+    s.last_fired1 = r.last_fired1;
+    s.last_active = r.last_active;
+    s.match_count = r.match_count;
+    s.ws = r.ws;
+    s.len = r.len;
+    s.cn = q.cn;
+    s.nruns = q.nruns;
+    s.ref_head = q.ref_head;
+    s.ref_count = q.ref_count;
+    s.ring_head = q.ring_head;
+    s.ring_used = q.ring_used;
+    s.last_run = s.nruns > 0 ? e.cand[p.cand_base + s.nruns - 1] : 0ull;
+    if (kOne && s.ref_count > 0) s.one = e.refmeta[p.meta_base];
+
+    uint32_t fires = 0;
+    unsigned long long x = g[0];
+    SynA na{};
+    SynB nb{};
+    if (!(static_cast<uint32_t>(x) & kExternalBit)) {
+        const uint32_t tm = static_cast<uint32_t>(x >> 32);
+        na = e.syna[tm];
+        nb = e.synb[tm];
+    }
+    for (uint32_t i = 0; i < len; ++i) {
+        const unsigned long long cur = x;
+        SynA a = na;
+        SynB b = nb;
+        const bool external = static_cast<uint32_t>(cur) & kExternalBit;
+        const uint32_t payload = static_cast<uint32_t>(cur >> 32);
+        bool same_next = false;
+        if (i + 1 < len) {  // prefetch the next event's synapse records
+            x = g[static_cast<size_t>(i + 1) * stride];
+            if (!(static_cast<uint32_t>(x) & kExternalBit)) {
+                const uint32_t tm = static_cast<uint32_t>(x >> 32);
+                same_next = !external && tm == payload;
+                if (!same_next) {
+                    na = e.syna[tm];
+                    nb = e.synb[tm];
+                }
+            }
+        }
+        const uint32_t due = static_cast<uint32_t>(cur) & ~kExternalBit;
+        bool fired;
+        if (external) {
+            fired = process_input<kOne>(s, p, 0u, 0u, __uint_as_float(payload), t, e, temporal);
+        } else {
+            const uint32_t tm = payload;
+            post_catch_up(a, t, fires, e, stdp);
+            const uint32_t delay = a.meta & kMetaDelayMask;
+            const uint32_t pre_tick = t >= delay ? t - delay : t;
+            const bool plastic = (a.meta >> kMetaPlasticBit) & 1u;
+            if (plastic && a.last_post1 != 0) stdp_apply(a, pre_tick, a.last_post1 - 1, e, stdp);
+            a.last_pre1 = pre_tick + 1;
+            b.pre_count += 1;
+            fired = process_input<kOne>(s, p, (a.meta >> kMetaCompShift) & 3u, (a.meta >> kMetaRecShift) & 3u,
+                                        a.weight, t, e, temporal);
+            uint16_t* lc = e.lcode + p.lcode_base + static_cast<size_t>(tm - p.in_begin) * p.max_refs * e.code_stride;
+            code_update(b, a.meta, p, t, lc, e.code_stride, temporal);
+            e.syna[tm] = a;
+            e.synb[tm] = b;
+            if (same_next) {
+                na = a;
+                nb = b;
+            }
+        }
+        if (fired) {
+            fires += 1;
+            atomicOr(&e.fire_bits[due >> 5], 1u << (due & 31));
+            e.fire_at[due] = n;
+        }
+    }
+    if (s.nruns > 0) e.cand[p.cand_base + s.nruns - 1] = s.last_run;
+    if (kOne && s.ref_count > 0) e.refmeta[p.meta_base] = s.one;
+    NeuronRec w;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        w.cur[c] = s.cur[c];
+        w.upd[c] = s.upd[c];
+    }
+    w.flags = s.flags;
+    w.membrane = s.membrane;
+    w.spike_count = s.spikes;
+    w.last_fired1 = s.last_fired1;
+    w.last_active = s.last_active;
+    w.match_count = s.match_count;
+    w.ws = s.ws;
+    w.len = s.len;
+    NeuronTp wq;
+    wq.cn = s.cn;
+    wq.nruns = s.nruns;
+    wq.ref_head = s.ref_head;
+    wq.ref_count = s.ref_count;
+    wq.ring_head = s.ring_head;
+    wq.ring_used = s.ring_used;
+    wq.pad = 0;
+    e.nrec[n] = w;
+    e.ntp[n] = wq;
+    if (fires > 0) {
+        const uint32_t j = atomicAdd(&e.ts->n_fired_targets, 1u);
+        e.fired_tgt[j] = n;
+        e.fired_cnt[j] = fires;
+    }
+}
+
+// One thread per touched target.  Exact because every state an event reads
+// or writes belongs to its target (the target's neuron state and the
+// target's incoming synapses); post-spike STDP of a fire is applied lazily
+// to synapses touched later in the tick and in bulk by k_post for the rest.
 __global__ void __launch_bounds__(kThreads) k_process(Engine e) {
+    __shared__ unsigned long long s_seg[kSegCache * kThreads];  // column per thread
     const uint32_t t = e.ts->tick;
     const uint32_t n_touched = e.ts->n_touched;
     const uint32_t n_due = e.ts->n_due;
@@ -502,101 +642,31 @@ __global__ void __launch_bounds__(kThreads) k_process(Engine e) {
         const uint32_t n = e.touched[k];
         const uint32_t beg = e.seg_start[n];
         const uint32_t end = k + 1 < n_touched ? e.seg_start[e.touched[k + 1]] : n_due;
-        unsigned long long* g = e.grp + beg;
         const uint32_t len = end - beg;
-        // restore due order (keys are unique due indices)
-        for (uint32_t i = 1; i < len; ++i) {
-            const unsigned long long x = g[i];
-            const uint32_t key = static_cast<uint32_t>(x) & ~kExternalBit;
+        unsigned long long* g;
+        uint32_t stride;
+        if (len <= kSegCache) {
+            g = s_seg + threadIdx.x;
+            stride = kThreads;
+        } else {
+            g = e.grp + beg;
+            stride = 1;
+        }
+        // restore due order (keys are unique due indices) by insertion
+        for (uint32_t i = 0; i < len; ++i) {
+            const unsigned long long v = e.grp[beg + i];
+            const uint32_t key = static_cast<uint32_t>(v) & ~kExternalBit;
             uint32_t j = i;
-            while (j > 0 && (static_cast<uint32_t>(g[j - 1]) & ~kExternalBit) > key) {
-                g[j] = g[j - 1];
+            while (j > 0 && (static_cast<uint32_t>(g[static_cast<size_t>(j - 1) * stride]) & ~kExternalBit) > key) {
+                g[static_cast<size_t>(j) * stride] = g[static_cast<size_t>(j - 1) * stride];
                 --j;
             }
-            g[j] = x;
+            g[static_cast<size_t>(j) * stride] = v;
         }
-        const NeuronParam p = e.nparam[n];
-        NeuronRec r = e.nrec[n];
-        NeuronTp q = e.ntp[n];
-        NState s;
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            s.cur[c] = r.cur[c];
-            s.upd[c] = r.upd[c];
-        }
-        s.flags = r.flags;
-        s.membrane = r.membrane;
-        s.spikes = r.spike_count;
-        s.last_fired1 = r.last_fired1;
-        s.last_active = r.last_active;
-        s.match_count = r.match_count;
-        s.ws = r.ws;
-        s.len = r.len;
-        s.cn = q.cn;
-        s.nruns = q.nruns;
-        s.ref_head = q.ref_head;
-        s.ref_count = q.ref_count;
-        s.ring_head = q.ring_head;
-        s.ring_used = q.ring_used;
-
-        uint32_t fires = 0;
-        for (uint32_t i = 0; i < len; ++i) {
-            const unsigned long long x = g[i];
-            const uint32_t due = static_cast<uint32_t>(x) & ~kExternalBit;
-            const uint32_t payload = static_cast<uint32_t>(x >> 32);
-            bool fired;
-            if (static_cast<uint32_t>(x) & kExternalBit) {
-                fired = process_input(s, p, 0u, 0u, __uint_as_float(payload), t, e, temporal);
-            } else {
-                const uint32_t tm = payload;
-                SynA a = e.syna[tm];
-                SynB b = e.synb[tm];
-                post_catch_up(a, t, fires, e, stdp);
-                const uint32_t delay = a.meta & kMetaDelayMask;
-                const uint32_t pre_tick = t >= delay ? t - delay : t;
-                const bool plastic = (a.meta >> kMetaPlasticBit) & 1u;
-                if (plastic && a.last_post1 != 0) stdp_apply(a, pre_tick, a.last_post1 - 1, e, stdp);
-                a.last_pre1 = pre_tick + 1;
-                b.pre_count += 1;
-                fired = process_input(s, p, (a.meta >> kMetaCompShift) & 3u, (a.meta >> kMetaRecShift) & 3u,
-                                      a.weight, t, e, temporal);
-                uint16_t* lc = e.lcode + p.lcode_base +
-                               static_cast<size_t>(tm - p.in_begin) * p.max_refs * e.code_stride;
-                code_update(b, a.meta, p, t, lc, e.code_stride, temporal);
-                e.syna[tm] = a;
-                e.synb[tm] = b;
-            }
-            if (fired) {
-                fires += 1;
-                atomicOr(&e.fire_bits[due >> 5], 1u << (due & 31));
-                e.fire_at[due] = n;
-            }
-        }
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            r.cur[c] = s.cur[c];
-            r.upd[c] = s.upd[c];
-        }
-        r.flags = s.flags;
-        r.membrane = s.membrane;
-        r.spike_count = s.spikes;
-        r.last_fired1 = s.last_fired1;
-        r.last_active = s.last_active;
-        r.match_count = s.match_count;
-        r.ws = s.ws;
-        r.len = s.len;
-        q.cn = s.cn;
-        q.nruns = s.nruns;
-        q.ref_head = s.ref_head;
-        q.ref_count = s.ref_count;
-        q.ring_head = s.ring_head;
-        q.ring_used = s.ring_used;
-        e.nrec[n] = r;
-        e.ntp[n] = q;
-        if (fires > 0) {
-            const uint32_t j = atomicAdd(&e.ts->n_fired_targets, 1u);
-            e.fired_tgt[j] = n;
-            e.fired_cnt[j] = fires;
+        if (e.nparam[n].max_refs == 1) {
+            process_target<true>(e, n, g, len, stride, t, stdp, temporal);
+        } else {
+            process_target<false>(e, n, g, len, stride, t, stdp, temporal);
         }
     }
 }
@@ -622,19 +692,13 @@ __global__ void k_post(Engine e) {
             if (post_catch_up(a, t, fires, e, stdp)) e.syna[tm] = a;
         }
     }
-    // fire bitmap tile popcounts
+    // fire bitmap tile popcounts (one thread per bitmap word)
     const uint32_t words = (e.ts->n_due + 31) / 32;
-    const uint32_t tiles = (words + kScanTile - 1) / kScanTile;
+    const uint32_t tiles = (words + kThreads - 1) / kThreads;
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        uint32_t c = 0;
-        const uint32_t base = tile * kScanTile + threadIdx.x * 16;
-#pragma unroll
-        for (int k = 0; k < 16; ++k) {
-            const uint32_t w = base + k;
-            c += w < words ? __popc(e.fire_bits[w]) : 0;
-        }
+        const uint32_t w = tile * kThreads + threadIdx.x;
         uint32_t tot;
-        block_excl_scan(c, &tot);
+        block_excl_scan(w < words ? __popc(e.fire_bits[w]) : 0u, &tot);
         if (threadIdx.x == 0) e.fire_tile[tile] = tot;
     }
     if (last_block(&e.ts->done_fire_tile)) {
@@ -644,65 +708,59 @@ __global__ void k_post(Engine e) {
     }
 }
 
-// Fires in due order.  Each fire's rank r is its position in the reference's
-// fire order; the fire list, the raster and the per-(expansion block, delay
-// class) event counts are written here, the bitmap is cleared.  The last
-// block turns the class counts into destination offsets in the wheel and
-// finishes the tick.
+// Fires in due order, one thread per bitmap word.  A fire's rank r is its
+// position in the reference's fire order (due order, NetworkPropagator.cpp:
+// 80-93); the fire list and the raster are written here and the bitmap is
+// cleared.
 __global__ void k_fire_list(Engine e) {
     const uint32_t t = e.ts->tick;
     const uint32_t words = (e.ts->n_due + 31) / 32;
-    const uint32_t tiles = (words + kScanTile - 1) / kScanTile;
-    const uint32_t nfires = e.ts->n_fires;
+    const uint32_t tiles = (words + kThreads - 1) / kThreads;
     const unsigned long long raster0 = e.ts->raster_count;
-    const uint32_t D = e.D;
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        const uint32_t base = tile * kScanTile + threadIdx.x * 16;
-        uint32_t c = 0;
-#pragma unroll
-        for (int k = 0; k < 16; ++k) {
-            const uint32_t w = base + k;
-            c += w < words ? __popc(e.fire_bits[w]) : 0;
-        }
-        uint32_t r = __ldcg(e.fire_tile + tile) + block_excl_scan(c, nullptr);
-        for (int k = 0; k < 16; ++k) {
-            const uint32_t w = base + k;
-            if (w >= words) break;
-            uint32_t bits = e.fire_bits[w];
-            if (bits == 0) continue;
-            e.fire_bits[w] = 0;
-            while (bits) {
-                const uint32_t bit = __ffs(bits) - 1;
-                bits &= bits - 1;
-                const uint32_t due = w * 32 + bit;
-                const uint32_t n = e.fire_at[due];
-                if (r < e.fire_cap) {
-                    e.fire_list[r] = n;
-                    const uint32_t* row = e.pre_off + static_cast<size_t>(n) * (D + 1);
-                    uint32_t* xs = e.xsum + static_cast<size_t>(r / kExpandFires) * D;
-                    for (uint32_t d = 0; d < D; ++d) {
-                        const uint32_t cnt = row[d + 1] - row[d];
-                        if (cnt) atomicAdd(xs + d, cnt);
-                    }
+        const uint32_t w = tile * kThreads + threadIdx.x;
+        uint32_t bits = w < words ? e.fire_bits[w] : 0u;
+        uint32_t r = __ldcg(e.fire_tile + tile) + block_excl_scan(__popc(bits), nullptr);
+        if (bits) e.fire_bits[w] = 0;
+        while (bits) {
+            const uint32_t bit = __ffs(bits) - 1;
+            bits &= bits - 1;
+            const uint32_t n = e.fire_at[w * 32 + bit];
+            if (r < e.fire_cap) e.fire_list[r] = n;
+            if (e.raster_cap > 0) {
+                const unsigned long long pos = raster0 + r;
+                if (pos < e.raster_cap) {
+                    e.raster[2 * pos] = t;
+                    e.raster[2 * pos + 1] = n;
                 }
-                if (e.raster_cap > 0) {
-                    const unsigned long long pos = raster0 + r;
-                    if (pos < e.raster_cap) {
-                        e.raster[2 * pos] = t;
-                        e.raster[2 * pos + 1] = n;
-                    }
-                }
-                r += 1;
             }
+            r += 1;
+        }
+    }
+}
+
+// Events per (expansion block of kExpandFires fires, delay class), one
+// thread per fire.  The last block turns the counts into wheel positions
+// (exclusive scan over blocks per class, appended behind each delivery slot's
+// current contents) and finishes the tick.
+__global__ void k_fire_count(Engine e) {
+    const uint32_t t = e.ts->tick;
+    const uint32_t nfires = e.ts->n_fires;
+    const uint32_t nf = nfires < e.fire_cap ? nfires : e.fire_cap;
+    const uint32_t D = e.D;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < nf; r += gridDim.x * blockDim.x) {
+        const uint32_t* row = e.pre_off + static_cast<size_t>(e.fire_list[r]) * (D + 1);
+        uint32_t* xs = e.xsum + static_cast<size_t>(r / kExpandFires) * D;
+        uint32_t prev = row[0];
+        for (uint32_t d = 0; d < D; ++d) {
+            const uint32_t next = row[d + 1];
+            if (next != prev) atomicAdd(xs + d, next - prev);
+            prev = next;
         }
     }
     if (!last_block(&e.ts->done_fire_list)) return;
-    // --- tick finish (single block) ---
     if (nfires > e.fire_cap && threadIdx.x == 0) raise_status(e, kStatusFireOverflow);
-    const uint32_t nf = nfires < e.fire_cap ? nfires : e.fire_cap;
     const uint32_t blocks = (nf + kExpandFires - 1) / kExpandFires;
-    // per delay class: exclusive scan over expansion blocks, then absolute
-    // wheel positions; xsum is reset to zero for the next tick.
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (uint32_t d = warp; d < D; d += kThreads / 32) {
         const uint32_t slot = (t + e.cls_delta[d]) & e.wmask;
@@ -732,6 +790,7 @@ __global__ void k_fire_list(Engine e) {
     if (threadIdx.x == 0) {
         TickState* ts = e.ts;
         const uint32_t due = ts->n_due;
+        const unsigned long long raster0 = ts->raster_count;
         ts->delivered += due;
         ts->fired += nfires;
         ts->touched_total += ts->n_touched;
@@ -748,48 +807,39 @@ __global__ void k_fire_list(Engine e) {
     }
 }
 
-// Spike-code offset expansion (NetworkPropagator.cpp:104-130): one warp per
+// Spike-code offset expansion (NetworkPropagator.cpp:104-130): one block per
 // fire copies the fire's pre-expanded events, class by class, to their
-// delivery slots.  Destinations were fixed by k_fire_list, so the wheel ends
+// delivery slots.  Destinations were fixed by k_fire_count, so the wheel ends
 // up in exactly the reference's scheduling order.
 __global__ void __launch_bounds__(kThreads) k_expand(Engine e) {
-    __shared__ uint32_t s_row[kExpandFires][kMaxClasses + 1];
-    __shared__ unsigned long long s_dst[kExpandFires][kMaxClasses];
+    __shared__ uint32_t s_row[kMaxClasses + 1];
+    __shared__ unsigned long long s_dst[kMaxClasses];
     const uint32_t nf = e.ts->expand_fires;
-    const uint32_t blocks = (nf + kExpandFires - 1) / kExpandFires;
     const uint32_t D = e.D;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (uint32_t blk = blockIdx.x; blk < blocks; blk += gridDim.x) {
-        const uint32_t r = blk * kExpandFires + warp;
-        const bool have = r < nf;
-        const uint32_t n = have ? e.fire_list[r] : 0;
-        if (have) {
-            const uint32_t* row = e.pre_off + static_cast<size_t>(n) * (D + 1);
-            for (uint32_t d = lane; d <= D; d += 32) s_row[warp][d] = row[d];
+    for (uint32_t r = blockIdx.x; r < nf; r += gridDim.x) {
+        const uint32_t n = e.fire_list[r];
+        const uint32_t* row = e.pre_off + static_cast<size_t>(n) * (D + 1);
+        for (uint32_t d = threadIdx.x; d <= D; d += blockDim.x) s_row[d] = row[d];
+        // destination = expansion-block base + the block's earlier fires
+        const uint32_t first = r - r % kExpandFires;
+        for (uint32_t d = threadIdx.x; d < D; d += blockDim.x) {
+            unsigned long long dst = __ldcg(e.xdst + static_cast<size_t>(r / kExpandFires) * D + d);
+            for (uint32_t q = first; q < r; ++q) {
+                const uint32_t* rq = e.pre_off + static_cast<size_t>(e.fire_list[q]) * (D + 1);
+                dst += rq[d + 1] - rq[d];
+            }
+            s_dst[d] = dst;
         }
         __syncthreads();
-        // destination of each class for this fire = block base + counts of the
-        // block's earlier fires
-        if (have) {
-            for (uint32_t d = lane; d < D; d += 32) {
-                unsigned long long dst = __ldcg(e.xdst + static_cast<size_t>(blk) * D + d);
-                for (int w = 0; w < warp; ++w) dst += s_row[w][d + 1] - s_row[w][d];
-                s_dst[warp][d] = dst;
+        const unsigned long long* src = e.pre_ev + e.pre_base[n];
+        const uint32_t total = s_row[D];
+        for (uint32_t j = threadIdx.x; j < total; j += blockDim.x) {
+            uint32_t lo = 0, hi = D;  // class of event j: last d with s_row[d] <= j
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (s_row[mid] <= j) lo = mid; else hi = mid;
             }
-        }
-        __syncwarp();
-        if (have) {
-            const unsigned long long* src = e.pre_ev + e.pre_base[n];
-            const uint32_t total = s_row[warp][D];
-            for (uint32_t j = lane; j < total; j += 32) {
-                // class of event j: last d with s_row[d] <= j
-                uint32_t lo = 0, hi = D;
-                while (hi - lo > 1) {
-                    const uint32_t mid = (lo + hi) >> 1;
-                    if (s_row[warp][mid] <= j) lo = mid; else hi = mid;
-                }
-                if (e.xdst_ok[lo]) e.wheel[s_dst[warp][lo] + (j - s_row[warp][lo])] = src[j];
-            }
+            if (e.xdst_ok[lo]) e.wheel[s_dst[lo] + (j - s_row[lo])] = src[j];
         }
         __syncthreads();
     }
@@ -831,12 +881,13 @@ void launch_tick(const Engine& e, cudaStream_t stream, cudaEvent_t* marks) {
     mark(false); k_process<<<e.grid_process, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_post<<<wide, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_fire_list<<<e.grid_fire, kThreads, 0, stream>>>(e); mark(true);
+    mark(false); k_fire_count<<<e.grid_wide, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_expand<<<wide, kThreads, 0, stream>>>(e); mark(true);
 }
 
 const char* kernel_name(int index) {
-    static const char* names[kKernelCount] = {"k_hist", "k_scan_tile", "k_scan_out", "k_scatter",
-                                              "k_process", "k_post", "k_fire_list", "k_expand"};
+    static const char* names[kKernelCount] = {"k_hist",    "k_scan_tile", "k_scan_out",   "k_scatter", "k_process",
+                                              "k_post",    "k_fire_list", "k_fire_count", "k_expand"};
     return index >= 0 && index < kKernelCount ? names[index] : "";
 }
 

@@ -469,7 +469,7 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.raster_cap = cfg.raster_capacity;
     const uint64_t xblocks = (fire_cap + kExpandFires - 1) / kExpandFires;
     const uint64_t bit_words = slot_cap / 32;
-    const uint64_t fire_tiles = (bit_words + kScanTile - 1) / kScanTile;
+    const uint64_t fire_tiles = (bit_words + 255) / 256;
     e.fire_tiles_cap = static_cast<uint32_t>(fire_tiles);
 
     // ---- tables ----

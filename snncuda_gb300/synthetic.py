@@ -17,11 +17,15 @@ tick):
                (threshold 1, window 500, similarity 0.93, 500 patterns),
                10 Hz drive of weight 1, 1,000 ticks, seed 0.
   stdp_100k    100,000 neurons (80/20), fan-out 1,000 (1e8 synapses),
-               lognormal(-1.5, 0.5) weights times g (inhibitory as GABA_A
-               magnitude), delays U{1..20}, 4 compartments, 1-4 code offsets
-               in U{0..7}, pair STDP (A+ 0.01, A- 0.012, tau 20, weights in
-               [0,1]), window 32, similarity 0.9, 1 pattern, 5 Hz drive,
-               10,000 ticks, seed 1.
+               lognormal(-1.5, 0.5) weights times g = 0.01 (inhibitory as
+               GABA_A magnitude), delays U{1..20}, 4 compartments, 1-4 code
+               offsets in U{0..7}, pair STDP (A+ 0.01, A- 0.012, tau 20,
+               StdpConfig weights in [0,1]; per-synapse max_weight = g, i.e.
+               the [0,1] clip in units of g), window 32, similarity 0.9, 1
+               pattern, 5 Hz drive, 10,000 ticks, seed 1.  The reference's
+               pair rule potentiates every recently active input at each post
+               spike, so with a clip of 1 the weights climb to it and the
+               network runs away within a few hundred ticks.
   recog_1m     1,000,000 neurons, fan-out 1,000 (1e9 synapses), stdp_100k
                distributions, plus 16 fixed 8-offset codes (offsets in
                U{0..31}) presented every 64 ticks to the first half of the
@@ -138,8 +142,8 @@ class Workload:
 
 PLAIN_1K = Workload("plain_1k", 1000, 0.8, 100, 0, weight_scale=0.3, delay=(1, 20), codes=(1, 1),
                     compartments=2, plastic=False, drive_rate_hz=10.0, ticks=1000, seed=0)
-STDP_100K = Workload("stdp_100k", 100_000, 0.8, 1000, 1, weight_scale=0.02, codes=(1, 4),
-                     code_offset_max=7, compartments=4, plastic=True, max_weight=1.0,
+STDP_100K = Workload("stdp_100k", 100_000, 0.8, 1000, 1, weight_scale=0.01, codes=(1, 4),
+                     code_offset_max=7, compartments=4, plastic=True, max_weight=0.01,
                      pattern_window_ticks=32, similarity_threshold=0.9, max_reference_patterns=1,
                      drive_rate_hz=5.0, ticks=10_000, seed=1, stdp_enabled=True)
 RECOG_1M = STDP_100K.scaled(name="recog_1m", neurons=1_000_000, ticks=2000, seed=2,

@@ -297,7 +297,7 @@ def sc_plain_1k():
 
 
 def _stdp_small():
-    return synthetic.STDP_100K.scaled(neurons=2000, fanout=100, weight_scale=0.12, seed=5)
+    return synthetic.STDP_100K.scaled(neurons=2000, fanout=100, weight_scale=0.12, max_weight=1.0, seed=5)
 
 
 STDP_CFG = {"max_weight": 1.0}
@@ -323,7 +323,7 @@ def sc_toggles():
 
 def sc_recog_small():
     """recog_1m distributions (temporal-code stimulus) at 2,000 neurons."""
-    w = synthetic.RECOG_1M.scaled(neurons=2000, fanout=100, weight_scale=0.06, seed=9)
+    w = synthetic.RECOG_1M.scaled(neurons=2000, fanout=100, weight_scale=0.06, max_weight=1.0, seed=9)
     s = _synthetic(w, 256, STDP_CFG)
     s.default_processor = False
     return s

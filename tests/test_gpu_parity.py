@@ -52,14 +52,14 @@ def _compare(gpu_lib, port_lib, net, drive, ticks, cfg, *, toggles=()):
 
 @pytest.mark.parametrize("neurons,fanout,ticks,g", [(20_000, 200, 300, 0.05), (5_000, 1000, 200, 0.01)])
 def test_stdp_network_matches_oracle(gpu_lib, port_lib, neurons, fanout, ticks, g):
-    w = synthetic.STDP_100K.scaled(neurons=neurons, fanout=fanout, weight_scale=g, seed=21)
+    w = synthetic.STDP_100K.scaled(neurons=neurons, fanout=fanout, weight_scale=g, max_weight=1.0, seed=21)
     net = synthetic.build_network(w)
     c = _compare(gpu_lib, port_lib, net, synthetic.build_drive(w, ticks), ticks, STDP_CFG)
     assert c["synaptic_events"] > 100_000
 
 
 def test_recognition_network_with_toggles_matches_oracle(gpu_lib, port_lib):
-    w = synthetic.RECOG_1M.scaled(neurons=10_000, fanout=200, weight_scale=0.03, seed=23)
+    w = synthetic.RECOG_1M.scaled(neurons=10_000, fanout=200, weight_scale=0.03, max_weight=1.0, seed=23)
     net = synthetic.build_network(w)
     _compare(gpu_lib, port_lib, net, synthetic.build_drive(w, 300), 300, STDP_CFG,
              toggles=[(99, "stdp", False), (149, "temporal", False), (199, "stdp", True),
