@@ -119,6 +119,10 @@ def workload_from_args(args):
     w = synthetic.WORKLOADS[args.workload]
     if args.weight_scale is not None:
         w = w.scaled(weight_scale=args.weight_scale)
+    if args.neurons is not None:
+        w = w.scaled(neurons=args.neurons)
+    if args.fanout is not None:
+        w = w.scaled(fanout=args.fanout)
     return w
 
 
@@ -173,7 +177,7 @@ def config_block(args, w):
     return {"workload": w.name, "neurons": w.neurons, "synapses": w.synapses, "fanout": w.fanout,
             "weight_scale": w.weight_scale, "ticks": w.ticks, "ticks_per_step": args.ticks_per_step,
             "stdp": w.stdp_enabled, "drive_hz": w.drive_rate_hz, "seed": w.seed,
-            "l2": "inputs larger than L2 (synapse state 64 B x 1e8 = 6.4 GB)",
+            "l2": f"inputs larger than L2 (synapse state 64 B x {w.synapses:.0e} = {64 * w.synapses / 1e9:.1f} GB)",
             "parallelism": f"replicas x{args.gpus}"}
 
 
@@ -186,6 +190,8 @@ def main():
     ap.add_argument("--workload", default="stdp_100k")
     ap.add_argument("--ticks-per-step", type=int, default=400)
     ap.add_argument("--weight-scale", type=float, default=None)
+    ap.add_argument("--neurons", type=int, default=None, help="smaller case of the workload (profiling)")
+    ap.add_argument("--fanout", type=int, default=None)
     ap.add_argument("--profile-ticks", type=int, default=200)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")

@@ -186,6 +186,7 @@ struct Engine {
     uint32_t* tile_nz;
     uint32_t* touched;                     // [N] target ids with due events, ascending
     unsigned long long* grp;               // [slot_cap] (payload << 32) | (due index | ext << 31)
+    unsigned long long* grp_sorted;        // [slot_cap] grp with every target's group in due order
     uint32_t* fire_bits;                   // [slot_cap/32] bitmap of due positions that fired
     uint32_t* fire_at;                     // [slot_cap] firing neuron at a due position
     uint32_t* fire_tile;                   // bitmap tile bases
@@ -217,7 +218,7 @@ constexpr uint32_t kMaxClasses = 256;    // distinct delivery delays
 // Host-side launchers (kernels.cu).
 // `marks` (optional) holds 2 * kKernelCount events recorded around every
 // kernel (before, after) for profiling graphs.
-constexpr int kKernelCount = 9;
+constexpr int kKernelCount = 10;
 void launch_tick(const Engine& e, cudaStream_t stream, cudaEvent_t* marks = nullptr);
 const char* kernel_name(int index);
 void launch_inject(const Engine& e, const unsigned long long* ev, const uint32_t* slot_of_group,

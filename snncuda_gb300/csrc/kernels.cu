@@ -501,7 +501,51 @@ __global__ void k_scatter(Engine e) {
     }
 }
 
-constexpr int kSegCache = 24;  // due events per target sorted in shared memory
+// Restore due order inside every target's group (k_scatter leaves it in
+// arbitrary order; keys are unique due indices).  One warp per target:
+// groups of up to 32 events are bitonic-sorted in registers, longer ones are
+// placed by rank (number of smaller keys).  Output goes to grp_sorted.
+__global__ void __launch_bounds__(kThreads) k_segsort(Engine e) {
+    const uint32_t n_touched = e.ts->n_touched;
+    const uint32_t n_due = e.ts->n_due;
+    const int lane = threadIdx.x & 31;
+    const uint32_t warps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t k = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); k < n_touched; k += warps) {
+        const uint32_t beg = e.seg_start[e.touched[k]];
+        const uint32_t end = k + 1 < n_touched ? e.seg_start[e.touched[k + 1]] : n_due;
+        const uint32_t len = end - beg;
+        const unsigned long long* src = e.grp + beg;
+        unsigned long long* dst = e.grp_sorted + beg;
+        if (len <= 32) {
+            unsigned long long v = lane < static_cast<int>(len) ? src[lane] : ~0ull;
+            uint32_t key = lane < static_cast<int>(len) ? static_cast<uint32_t>(v) & ~kExternalBit : 0xFFFFFFFFu;
+#pragma unroll
+            for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+                for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                    const uint32_t ok = __shfl_xor_sync(0xffffffffu, key, stride);
+                    const unsigned long long ov = __shfl_xor_sync(0xffffffffu, v, stride);
+                    const bool up = ((lane & size) == 0);
+                    const bool lower = (lane & stride) == 0;
+                    const bool take_min = (lower == up);
+                    if (take_min ? (ok < key) : (ok > key)) {
+                        key = ok;
+                        v = ov;
+                    }
+                }
+            }
+            if (lane < static_cast<int>(len)) dst[lane] = v;
+        } else {
+            for (uint32_t j = lane; j < len; j += 32) {
+                const unsigned long long v = src[j];
+                const uint32_t key = static_cast<uint32_t>(v) & ~kExternalBit;
+                uint32_t rank = 0;
+                for (uint32_t i = 0; i < len; ++i) rank += (static_cast<uint32_t>(src[i]) & ~kExternalBit) < key;
+                dst[rank] = v;
+            }
+        }
+    }
+}
 
 // The events of one target in due order, then the reference's sequential
 // per-event loop (NetworkPropagator.cpp:80-131) restricted to this target.
@@ -632,7 +676,6 @@ __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, cons
 // target's incoming synapses); post-spike STDP of a fire is applied lazily
 // to synapses touched later in the tick and in bulk by k_post for the rest.
 __global__ void __launch_bounds__(kThreads) k_process(Engine e) {
-    __shared__ unsigned long long s_seg[kSegCache * kThreads];  // column per thread
     const uint32_t t = e.ts->tick;
     const uint32_t n_touched = e.ts->n_touched;
     const uint32_t n_due = e.ts->n_due;
@@ -642,31 +685,11 @@ __global__ void __launch_bounds__(kThreads) k_process(Engine e) {
         const uint32_t n = e.touched[k];
         const uint32_t beg = e.seg_start[n];
         const uint32_t end = k + 1 < n_touched ? e.seg_start[e.touched[k + 1]] : n_due;
-        const uint32_t len = end - beg;
-        unsigned long long* g;
-        uint32_t stride;
-        if (len <= kSegCache) {
-            g = s_seg + threadIdx.x;
-            stride = kThreads;
-        } else {
-            g = e.grp + beg;
-            stride = 1;
-        }
-        // restore due order (keys are unique due indices) by insertion
-        for (uint32_t i = 0; i < len; ++i) {
-            const unsigned long long v = e.grp[beg + i];
-            const uint32_t key = static_cast<uint32_t>(v) & ~kExternalBit;
-            uint32_t j = i;
-            while (j > 0 && (static_cast<uint32_t>(g[static_cast<size_t>(j - 1) * stride]) & ~kExternalBit) > key) {
-                g[static_cast<size_t>(j) * stride] = g[static_cast<size_t>(j - 1) * stride];
-                --j;
-            }
-            g[static_cast<size_t>(j) * stride] = v;
-        }
+        const unsigned long long* g = e.grp_sorted + beg;
         if (e.nparam[n].max_refs == 1) {
-            process_target<true>(e, n, g, len, stride, t, stdp, temporal);
+            process_target<true>(e, n, g, end - beg, 1, t, stdp, temporal);
         } else {
-            process_target<false>(e, n, g, len, stride, t, stdp, temporal);
+            process_target<false>(e, n, g, end - beg, 1, t, stdp, temporal);
         }
     }
 }
@@ -878,6 +901,7 @@ void launch_tick(const Engine& e, cudaStream_t stream, cudaEvent_t* marks) {
     mark(false); k_scan_tile<<<scan_grid, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_scan_out<<<scan_grid, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_scatter<<<wide, kThreads, 0, stream>>>(e); mark(true);
+    mark(false); k_segsort<<<e.grid_wide * 4, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_process<<<e.grid_process, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_post<<<wide, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_fire_list<<<e.grid_fire, kThreads, 0, stream>>>(e); mark(true);
@@ -886,8 +910,8 @@ void launch_tick(const Engine& e, cudaStream_t stream, cudaEvent_t* marks) {
 }
 
 const char* kernel_name(int index) {
-    static const char* names[kKernelCount] = {"k_hist",    "k_scan_tile", "k_scan_out",   "k_scatter", "k_process",
-                                              "k_post",    "k_fire_list", "k_fire_count", "k_expand"};
+    static const char* names[kKernelCount] = {"k_hist",  "k_scan_tile", "k_scan_out",   "k_scatter", "k_segsort",
+                                              "k_process", "k_post",    "k_fire_list",  "k_fire_count", "k_expand"};
     return index >= 0 && index < kKernelCount ? names[index] : "";
 }
 

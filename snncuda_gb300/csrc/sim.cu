@@ -132,7 +132,9 @@ struct snncuda_sim {
     std::vector<uint32_t> tm_of_c;     // target-major slot of each Connectome index
     std::vector<uint64_t> in_ptr;      // host copy of the row pointers
     std::vector<NeuronParam> nparam;   // host copy
-    std::vector<Pending> pending;      // queued injections, call order
+    std::vector<Pending> pending;      // queued injections; [pend_head, pend_sorted) sorted by tick
+    size_t pend_head{0};
+    size_t pend_sorted{0};
     // far-future buffers (stable addresses while a graph uses them)
     unsigned long long* far_ev{nullptr};
     uint32_t* far_idx{nullptr};
@@ -503,6 +505,7 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.tile_nz = dalloc<uint32_t>(own, scan_tiles + 2);
     e.touched = dalloc<uint32_t>(own, N);
     e.grp = dalloc<unsigned long long>(own, slot_cap);
+    e.grp_sorted = dalloc<unsigned long long>(own, slot_cap);
     e.fire_bits = dalloc<uint32_t>(own, bit_words);
     e.fire_at = dalloc<uint32_t>(own, slot_cap);
     e.fire_tile = dalloc<uint32_t>(own, fire_tiles + 2);
@@ -592,18 +595,31 @@ void run_impl(snncuda_sim* sim, uint64_t T, snncuda_profile* prof = nullptr) {
     // Injections in (delivery, call order).  Those due within W ticks go into
     // their slots now, behind everything scheduled before this call; later
     // ones are moved in by k_hist the tick their slot frees up; the rest wait.
-    std::stable_sort(sim->pending.begin(), sim->pending.end(),
-                     [](const Pending& a, const Pending& b) { return a.tick < b.tick; });
-    size_t a_end = 0;
-    while (a_end < sim->pending.size() && sim->pending[a_end].tick < p + W) ++a_end;
-    size_t b_end = a_end;
-    while (b_end < sim->pending.size() && sim->pending[b_end].tick <= T + W - 1) ++b_end;
+    auto& pend = sim->pending;
+    if (sim->pend_sorted < pend.size()) {
+        // new injections are sorted on their own (stable: call order kept),
+        // then merged behind the earlier ones they tie with
+        auto by_tick = [](const Pending& a, const Pending& b) { return a.tick < b.tick; };
+        const auto mid = pend.begin() + static_cast<std::ptrdiff_t>(sim->pend_sorted);
+        std::stable_sort(mid, pend.end(), by_tick);
+        std::inplace_merge(pend.begin() + static_cast<std::ptrdiff_t>(sim->pend_head), mid, pend.end(), by_tick);
+        sim->pend_sorted = pend.size();
+    }
+    const Pending* base = pend.data() + sim->pend_head;
+    const size_t live = pend.size() - sim->pend_head;
+    auto first_at_or_after = [&](uint64_t tick) {
+        return static_cast<size_t>(std::partition_point(base, base + live,
+                                                        [tick](const Pending& q) { return q.tick < tick; }) -
+                                   base);
+    };
+    const size_t a_end = first_at_or_after(p + W);
+    const size_t b_end = first_at_or_after(T + W);
     cudaStream_t st = sim->stream;
     if (a_end > 0) {
         std::vector<uint32_t> slots, offs;
         for (size_t i = 0; i < a_end; ++i) {
-            const uint32_t slot = static_cast<uint32_t>(sim->pending[i].tick & (W - 1));
-            if (i == 0 || sim->pending[i].tick != sim->pending[i - 1].tick) {
+            const uint32_t slot = static_cast<uint32_t>(base[i].tick & (W - 1));
+            if (i == 0 || base[i].tick != base[i - 1].tick) {
                 slots.push_back(slot);
                 offs.push_back(static_cast<uint32_t>(i));
             }
@@ -611,7 +627,7 @@ void run_impl(snncuda_sim* sim, uint64_t T, snncuda_profile* prof = nullptr) {
         offs.push_back(static_cast<uint32_t>(a_end));
         sim->ensure_inject(a_end, slots.size());
         sim->ensure_host(a_end, 2 * slots.size() + 1);
-        for (size_t i = 0; i < a_end; ++i) sim->host_ev[i] = sim->pending[i].event;
+        for (size_t i = 0; i < a_end; ++i) sim->host_ev[i] = base[i].event;
         std::copy(slots.begin(), slots.end(), sim->host_idx);
         std::copy(offs.begin(), offs.end(), sim->host_idx + slots.size());
         check(cudaMemcpyAsync(sim->inj_ev, sim->host_ev, a_end * 8, cudaMemcpyHostToDevice, st), "inject copy");
@@ -633,7 +649,7 @@ void run_impl(snncuda_sim* sim, uint64_t T, snncuda_profile* prof = nullptr) {
         uint32_t* idx = sim->host_idx;
         std::fill(idx, idx + far_ticks + 1, 0u);
         for (size_t i = 0; i < n; ++i) {
-            const Pending& q = sim->pending[a_end + i];
+            const Pending& q = base[a_end + i];
             sim->host_ev[i] = q.event;
             idx[q.tick - far_first + 1] += 1;
         }
@@ -643,7 +659,15 @@ void run_impl(snncuda_sim* sim, uint64_t T, snncuda_profile* prof = nullptr) {
                               st), "far copy");
         check(cudaStreamSynchronize(st), "far copy");
     }
-    sim->pending.erase(sim->pending.begin(), sim->pending.begin() + static_cast<std::ptrdiff_t>(b_end));
+    sim->pend_head += b_end;
+    if (sim->pend_head == pend.size()) {
+        pend.clear();
+        sim->pend_head = sim->pend_sorted = 0;
+    } else if (sim->pend_head > (1u << 16) && sim->pend_head * 2 > pend.size()) {
+        pend.erase(pend.begin(), pend.begin() + static_cast<std::ptrdiff_t>(sim->pend_head));
+        sim->pend_sorted -= sim->pend_head;
+        sim->pend_head = 0;
+    }
     // run parameters live in device memory so the captured graphs stay valid
     check(cudaMemcpyAsync(reinterpret_cast<char*>(e.ts) + offsetof(TickState, far_first_tick), &far_first, 4,
                           cudaMemcpyHostToDevice, st), "run params");
@@ -878,7 +902,7 @@ int snncuda_sim_counters(snncuda_sim* sim, snncuda_counters* out) {
     return guarded([&] {
         const TickState ts = sim->read_ts();
         const std::vector<uint32_t> counts = sim->d2h(sim->e.slot_count, sim->e.W);
-        uint64_t pending = sim->pending.size();
+        uint64_t pending = sim->pending.size() - sim->pend_head;
         for (uint32_t c : counts) pending += c;
         out->delivered_spikes = ts.delivered;
         out->fired_spikes = ts.fired;
