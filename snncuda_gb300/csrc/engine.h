@@ -57,8 +57,14 @@ struct alignas(32) SynB {
     uint8_t code_len;       // code_offsets.size() (<= expected)
     uint8_t last_code_match;
     uint16_t learned_count; // learned_code_patterns.size()
-    uint16_t ring[kMaxExpected];  // code_offsets in order
+    // code_offsets in order, 16 bits each: offsets 0-3 in ring_lo, 4-7 in ring_hi
+    unsigned long long ring_lo;
+    unsigned long long ring_hi;
 };
+
+__host__ __device__ inline uint32_t ring_get(unsigned long long lo, unsigned long long hi, uint32_t j) {
+    return static_cast<uint32_t>((j < 4 ? lo >> (16 * j) : hi >> (16 * (j - 4))) & 0xFFFFu);
+}
 
 struct alignas(64) NeuronRec {
     float cur[4];          // soma, basal, apical, inhibitory current

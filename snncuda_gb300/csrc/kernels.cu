@@ -36,6 +36,11 @@ namespace {
 
 constexpr int kThreads = 256;
 
+// Minimum resident blocks per SM requested for k_process (register budget).
+#ifndef SNNGB_PROCESS_MIN_BLOCKS
+#define SNNGB_PROCESS_MIN_BLOCKS 2
+#endif
+
 __device__ __forceinline__ float rec_gain(uint32_t r) { return r == 1 ? 0.55f : (r == 3 ? 0.65f : 1.0f); }
 __device__ __forceinline__ float rec_sign(uint32_t r) { return r >= 2 ? -1.0f : 1.0f; }
 
@@ -140,6 +145,11 @@ struct NState {
     uint32_t nruns, ref_head, ref_count, ring_head, ring_used;
     unsigned long long last_run;  // cand[nruns-1], kept in a register while nruns > 0
     RefMeta one;                  // the learned pattern when max_reference_patterns == 1
+    // kOne: the newest pattern's runs are copied into the ring once, at the
+    // end of the target's tick (until then nothing reads them)
+    bool snap_pending;
+    uint32_t snap_nruns;
+    unsigned long long snap_last;
 };
 
 __device__ __forceinline__ float decay_factor(const Tables& tb, uint32_t code, uint32_t elapsed) {
@@ -243,9 +253,15 @@ __device__ void temporal_update(NState& s, const NeuronParam& p, uint32_t t, con
         raise_status(e, kStatusRingOverflow);
         return;
     }
-    cand[s.nruns - 1] = s.last_run;
     const uint32_t start = s.ring_head;
-    for (uint32_t j = 0; j < s.nruns; ++j) ring[(start + j) % p.ring_cap] = cand[j];
+    if constexpr (kOne) {
+        s.snap_pending = true;
+        s.snap_nruns = s.nruns;
+        s.snap_last = s.last_run;
+    } else {
+        cand[s.nruns - 1] = s.last_run;
+        for (uint32_t j = 0; j < s.nruns; ++j) ring[(start + j) % p.ring_cap] = cand[j];
+    }
     s.ring_head = (start + s.nruns) % p.ring_cap;
     s.ring_used += s.nruns;
     RefMeta& m = ref(s.ref_count);
@@ -338,7 +354,53 @@ __device__ __forceinline__ bool post_catch_up(SynA& a, uint32_t t, uint32_t fire
     return true;
 }
 
-// SynapseDendriteProcessor.cpp:318-365 on a fixed ring of `expected` offsets.
+__device__ __forceinline__ void ring_set(unsigned long long& lo, unsigned long long& hi, uint32_t j,
+                                         uint32_t v) {
+    if (j < 4) {
+        const int sh = 16 * j;
+        lo = (lo & ~(0xFFFFull << sh)) | (static_cast<unsigned long long>(v) << sh);
+    } else {
+        const int sh = 16 * (j - 4);
+        hi = (hi & ~(0xFFFFull << sh)) | (static_cast<unsigned long long>(v) << sh);
+    }
+}
+
+// A learned code pattern of `stride` 16-bit offsets, loaded with the widest
+// aligned access the stride allows.
+__device__ __forceinline__ void load_pattern(const uint16_t* pat, uint32_t stride, unsigned long long& lo,
+                                             unsigned long long& hi) {
+    if (stride == 4) {
+        lo = *reinterpret_cast<const unsigned long long*>(pat);
+        hi = 0;
+    } else if (stride == 8) {
+        const uint4 v = *reinterpret_cast<const uint4*>(pat);
+        lo = (static_cast<unsigned long long>(v.y) << 32) | v.x;
+        hi = (static_cast<unsigned long long>(v.w) << 32) | v.z;
+    } else if (stride == 2) {
+        lo = *reinterpret_cast<const uint32_t*>(pat);
+        hi = 0;
+    } else {
+        lo = hi = 0;
+        for (uint32_t j = 0; j < stride; ++j) ring_set(lo, hi, j, pat[j]);
+    }
+}
+
+__device__ __forceinline__ void store_pattern(uint16_t* pat, uint32_t stride, unsigned long long lo,
+                                              unsigned long long hi) {
+    if (stride == 4) {
+        *reinterpret_cast<unsigned long long*>(pat) = lo;
+    } else if (stride == 8) {
+        *reinterpret_cast<uint4*>(pat) = make_uint4(static_cast<uint32_t>(lo), static_cast<uint32_t>(lo >> 32),
+                                                    static_cast<uint32_t>(hi), static_cast<uint32_t>(hi >> 32));
+    } else if (stride == 2) {
+        *reinterpret_cast<uint32_t*>(pat) = static_cast<uint32_t>(lo);
+    } else {
+        for (uint32_t j = 0; j < stride; ++j) pat[j] = static_cast<uint16_t>(ring_get(lo, hi, j));
+    }
+}
+
+// SynapseDendriteProcessor.cpp:318-365 on a fixed ring of `expected` offsets
+// held in two 64-bit words.
 __device__ void code_update(SynB& b, uint32_t meta, const NeuronParam& p, uint32_t t, uint16_t* lc,
                             uint32_t stride, int enabled) {
     if (!enabled) {
@@ -349,26 +411,32 @@ __device__ void code_update(SynB& b, uint32_t meta, const NeuronParam& p, uint32
         b.code_ws = t;
         b.code_len = 0;
     }
-    const uint16_t o = static_cast<uint16_t>(t - b.code_ws);
+    const uint32_t o = t - b.code_ws;
     const uint32_t expected = (meta >> kMetaExpectedShift) & 15u;
     if (b.code_len < expected) {
-        b.ring[b.code_len] = o;
+        ring_set(b.ring_lo, b.ring_hi, b.code_len, o);
         b.code_len += 1;
-    } else {
-        for (uint32_t j = 0; j + 1 < expected; ++j) b.ring[j] = b.ring[j + 1];
-        b.ring[expected - 1] = o;
+    } else {  // keep the last `expected` offsets
+        b.ring_lo = (b.ring_lo >> 16) | (b.ring_hi << 48);
+        b.ring_hi >>= 16;
+        ring_set(b.ring_lo, b.ring_hi, expected - 1, o);
     }
     b.last_code_match = 0;
     if (b.code_len < expected) return;
     bool match = 0.0f >= p.similarity;
     unsigned long long cn = 0;
-    for (uint32_t j = 0; j < expected; ++j) cn += static_cast<unsigned long long>(b.ring[j]) * b.ring[j];
+    for (uint32_t j = 0; j < expected; ++j) {
+        const unsigned long long v = ring_get(b.ring_lo, b.ring_hi, j);
+        cn += v * v;
+    }
     for (uint32_t i = 0; i < b.learned_count && !match; ++i) {
-        const uint16_t* pat = lc + static_cast<size_t>(i) * stride;
+        unsigned long long plo, phi;
+        load_pattern(lc + static_cast<size_t>(i) * stride, stride, plo, phi);
         unsigned long long dot = 0, rn = 0;
         for (uint32_t j = 0; j < expected; ++j) {
-            dot += static_cast<unsigned long long>(pat[j]) * b.ring[j];
-            rn += static_cast<unsigned long long>(pat[j]) * pat[j];
+            const unsigned long long pv = ring_get(plo, phi, j);
+            dot += pv * ring_get(b.ring_lo, b.ring_hi, j);
+            rn += pv * pv;
         }
         match = cos_ge(dot, rn, cn, p.similarity);
     }
@@ -379,11 +447,11 @@ __device__ void code_update(SynB& b, uint32_t meta, const NeuronParam& p, uint32
     }
     if (b.learned_count >= p.max_refs) {
         for (uint32_t i = 1; i < b.learned_count; ++i)
-            for (uint32_t j = 0; j < expected; ++j)
+            for (uint32_t j = 0; j < stride; ++j)
                 lc[static_cast<size_t>(i - 1) * stride + j] = lc[static_cast<size_t>(i) * stride + j];
         b.learned_count -= 1;
     }
-    for (uint32_t j = 0; j < expected; ++j) lc[static_cast<size_t>(b.learned_count) * stride + j] = b.ring[j];
+    store_pattern(lc + static_cast<size_t>(b.learned_count) * stride, stride, b.ring_lo, b.ring_hi);
     b.learned_count += 1;
 }
 
@@ -580,6 +648,7 @@ __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, cons
     s.ring_used = q.ring_used;
     s.last_run = s.nruns > 0 ? e.cand[p.cand_base + s.nruns - 1] : 0ull;
     if (kOne && s.ref_count > 0) s.one = e.refmeta[p.meta_base];
+    s.snap_pending = false;
 
     uint32_t fires = 0;
     unsigned long long x = g[0];
@@ -640,6 +709,13 @@ __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, cons
     }
     if (s.nruns > 0) e.cand[p.cand_base + s.nruns - 1] = s.last_run;
     if (kOne && s.ref_count > 0) e.refmeta[p.meta_base] = s.one;
+    if (kOne && s.snap_pending) {
+        // runs 0 .. snap_nruns-2 are final in cand; the last one was saved
+        unsigned long long* ring = e.ring + p.ring_base;
+        const unsigned long long* cand = e.cand + p.cand_base;
+        for (uint32_t j = 0; j + 1 < s.snap_nruns; ++j) ring[(s.one.start + j) % p.ring_cap] = cand[j];
+        ring[(s.one.start + s.snap_nruns - 1) % p.ring_cap] = s.snap_last;
+    }
     NeuronRec w;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
@@ -675,7 +751,7 @@ __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, cons
 // or writes belongs to its target (the target's neuron state and the
 // target's incoming synapses); post-spike STDP of a fire is applied lazily
 // to synapses touched later in the tick and in bulk by k_post for the rest.
-__global__ void __launch_bounds__(kThreads) k_process(Engine e) {
+__global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(Engine e) {
     const uint32_t t = e.ts->tick;
     const uint32_t n_touched = e.ts->n_touched;
     const uint32_t n_due = e.ts->n_due;

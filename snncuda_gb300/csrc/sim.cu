@@ -995,7 +995,7 @@ int snncuda_sim_read_pattern(snncuda_sim* sim, int32_t kind, uint64_t index, uin
             const SynA a = sim->d2h(sim->e.syna + tm, 1)[0];
             const SynB b = sim->d2h(sim->e.synb + tm, 1)[0];
             if (kind == 2) {
-                v.assign(b.ring, b.ring + b.code_len);
+                for (uint32_t j = 0; j < b.code_len; ++j) v.push_back(ring_get(b.ring_lo, b.ring_hi, j));
             } else {
                 if (which >= b.learned_count) throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "pattern index out of range");
                 const uint32_t n = static_cast<uint32_t>(
@@ -1063,7 +1063,7 @@ int snncuda_sim_state_digest(snncuda_sim* sim, uint64_t* neuron_digest, uint64_t
                 d.f32(a.last_delta);
                 d.word(b.code_ws);
                 d.word(b.code_len);
-                for (uint32_t j = 0; j < b.code_len; ++j) d.word(b.ring[j]);
+                for (uint32_t j = 0; j < b.code_len; ++j) d.word(ring_get(b.ring_lo, b.ring_hi, j));
                 d.word(b.learned_count);
                 for (uint32_t j = 0; j < b.learned_count; ++j) {
                     synapse_learned(sim, h, tm, j, v);
