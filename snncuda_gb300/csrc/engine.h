@@ -57,10 +57,17 @@ struct alignas(32) SynB {
     uint8_t code_len;       // code_offsets.size() (<= expected)
     uint8_t last_code_match;
     uint16_t learned_count; // learned_code_patterns.size()
-    // code_offsets in order, 16 bits each: offsets 0-3 in ring_lo, 4-7 in ring_hi
+    // code_offsets in order, 16 bits each: offsets 0-3 in ring_lo, 4-7 in
+    // ring_hi.  When the target keeps a single reference pattern and no code
+    // has more than 4 offsets (inline_code_pattern), ring_hi instead holds the
+    // synapse's one learned code pattern.
     unsigned long long ring_lo;
     unsigned long long ring_hi;
 };
+
+__host__ __device__ inline bool inline_code_pattern(uint32_t max_refs, uint32_t code_stride) {
+    return max_refs == 1 && code_stride <= 4;
+}
 
 __host__ __device__ inline uint32_t ring_get(unsigned long long lo, unsigned long long hi, uint32_t j) {
     return static_cast<uint32_t>((j < 4 ? lo >> (16 * j) : hi >> (16 * (j - 4))) & 0xFFFFu);

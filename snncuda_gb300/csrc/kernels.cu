@@ -161,10 +161,19 @@ __device__ __forceinline__ float decay_factor(const Tables& tb, uint32_t code, u
 // representation: offsets inside a window never decrease, so the window is
 // kept as runs (value, count); learned patterns are run lists in a per-neuron
 // ring, each with running integer sums of its cosine against the window.
-// kOne: max_reference_patterns == 1, the single pattern's sums live in
-// registers (s.one) for the whole of the target's events in a tick.
+//
+// Applied once per target and tick for all k of its events: every event of
+// tick t appends the same offset t - window_start (only the first can restart
+// the window), and nothing in the neuron's temporal state feeds the membrane,
+// so the reference's per-event sequence of appends is reproduced here in one
+// pass.  Once no learned pattern is still being compared element by element
+// and a cached result already matches, every remaining append matches too
+// (the sums are frozen), which makes the common case O(1) per tick.
+// kOne: max_reference_patterns == 1, the single pattern lives in s.one.
 template <bool kOne>
-__device__ void temporal_update(NState& s, const NeuronParam& p, uint32_t t, const Engine& e, int enabled) {
+__device__ void temporal_tick(NState& s, const NeuronParam& p, uint32_t t, const Engine& e, int enabled,
+                              uint32_t k) {
+    if (k == 0) return;
     if (!enabled) {
         s.flags &= ~(1u << 8);
         return;
@@ -196,91 +205,117 @@ __device__ void temporal_update(NState& s, const NeuronParam& p, uint32_t t, con
     }
     const uint32_t o = t - s.ws;
     const unsigned long long oo = static_cast<unsigned long long>(o) * o;
-    if (s.nruns > 0 && run_value(s.last_run) == o) {
-        s.last_run += (1ull << 16);
-    } else {
-        if (s.nruns > p.window) {  // cannot happen: at most window+1 distinct offsets
-            raise_status(e, kStatusRunOverflow);
+    for (uint32_t j = 0; j < k; ++j) {
+        if (s.len >= 1 && s.ref_count > 0 && s.nruns > 0 && run_value(s.last_run) == o) {
+            bool frozen = true;
+            bool hit = 0.0f >= p.similarity;
+            for (uint32_t r = 0; r < s.ref_count; ++r) {
+                RefMeta& m = ref(r);
+                if (s.len + 1 <= m.len) {
+                    frozen = false;
+                    break;
+                }
+                if (!hit) {
+                    if (m.match == 2) m.match = cos_ge(m.dot, m.rn, m.cn, p.similarity) ? 1 : 0;
+                    hit = m.match == 1;
+                }
+            }
+            if (frozen && hit) {
+                const uint32_t n = k - j;
+                s.last_run += static_cast<unsigned long long>(n) << 16;
+                s.len += n;
+                s.cn += oo * n;
+                s.match_count += n;
+                s.flags |= (1u << 8);
+                return;
+            }
+        }
+        // one append (spike_offsets.push_back, :309)
+        if (s.nruns > 0 && run_value(s.last_run) == o) {
+            s.last_run += (1ull << 16);
+        } else {
+            if (s.nruns > p.window) {  // cannot happen: at most window+1 distinct offsets
+                raise_status(e, kStatusRunOverflow);
+                return;
+            }
+            if (s.nruns > 0) cand[s.nruns - 1] = s.last_run;
+            s.last_run = static_cast<unsigned long long>(o) | (1ull << 16);
+            s.nruns += 1;
+        }
+        s.len += 1;
+        s.cn += oo;
+        for (uint32_t r = 0; r < s.ref_count; ++r) {
+            RefMeta& m = ref(r);
+            if (s.len <= m.len) {
+                const unsigned long long run = ring[(m.start + m.cur_run) % p.ring_cap];
+                const unsigned long long v = run_value(run);
+                if (++m.cur_pos == run_count(run)) {
+                    m.cur_run += 1;
+                    m.cur_pos = 0;
+                }
+                m.dot += v * o;
+                m.rn += v * v;
+                m.cn += oo;
+                m.match = 2;
+            }
+        }
+        bool match = false;
+        if (s.ref_count > 0 && s.len >= 2) {
+            if (0.0f >= p.similarity) {
+                match = true;
+            } else {
+                for (uint32_t r = 0; r < s.ref_count && !match; ++r) {
+                    RefMeta& m = ref(r);
+                    if (m.match == 2) m.match = cos_ge(m.dot, m.rn, m.cn, p.similarity) ? 1 : 0;
+                    match = m.match == 1;
+                }
+            }
+        }
+        if (match) {
+            s.flags |= (1u << 8);
+            s.match_count += 1;
+            continue;
+        }
+        s.flags &= ~(1u << 8);
+        if (s.len < 2) continue;
+        // learn_pattern (:31-41): FIFO with max_reference_patterns entries.
+        if (s.ref_count >= p.max_refs) {
+            s.ring_used -= ref(0).nruns;
+            s.ref_head = (s.ref_head + 1) % p.max_refs;
+            s.ref_count -= 1;
+        }
+        if (s.ring_used + s.nruns > p.ring_cap) {
+            raise_status(e, kStatusRingOverflow);
             return;
         }
-        if (s.nruns > 0) cand[s.nruns - 1] = s.last_run;
-        s.last_run = static_cast<unsigned long long>(o) | (1ull << 16);
-        s.nruns += 1;
-    }
-    s.len += 1;
-    s.cn += oo;
-    for (uint32_t r = 0; r < s.ref_count; ++r) {
-        RefMeta& m = ref(r);
-        if (s.len <= m.len) {
-            const unsigned long long run = ring[(m.start + m.cur_run) % p.ring_cap];
-            const unsigned long long v = run_value(run);
-            if (++m.cur_pos == run_count(run)) {
-                m.cur_run += 1;
-                m.cur_pos = 0;
-            }
-            m.dot += v * o;
-            m.rn += v * v;
-            m.cn += oo;
-            m.match = 2;
-        }
-    }
-    bool match = false;
-    if (s.ref_count > 0 && s.len >= 2) {
-        if (0.0f >= p.similarity) {
-            match = true;
+        const uint32_t start = s.ring_head;
+        if constexpr (kOne) {
+            s.snap_pending = true;
+            s.snap_nruns = s.nruns;
+            s.snap_last = s.last_run;
         } else {
-            for (uint32_t r = 0; r < s.ref_count && !match; ++r) {
-                RefMeta& m = ref(r);
-                if (m.match == 2) m.match = cos_ge(m.dot, m.rn, m.cn, p.similarity) ? 1 : 0;
-                match = m.match == 1;
-            }
+            cand[s.nruns - 1] = s.last_run;
+            for (uint32_t i = 0; i < s.nruns; ++i) ring[(start + i) % p.ring_cap] = cand[i];
         }
+        s.ring_head = (start + s.nruns) % p.ring_cap;
+        s.ring_used += s.nruns;
+        RefMeta& m = ref(s.ref_count);
+        m.dot = s.cn;
+        m.rn = s.cn;
+        m.cn = s.cn;
+        m.start = start;
+        m.nruns = s.nruns;
+        m.len = s.len;
+        m.cur_run = 0;
+        m.cur_pos = 0;
+        m.match = 2;
+        s.ref_count += 1;
     }
-    if (match) {
-        s.flags |= (1u << 8);
-        s.match_count += 1;
-        return;
-    }
-    s.flags &= ~(1u << 8);
-    if (s.len < 2) return;
-    // learn_pattern: FIFO with max_reference_patterns entries.
-    if (s.ref_count >= p.max_refs) {
-        s.ring_used -= ref(0).nruns;
-        s.ref_head = (s.ref_head + 1) % p.max_refs;
-        s.ref_count -= 1;
-    }
-    if (s.ring_used + s.nruns > p.ring_cap) {
-        raise_status(e, kStatusRingOverflow);
-        return;
-    }
-    const uint32_t start = s.ring_head;
-    if constexpr (kOne) {
-        s.snap_pending = true;
-        s.snap_nruns = s.nruns;
-        s.snap_last = s.last_run;
-    } else {
-        cand[s.nruns - 1] = s.last_run;
-        for (uint32_t j = 0; j < s.nruns; ++j) ring[(start + j) % p.ring_cap] = cand[j];
-    }
-    s.ring_head = (start + s.nruns) % p.ring_cap;
-    s.ring_used += s.nruns;
-    RefMeta& m = ref(s.ref_count);
-    m.dot = s.cn;
-    m.rn = s.cn;
-    m.cn = s.cn;
-    m.start = start;
-    m.nruns = s.nruns;
-    m.len = s.len;
-    m.cur_run = 0;
-    m.cur_pos = 0;
-    m.match = 2;
-    s.ref_count += 1;
 }
 
 // SynapseDendriteProcessor.cpp:175-229.  Returns whether the neuron fired.
-template <bool kOne>
 __device__ bool process_input(NState& s, const NeuronParam& p, uint32_t comp, uint32_t rec, float w,
-                              uint32_t t, const Engine& e, int temporal) {
+                              uint32_t t, const Engine& e) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         if (t <= s.upd[k] || s.cur[k] == 0.0f) {
@@ -300,8 +335,7 @@ __device__ bool process_input(NState& s, const NeuronParam& p, uint32_t comp, ui
             s.flags = (s.flags & ~(3u << (2 * k))) | (rec << (2 * k));
         }
     }
-    s.last_active = t;
-    temporal_update<kOne>(s, p, t, e, temporal);
+    s.last_active = t;  // the temporal-pattern update of this event is done by temporal_tick
     s.membrane = __fadd_rn(__fadd_rn(__fadd_rn(s.cur[0], s.cur[1]), s.cur[2]), s.cur[3]);
     if (s.membrane >= p.threshold) {
         s.membrane = 0.0f;
@@ -400,9 +434,11 @@ __device__ __forceinline__ void store_pattern(uint16_t* pat, uint32_t stride, un
 }
 
 // SynapseDendriteProcessor.cpp:318-365 on a fixed ring of `expected` offsets
-// held in two 64-bit words.
+// held in two 64-bit words.  `inline_pattern`: the target keeps one reference
+// pattern and codes have at most 4 offsets, so the single learned code
+// pattern is stored in ring_hi instead of the pattern pool.
 __device__ void code_update(SynB& b, uint32_t meta, const NeuronParam& p, uint32_t t, uint16_t* lc,
-                            uint32_t stride, int enabled) {
+                            uint32_t stride, int enabled, bool inline_pattern) {
     if (!enabled) {
         b.last_code_match = 0;
         return;
@@ -416,7 +452,10 @@ __device__ void code_update(SynB& b, uint32_t meta, const NeuronParam& p, uint32
     if (b.code_len < expected) {
         ring_set(b.ring_lo, b.ring_hi, b.code_len, o);
         b.code_len += 1;
-    } else {  // keep the last `expected` offsets
+    } else if (inline_pattern) {  // keep the last `expected` offsets (all in ring_lo)
+        b.ring_lo >>= 16;
+        ring_set(b.ring_lo, b.ring_hi, expected - 1, o);
+    } else {
         b.ring_lo = (b.ring_lo >> 16) | (b.ring_hi << 48);
         b.ring_hi >>= 16;
         ring_set(b.ring_lo, b.ring_hi, expected - 1, o);
@@ -426,16 +465,20 @@ __device__ void code_update(SynB& b, uint32_t meta, const NeuronParam& p, uint32
     bool match = 0.0f >= p.similarity;
     unsigned long long cn = 0;
     for (uint32_t j = 0; j < expected; ++j) {
-        const unsigned long long v = ring_get(b.ring_lo, b.ring_hi, j);
+        const unsigned long long v = ring_get(b.ring_lo, inline_pattern ? 0ull : b.ring_hi, j);
         cn += v * v;
     }
     for (uint32_t i = 0; i < b.learned_count && !match; ++i) {
-        unsigned long long plo, phi;
-        load_pattern(lc + static_cast<size_t>(i) * stride, stride, plo, phi);
+        unsigned long long plo, phi = 0;
+        if (inline_pattern) {
+            plo = b.ring_hi;
+        } else {
+            load_pattern(lc + static_cast<size_t>(i) * stride, stride, plo, phi);
+        }
         unsigned long long dot = 0, rn = 0;
         for (uint32_t j = 0; j < expected; ++j) {
             const unsigned long long pv = ring_get(plo, phi, j);
-            dot += pv * ring_get(b.ring_lo, b.ring_hi, j);
+            dot += pv * ring_get(b.ring_lo, inline_pattern ? 0ull : b.ring_hi, j);
             rn += pv * pv;
         }
         match = cos_ge(dot, rn, cn, p.similarity);
@@ -443,6 +486,11 @@ __device__ void code_update(SynB& b, uint32_t meta, const NeuronParam& p, uint32
     if (match) {
         b.code_matches += 1;
         b.last_code_match = 1;
+        return;
+    }
+    if (inline_pattern) {
+        b.ring_hi = b.ring_lo;
+        b.learned_count = 1;
         return;
     }
     if (b.learned_count >= p.max_refs) {
@@ -680,7 +728,7 @@ __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, cons
         const uint32_t due = static_cast<uint32_t>(cur) & ~kExternalBit;
         bool fired;
         if (external) {
-            fired = process_input<kOne>(s, p, 0u, 0u, __uint_as_float(payload), t, e, temporal);
+            fired = process_input(s, p, 0u, 0u, __uint_as_float(payload), t, e);
         } else {
             const uint32_t tm = payload;
             post_catch_up(a, t, fires, e, stdp);
@@ -690,10 +738,10 @@ __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, cons
             if (plastic && a.last_post1 != 0) stdp_apply(a, pre_tick, a.last_post1 - 1, e, stdp);
             a.last_pre1 = pre_tick + 1;
             b.pre_count += 1;
-            fired = process_input<kOne>(s, p, (a.meta >> kMetaCompShift) & 3u, (a.meta >> kMetaRecShift) & 3u,
-                                        a.weight, t, e, temporal);
+            fired = process_input(s, p, (a.meta >> kMetaCompShift) & 3u, (a.meta >> kMetaRecShift) & 3u, a.weight,
+                                  t, e);
             uint16_t* lc = e.lcode + p.lcode_base + static_cast<size_t>(tm - p.in_begin) * p.max_refs * e.code_stride;
-            code_update(b, a.meta, p, t, lc, e.code_stride, temporal);
+            code_update(b, a.meta, p, t, lc, e.code_stride, temporal, kOne && e.code_stride <= 4);
             e.syna[tm] = a;
             e.synb[tm] = b;
             if (same_next) {
@@ -707,6 +755,7 @@ __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, cons
             e.fire_at[due] = n;
         }
     }
+    temporal_tick<kOne>(s, p, t, e, temporal, len);
     if (s.nruns > 0) e.cand[p.cand_base + s.nruns - 1] = s.last_run;
     if (kOne && s.ref_count > 0) e.refmeta[p.meta_base] = s.one;
     if (kOne && s.snap_pending) {

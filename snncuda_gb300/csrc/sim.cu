@@ -353,7 +353,8 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
         p.ring_base = ring_total;
         ring_total += p.ring_cap;
         p.lcode_base = lcode_total;
-        lcode_total += (in_ptr[n + 1] - in_ptr[n]) * refs * max_expected;
+        if (!inline_code_pattern(p.max_refs, max_expected))
+            lcode_total += (in_ptr[n + 1] - in_ptr[n]) * refs * max_expected;
     }
 
     // ---- synapse records, target-major ----
@@ -756,6 +757,11 @@ void synapse_learned(const snncuda_sim* sim, const HostState& h, uint64_t tm, ui
     const uint32_t n = static_cast<uint32_t>(std::upper_bound(sim->in_ptr.begin(), sim->in_ptr.end(), tm) -
                                              sim->in_ptr.begin() - 1);
     const NeuronParam& p = sim->nparam[n];
+    if (inline_code_pattern(p.max_refs, sim->e.code_stride)) {
+        out.clear();
+        for (uint32_t j = 0; j < expected_of(h.syna[tm]); ++j) out.push_back(ring_get(h.synb[tm].ring_hi, 0, j));
+        return;
+    }
     const uint16_t* lc = h.lcode.data() + p.lcode_base + (tm - p.in_begin) * p.max_refs * sim->e.code_stride +
                          static_cast<size_t>(which) * sim->e.code_stride;
     out.assign(lc, lc + expected_of(h.syna[tm]));
@@ -775,7 +781,8 @@ HostState fetch_all(snncuda_sim* sim, bool temporal) {
             cand += p.window + 1;
             ring += p.ring_cap;
             meta += p.max_refs;
-            lcode += (sim->in_ptr[n + 1] - sim->in_ptr[n]) * p.max_refs * e.code_stride;
+            if (!inline_code_pattern(p.max_refs, e.code_stride))
+                lcode += (sim->in_ptr[n + 1] - sim->in_ptr[n]) * p.max_refs * e.code_stride;
         }
         h.cand = sim->d2h(e.cand, cand);
         h.ring = sim->d2h(e.ring, ring);
@@ -995,16 +1002,20 @@ int snncuda_sim_read_pattern(snncuda_sim* sim, int32_t kind, uint64_t index, uin
             const SynA a = sim->d2h(sim->e.syna + tm, 1)[0];
             const SynB b = sim->d2h(sim->e.synb + tm, 1)[0];
             if (kind == 2) {
-                for (uint32_t j = 0; j < b.code_len; ++j) v.push_back(ring_get(b.ring_lo, b.ring_hi, j));
+                for (uint32_t j = 0; j < b.code_len; ++j) v.push_back(ring_get(b.ring_lo, b.ring_hi, j));  // code_len <= 4 when inline
             } else {
                 if (which >= b.learned_count) throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "pattern index out of range");
                 const uint32_t n = static_cast<uint32_t>(
                     std::upper_bound(sim->in_ptr.begin(), sim->in_ptr.end(), tm) - sim->in_ptr.begin() - 1);
                 const NeuronParam& p = sim->nparam[n];
-                const uint64_t off = p.lcode_base + (tm - p.in_begin) * p.max_refs * sim->e.code_stride +
-                                     which * sim->e.code_stride;
-                const std::vector<uint16_t> lc = sim->d2h(sim->e.lcode + off, expected_of(a));
-                v.assign(lc.begin(), lc.end());
+                if (inline_code_pattern(p.max_refs, sim->e.code_stride)) {
+                    for (uint32_t j = 0; j < expected_of(a); ++j) v.push_back(ring_get(b.ring_hi, 0, j));
+                } else {
+                    const uint64_t off = p.lcode_base + (tm - p.in_begin) * p.max_refs * sim->e.code_stride +
+                                         which * sim->e.code_stride;
+                    const std::vector<uint16_t> lc = sim->d2h(sim->e.lcode + off, expected_of(a));
+                    v.assign(lc.begin(), lc.end());
+                }
             }
         } else {
             throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "unknown pattern kind");
