@@ -119,6 +119,17 @@ __device__ void block_scan_inplace(uint32_t* data, uint32_t n, uint32_t* total_o
 // per-event physics
 // ---------------------------------------------------------------------------
 
+// Approximate u64 -> f32 (relative error < 2^-22) from 32-bit bit operations.
+// Conversions with 64-bit operands run on the FP64 pipe, which GB300 keeps
+// small; this estimate only feeds the threshold screen below.
+__device__ __forceinline__ float u64_to_f32_approx(unsigned long long x) {
+    if (x < (1ull << 23)) return __int_as_float(0x4B000000u | static_cast<uint32_t>(x)) - 8388608.0f;
+    const int sh = 41 - __clzll(static_cast<long long>(x));  // x >> sh < 2^23
+    const uint32_t m = static_cast<uint32_t>(x >> sh);
+    const float f = __int_as_float(0x4B000000u | m) - 8388608.0f;
+    return f * __int_as_float((127 + sh) << 23);
+}
+
 // float(dot / (sqrt(rn) * sqrt(cn))) >= sim for sim > 0
 // (TemporalPattern.cpp:35-60, :20-22).  dot, rn, cn are the exact integer
 // sums the reference accumulates in double.  A single-precision estimate
@@ -126,13 +137,19 @@ __device__ void block_scan_inplace(uint32_t* data, uint32_t n, uint32_t* total_o
 // threshold; the rest take the reference's exact double expression.
 __device__ bool cos_ge(unsigned long long dot, unsigned long long rn, unsigned long long cn, float sim) {
     if (rn == 0 || cn == 0) return false;  // similarity 0.0f < sim
-    const float est = __fmul_rn(__fmul_rn(__ull2float_rn(dot), rsqrtf(__ull2float_rn(rn))),
-                                rsqrtf(__ull2float_rn(cn)));
+    const float est = __fmul_rn(__fmul_rn(u64_to_f32_approx(dot), rsqrtf(u64_to_f32_approx(rn))),
+                                rsqrtf(u64_to_f32_approx(cn)));
     if (est >= sim * 1.00002f) return true;
     if (est <= sim * 0.99998f) return false;
     const double q = __ddiv_rn(__ull2double_rn(dot),
                                __dmul_rn(__dsqrt_rn(__ull2double_rn(rn)), __dsqrt_rn(__ull2double_rn(cn))));
     return __double2float_rn(q) >= sim;
+}
+
+// (a + b) mod m for a < m and b <= m, without an integer division.
+__device__ __forceinline__ uint32_t wrap_add(uint32_t a, uint32_t b, uint32_t m) {
+    const uint32_t x = a + b;
+    return x >= m ? x - m : x;
 }
 
 struct NState {
@@ -185,7 +202,7 @@ __device__ void temporal_tick(NState& s, const NeuronParam& p, uint32_t t, const
         if constexpr (kOne) {
             return s.one;
         } else {
-            return meta[(s.ref_head + r) % p.max_refs];
+            return meta[wrap_add(s.ref_head, r, p.max_refs)];
         }
     };
     if (s.len == 0 || t - s.ws > p.window) {
@@ -247,7 +264,7 @@ __device__ void temporal_tick(NState& s, const NeuronParam& p, uint32_t t, const
         for (uint32_t r = 0; r < s.ref_count; ++r) {
             RefMeta& m = ref(r);
             if (s.len <= m.len) {
-                const unsigned long long run = ring[(m.start + m.cur_run) % p.ring_cap];
+                const unsigned long long run = ring[wrap_add(m.start, m.cur_run, p.ring_cap)];
                 const unsigned long long v = run_value(run);
                 if (++m.cur_pos == run_count(run)) {
                     m.cur_run += 1;
@@ -281,7 +298,7 @@ __device__ void temporal_tick(NState& s, const NeuronParam& p, uint32_t t, const
         // learn_pattern (:31-41): FIFO with max_reference_patterns entries.
         if (s.ref_count >= p.max_refs) {
             s.ring_used -= ref(0).nruns;
-            s.ref_head = (s.ref_head + 1) % p.max_refs;
+            s.ref_head = wrap_add(s.ref_head, 1, p.max_refs);
             s.ref_count -= 1;
         }
         if (s.ring_used + s.nruns > p.ring_cap) {
@@ -295,9 +312,9 @@ __device__ void temporal_tick(NState& s, const NeuronParam& p, uint32_t t, const
             s.snap_last = s.last_run;
         } else {
             cand[s.nruns - 1] = s.last_run;
-            for (uint32_t i = 0; i < s.nruns; ++i) ring[(start + i) % p.ring_cap] = cand[i];
+            for (uint32_t i = 0; i < s.nruns; ++i) ring[wrap_add(start, i, p.ring_cap)] = cand[i];
         }
-        s.ring_head = (start + s.nruns) % p.ring_cap;
+        s.ring_head = wrap_add(start, s.nruns, p.ring_cap);
         s.ring_used += s.nruns;
         RefMeta& m = ref(s.ref_count);
         m.dot = s.cn;
@@ -762,8 +779,8 @@ __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, cons
         // runs 0 .. snap_nruns-2 are final in cand; the last one was saved
         unsigned long long* ring = e.ring + p.ring_base;
         const unsigned long long* cand = e.cand + p.cand_base;
-        for (uint32_t j = 0; j + 1 < s.snap_nruns; ++j) ring[(s.one.start + j) % p.ring_cap] = cand[j];
-        ring[(s.one.start + s.snap_nruns - 1) % p.ring_cap] = s.snap_last;
+        for (uint32_t j = 0; j + 1 < s.snap_nruns; ++j) ring[wrap_add(s.one.start, j, p.ring_cap)] = cand[j];
+        ring[wrap_add(s.one.start, s.snap_nruns - 1, p.ring_cap)] = s.snap_last;
     }
     NeuronRec w;
 #pragma unroll
