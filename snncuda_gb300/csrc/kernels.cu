@@ -130,20 +130,29 @@ __device__ __forceinline__ float u64_to_f32_approx(unsigned long long x) {
     return f * __int_as_float((127 + sh) << 23);
 }
 
+// The reference's exact expression, in double.  Kept out of line: inlined,
+// its 64-bit conversions get hoisted above the branch into every call and
+// occupy GB300's small FP64 pipe.
+__device__ __noinline__ bool cos_ge_exact(unsigned long long dot, unsigned long long rn, unsigned long long cn,
+                                          float sim) {
+    const double q = __ddiv_rn(__ull2double_rn(dot),
+                               __dmul_rn(__dsqrt_rn(__ull2double_rn(rn)), __dsqrt_rn(__ull2double_rn(cn))));
+    return __double2float_rn(q) >= sim;
+}
+
 // float(dot / (sqrt(rn) * sqrt(cn))) >= sim for sim > 0
 // (TemporalPattern.cpp:35-60, :20-22).  dot, rn, cn are the exact integer
 // sums the reference accumulates in double.  A single-precision estimate
 // (relative error < 1e-6) decides every case farther than 2e-5 from the
 // threshold; the rest take the reference's exact double expression.
-__device__ bool cos_ge(unsigned long long dot, unsigned long long rn, unsigned long long cn, float sim) {
+__device__ __forceinline__ bool cos_ge(unsigned long long dot, unsigned long long rn, unsigned long long cn,
+                                       float sim) {
     if (rn == 0 || cn == 0) return false;  // similarity 0.0f < sim
     const float est = __fmul_rn(__fmul_rn(u64_to_f32_approx(dot), rsqrtf(u64_to_f32_approx(rn))),
                                 rsqrtf(u64_to_f32_approx(cn)));
     if (est >= sim * 1.00002f) return true;
     if (est <= sim * 0.99998f) return false;
-    const double q = __ddiv_rn(__ull2double_rn(dot),
-                               __dmul_rn(__dsqrt_rn(__ull2double_rn(rn)), __dsqrt_rn(__ull2double_rn(cn))));
-    return __double2float_rn(q) >= sim;
+    return cos_ge_exact(dot, rn, cn, sim);
 }
 
 // (a + b) mod m for a < m and b <= m, without an integer division.
