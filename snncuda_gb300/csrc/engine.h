@@ -55,7 +55,7 @@ struct alignas(32) SynB {
     uint32_t code_ws;       // code_window_start_tick
     uint32_t code_matches;  // code_match_count
     uint8_t code_len;       // code_offsets.size() (<= expected)
-    uint8_t last_code_match;
+    uint8_t flags;          // bit 0: last_code_match; bits 4-7: expected = max(2, #code offsets)
     uint16_t learned_count; // learned_code_patterns.size()
     // code_offsets in order, 16 bits each: offsets 0-3 in ring_lo, 4-7 in
     // ring_hi.  When the target keeps a single reference pattern and no code
@@ -200,6 +200,8 @@ struct Engine {
     uint32_t* touched;                     // [N] target ids with due events, ascending
     unsigned long long* grp;               // [slot_cap] (payload << 32) | (due index | ext << 31)
     unsigned long long* grp_sorted;        // [slot_cap] grp with every target's group in due order
+    uint32_t* evt_tgt;                     // [slot_cap] target of each grp_sorted entry
+    uint32_t* seg_len;                     // [N] due events of each touched target
     uint32_t* fire_bits;                   // [slot_cap/32] bitmap of due positions that fired
     uint32_t* fire_at;                     // [slot_cap] firing neuron at a due position
     uint32_t* fire_tile;                   // bitmap tile bases
@@ -224,17 +226,19 @@ struct Engine {
     uint32_t grid_fire;
 };
 
-constexpr int kScanTile = 4096;          // entries per scan tile (256 threads x 16)
+constexpr int kScanTile = 1024;          // entries per scan tile (256 threads x 4)
 constexpr int kExpandFires = 8;          // fires per expansion block (one warp each)
 constexpr uint32_t kMaxClasses = 256;    // distinct delivery delays
 
 // Host-side launchers (kernels.cu).
 // `marks` (optional) holds 2 * kKernelCount events recorded around every
 // kernel (before, after) for profiling graphs.
-constexpr int kKernelCount = 10;
+constexpr int kKernelCount = 11;
 void launch_tick(const Engine& e, cudaStream_t stream, cudaEvent_t* marks = nullptr);
 const char* kernel_name(int index);
 void launch_inject(const Engine& e, const unsigned long long* ev, const uint32_t* slot_of_group,
                    const uint32_t* group_off, uint32_t groups, cudaStream_t stream);
+// Zeroes the code-pattern records and stores each synapse's `expected`.
+void launch_init_synb(const Engine& e, cudaStream_t stream);
 
 }  // namespace snngb

@@ -463,18 +463,16 @@ __device__ __forceinline__ void store_pattern(uint16_t* pat, uint32_t stride, un
 // held in two 64-bit words.  `inline_pattern`: the target keeps one reference
 // pattern and codes have at most 4 offsets, so the single learned code
 // pattern is stored in ring_hi instead of the pattern pool.
-__device__ void code_update(SynB& b, uint32_t meta, const NeuronParam& p, uint32_t t, uint16_t* lc,
-                            uint32_t stride, int enabled, bool inline_pattern) {
-    if (!enabled) {
-        b.last_code_match = 0;
-        return;
-    }
+__device__ void code_update(SynB& b, const NeuronParam& p, uint32_t t, uint16_t* lc, uint32_t stride, int enabled,
+                            bool inline_pattern) {
+    b.flags &= 0xF0u;  // last_code_match = false
+    if (!enabled) return;
     if (b.code_len == 0 || t - b.code_ws > p.window) {
         b.code_ws = t;
         b.code_len = 0;
     }
     const uint32_t o = t - b.code_ws;
-    const uint32_t expected = (meta >> kMetaExpectedShift) & 15u;
+    const uint32_t expected = b.flags >> 4;
     if (b.code_len < expected) {
         ring_set(b.ring_lo, b.ring_hi, b.code_len, o);
         b.code_len += 1;
@@ -486,7 +484,6 @@ __device__ void code_update(SynB& b, uint32_t meta, const NeuronParam& p, uint32
         b.ring_hi >>= 16;
         ring_set(b.ring_lo, b.ring_hi, expected - 1, o);
     }
-    b.last_code_match = 0;
     if (b.code_len < expected) return;
     bool match = 0.0f >= p.similarity;
     unsigned long long cn = 0;
@@ -511,7 +508,7 @@ __device__ void code_update(SynB& b, uint32_t meta, const NeuronParam& p, uint32
     }
     if (match) {
         b.code_matches += 1;
-        b.last_code_match = 1;
+        b.flags |= 1u;
         return;
     }
     if (inline_pattern) {
@@ -574,12 +571,13 @@ __global__ void k_hist(Engine e) {
 // Phase 1 of the per-target scan: tile sums of counts and of touched targets;
 // the last block turns them into exclusive tile bases.
 __global__ void k_scan_tile(Engine e) {
+    constexpr int kItems = kScanTile / kThreads;
     const uint32_t tiles = (e.N + kScanTile - 1) / kScanTile;
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         uint32_t sum = 0, nz = 0;
-        const uint32_t base = tile * kScanTile + threadIdx.x * 16;
+        const uint32_t base = tile * kScanTile + threadIdx.x * kItems;
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
+        for (int j = 0; j < kItems; ++j) {
             const uint32_t i = base + j;
             const uint32_t c = i < e.N ? e.cnt[i] : 0;
             sum += c;
@@ -601,13 +599,14 @@ __global__ void k_scan_tile(Engine e) {
 
 // Phase 2: per-target segment starts and the ascending touched list.
 __global__ void k_scan_out(Engine e) {
+    constexpr int kItems = kScanTile / kThreads;
     const uint32_t tiles = (e.N + kScanTile - 1) / kScanTile;
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        const uint32_t base = tile * kScanTile + threadIdx.x * 16;
-        uint32_t c[16];
+        const uint32_t base = tile * kScanTile + threadIdx.x * kItems;
+        uint32_t c[kItems];
         uint32_t sum = 0, nz = 0;
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
+        for (int j = 0; j < kItems; ++j) {
             const uint32_t i = base + j;
             c[j] = i < e.N ? e.cnt[i] : 0;
             sum += c[j];
@@ -616,7 +615,7 @@ __global__ void k_scan_out(Engine e) {
         uint32_t seg = __ldcg(e.tile_sum + tile) + block_excl_scan(sum, nullptr);
         uint32_t pos = __ldcg(e.tile_nz + tile) + block_excl_scan(nz, nullptr);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
+        for (int j = 0; j < kItems; ++j) {
             const uint32_t i = base + j;
             if (i < e.N && c[j] != 0) {
                 e.seg_start[i] = seg;
@@ -653,11 +652,14 @@ __global__ void __launch_bounds__(kThreads) k_segsort(Engine e) {
     const int lane = threadIdx.x & 31;
     const uint32_t warps = gridDim.x * (blockDim.x / 32);
     for (uint32_t k = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); k < n_touched; k += warps) {
-        const uint32_t beg = e.seg_start[e.touched[k]];
+        const uint32_t n = e.touched[k];
+        const uint32_t beg = e.seg_start[n];
         const uint32_t end = k + 1 < n_touched ? e.seg_start[e.touched[k + 1]] : n_due;
         const uint32_t len = end - beg;
         const unsigned long long* src = e.grp + beg;
         unsigned long long* dst = e.grp_sorted + beg;
+        for (uint32_t j = lane; j < len; j += 32) e.evt_tgt[beg + j] = n;
+        if (lane == 0) e.seg_len[n] = len;
         if (len <= 32) {
             unsigned long long v = lane < static_cast<int>(len) ? src[lane] : ~0ull;
             uint32_t key = lane < static_cast<int>(len) ? static_cast<uint32_t>(v) & ~kExternalBit : 0xFFFFFFFFu;
@@ -690,9 +692,12 @@ __global__ void __launch_bounds__(kThreads) k_segsort(Engine e) {
 }
 
 // The events of one target in due order, then the reference's sequential
-// per-event loop (NetworkPropagator.cpp:80-131) restricted to this target.
-// Synapse records of the next event are loaded while the current one is
-// processed; a repeat of the same synapse takes the just-updated record.
+// per-event loop (NetworkPropagator.cpp:80-131) restricted to this target:
+// STDP state of the synapse (SynA) and the neuron's physics.  The synapse's
+// spike-code pattern and pre-spike count (SynB) depend on nothing the loop
+// computes and are updated by k_code.  The next event's SynA is loaded while
+// the current one is processed; a repeat of the same synapse takes the
+// just-updated record.
 template <bool kOne>
 __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, const unsigned long long* g,
                                                uint32_t len, uint32_t stride, uint32_t t, int stdp,
@@ -727,16 +732,10 @@ __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, cons
     uint32_t fires = 0;
     unsigned long long x = g[0];
     SynA na{};
-    SynB nb{};
-    if (!(static_cast<uint32_t>(x) & kExternalBit)) {
-        const uint32_t tm = static_cast<uint32_t>(x >> 32);
-        na = e.syna[tm];
-        nb = e.synb[tm];
-    }
+    if (!(static_cast<uint32_t>(x) & kExternalBit)) na = e.syna[static_cast<uint32_t>(x >> 32)];
     for (uint32_t i = 0; i < len; ++i) {
         const unsigned long long cur = x;
         SynA a = na;
-        SynB b = nb;
         const bool external = static_cast<uint32_t>(cur) & kExternalBit;
         const uint32_t payload = static_cast<uint32_t>(cur >> 32);
         bool same_next = false;
@@ -745,10 +744,7 @@ __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, cons
             if (!(static_cast<uint32_t>(x) & kExternalBit)) {
                 const uint32_t tm = static_cast<uint32_t>(x >> 32);
                 same_next = !external && tm == payload;
-                if (!same_next) {
-                    na = e.syna[tm];
-                    nb = e.synb[tm];
-                }
+                if (!same_next) na = e.syna[tm];
             }
         }
         const uint32_t due = static_cast<uint32_t>(cur) & ~kExternalBit;
@@ -763,17 +759,10 @@ __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, cons
             const bool plastic = (a.meta >> kMetaPlasticBit) & 1u;
             if (plastic && a.last_post1 != 0) stdp_apply(a, pre_tick, a.last_post1 - 1, e, stdp);
             a.last_pre1 = pre_tick + 1;
-            b.pre_count += 1;
             fired = process_input(s, p, (a.meta >> kMetaCompShift) & 3u, (a.meta >> kMetaRecShift) & 3u, a.weight,
                                   t, e);
-            uint16_t* lc = e.lcode + p.lcode_base + static_cast<size_t>(tm - p.in_begin) * p.max_refs * e.code_stride;
-            code_update(b, a.meta, p, t, lc, e.code_stride, temporal, kOne && e.code_stride <= 4);
             e.syna[tm] = a;
-            e.synb[tm] = b;
-            if (same_next) {
-                na = a;
-                nb = b;
-            }
+            if (same_next) na = a;
         }
         if (fired) {
             fires += 1;
@@ -842,6 +831,54 @@ __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(
         } else {
             process_target<false>(e, n, g, end - beg, 1, t, stdp, temporal);
         }
+    }
+}
+
+// Spike-code pattern and pre-spike count of every synaptic event
+// (SynapseDendriteProcessor.cpp:126, :133, :318-365), one thread per event.
+// These read and write only the synapse's own SynB record and the target's
+// parameters, so events run in parallel; several events of the same synapse
+// within the tick are applied in due order by the thread of the first one.
+__global__ void __launch_bounds__(kThreads) k_code(Engine e) {
+    const uint32_t t = e.ts->tick;
+    const uint32_t n_due = e.ts->n_due;
+    const int temporal = e.ts->temporal_enabled;
+    for (uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x; pos < n_due; pos += gridDim.x * blockDim.x) {
+        const unsigned long long x = e.grp_sorted[pos];
+        if (static_cast<uint32_t>(x) & kExternalBit) continue;
+        const uint32_t tm = static_cast<uint32_t>(x >> 32);
+        const uint32_t n = e.evt_tgt[pos];
+        const uint32_t beg = e.seg_start[n];
+        const uint32_t end = beg + e.seg_len[n];
+        bool first = true;
+        for (uint32_t q = beg; q < pos && first; ++q) {
+            const unsigned long long y = e.grp_sorted[q];
+            first = !(!(static_cast<uint32_t>(y) & kExternalBit) && static_cast<uint32_t>(y >> 32) == tm);
+        }
+        if (!first) continue;
+        const NeuronParam p = e.nparam[n];
+        uint16_t* lc = e.lcode + p.lcode_base + static_cast<size_t>(tm - p.in_begin) * p.max_refs * e.code_stride;
+        const bool inl = inline_code_pattern(p.max_refs, e.code_stride);
+        SynB b = e.synb[tm];
+        b.pre_count += 1;
+        code_update(b, p, t, lc, e.code_stride, temporal, inl);
+        for (uint32_t q = pos + 1; q < end; ++q) {
+            const unsigned long long y = e.grp_sorted[q];
+            if (!(static_cast<uint32_t>(y) & kExternalBit) && static_cast<uint32_t>(y >> 32) == tm) {
+                b.pre_count += 1;
+                code_update(b, p, t, lc, e.code_stride, temporal, inl);
+            }
+        }
+        e.synb[tm] = b;
+    }
+}
+
+__global__ void k_init_synb(const SynA* syna, SynB* synb, unsigned long long S) {
+    for (unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; i < S;
+         i += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+        SynB b{};
+        b.flags = static_cast<uint8_t>(((syna[i].meta >> kMetaExpectedShift) & 15u) << 4);
+        synb[i] = b;
     }
 }
 
@@ -1054,6 +1091,7 @@ void launch_tick(const Engine& e, cudaStream_t stream, cudaEvent_t* marks) {
     mark(false); k_scatter<<<wide, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_segsort<<<e.grid_wide * 4, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_process<<<e.grid_process, kThreads, 0, stream>>>(e); mark(true);
+    mark(false); k_code<<<e.grid_wide * 4, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_post<<<wide, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_fire_list<<<e.grid_fire, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_fire_count<<<e.grid_wide, kThreads, 0, stream>>>(e); mark(true);
@@ -1061,9 +1099,15 @@ void launch_tick(const Engine& e, cudaStream_t stream, cudaEvent_t* marks) {
 }
 
 const char* kernel_name(int index) {
-    static const char* names[kKernelCount] = {"k_hist",  "k_scan_tile", "k_scan_out",   "k_scatter", "k_segsort",
-                                              "k_process", "k_post",    "k_fire_list",  "k_fire_count", "k_expand"};
+    static const char* names[kKernelCount] = {"k_hist",   "k_scan_tile", "k_scan_out",  "k_scatter",
+                                              "k_segsort", "k_process",  "k_code",      "k_post",
+                                              "k_fire_list", "k_fire_count", "k_expand"};
     return index >= 0 && index < kKernelCount ? names[index] : "";
+}
+
+void launch_init_synb(const Engine& e, cudaStream_t stream) {
+    if (e.S == 0) return;
+    k_init_synb<<<1024, kThreads, 0, stream>>>(e.syna, e.synb, e.S);
 }
 
 void launch_inject(const Engine& e, const unsigned long long* ev, const uint32_t* slot_of_group,

@@ -507,6 +507,8 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.touched = dalloc<uint32_t>(own, N);
     e.grp = dalloc<unsigned long long>(own, slot_cap);
     e.grp_sorted = dalloc<unsigned long long>(own, slot_cap);
+    e.evt_tgt = dalloc<uint32_t>(own, slot_cap);
+    e.seg_len = dalloc<uint32_t>(own, N);
     e.fire_bits = dalloc<uint32_t>(own, bit_words);
     e.fire_at = dalloc<uint32_t>(own, slot_cap);
     e.fire_tile = dalloc<uint32_t>(own, fire_tiles + 2);
@@ -535,7 +537,6 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     zero(e.nrec, sizeof(NeuronRec) * N);
     zero(e.ntp, sizeof(NeuronTp) * N);
     h2d(e.syna, syna.data(), syna.size() * sizeof(SynA));
-    zero(e.synb, sizeof(SynB) * S);
     zero(e.lcode, sizeof(uint16_t) * lcode_total);
     h2d(d_pre_base, pre_base.data(), pre_base.size() * sizeof(unsigned long long));
     h2d(d_pre_off, pre_off.data(), pre_off.size() * sizeof(uint32_t));
@@ -565,6 +566,8 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.tab.ltp = d_ltp;
     e.tab.ltd = d_ltd;
     e.tab.stdp_len = static_cast<uint32_t>(ltp.size());
+    launch_init_synb(e, st);
+    check(cudaGetLastError(), "init launch");
     sim->in_ptr = std::move(in_ptr);
 
     int sms = 0;
@@ -971,7 +974,7 @@ int snncuda_sim_read_synapses(snncuda_sim* sim, const snncuda_synapse_state* o) 
             if (o->code_offset_count) o->code_offset_count[i] = b[tm].code_len;
             if (o->learned_code_count) o->learned_code_count[i] = b[tm].learned_count;
             if (o->code_match_count) o->code_match_count[i] = b[tm].code_matches;
-            if (o->last_code_match) o->last_code_match[i] = b[tm].last_code_match;
+            if (o->last_code_match) o->last_code_match[i] = b[tm].flags & 1u;
         }
     });
 }
@@ -1082,7 +1085,7 @@ int snncuda_sim_state_digest(snncuda_sim* sim, uint64_t* neuron_digest, uint64_t
                     for (uint32_t x : v) d.word(x);
                 }
                 d.word(b.code_matches);
-                d.word(b.last_code_match);
+                d.word(b.flags & 1u);
             }
             *synapse_digest = d.h;
         }
