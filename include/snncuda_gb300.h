@@ -233,6 +233,26 @@ typedef struct snncuda_profile {
 int snncuda_sim_profile(snncuda_sim* sim, uint64_t inclusive_tick, snncuda_profile* out);
 const char* snncuda_kernel_name(int32_t index);
 
+/* ---- building block: group a tick's due events by target ----------------
+ * Replaces, for one tick, the due list SpikeScheduler::pop_due returns
+ * (SpikeScheduler.cpp:25-47) as NetworkPropagator::process_tick consumes it
+ * per target (NetworkPropagator.cpp:80-131): the events regrouped by target
+ * neuron with their due order kept inside each target -- the engine's own
+ * grouping step.
+ *   events         device array of `count` event words: low 32 bits target
+ *                  neuron (bit 31 set for an external input), high 32 bits
+ *                  payload (synapse slot or input weight bits)
+ *   grouped        device array of `count` words: targets in ascending order,
+ *                  each target's events as (payload << 32) | (input index |
+ *                  external bit), in input order
+ *   segment_start  device array of neuron_count + 1 entries: first grouped
+ *                  word of each target; [neuron_count] = count
+ * Runs on cuda_stream (NULL: the legacy default stream) and returns when the
+ * device has finished.  Allocates and frees its scratch on every call.
+ * A target >= neuron_count fails with SNNCUDA_ERR_INVALID_ARGUMENT. */
+int snncuda_group_events(const uint64_t* events, uint32_t count, uint32_t neuron_count, uint64_t* grouped,
+                         uint32_t* segment_start, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

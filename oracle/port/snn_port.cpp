@@ -660,5 +660,28 @@ int snncuda_sim_profile(snncuda_sim* sim, uint64_t inclusive_tick, snncuda_profi
 
 const char* snncuda_kernel_name(int32_t) { return ""; }
 
+// Stable grouping of an event buffer by target (host memory here).
+int snncuda_group_events(const uint64_t* events, uint32_t count, uint32_t neuron_count, uint64_t* grouped,
+                         uint32_t* segment_start, void*) {
+    if ((count > 0 && (events == nullptr || grouped == nullptr)) || segment_start == nullptr)
+        return fail(SNNCUDA_ERR_INVALID_ARGUMENT, "null array");
+    std::vector<uint32_t> start(static_cast<size_t>(neuron_count) + 1, 0);
+    for (uint32_t i = 0; i < count; ++i) {
+        const uint32_t tgt = static_cast<uint32_t>(events[i]) & 0x7FFFFFFFu;
+        if (tgt >= neuron_count) return fail(SNNCUDA_ERR_INVALID_ARGUMENT, "event target >= neuron_count");
+        start[tgt + 1] += 1;
+    }
+    for (uint32_t n = 0; n < neuron_count; ++n) start[n + 1] += start[n];
+    for (uint32_t n = 0; n <= neuron_count; ++n) segment_start[n] = start[n];
+    for (uint32_t i = 0; i < count; ++i) {
+        const uint32_t lo = static_cast<uint32_t>(events[i]);
+        const uint32_t tgt = lo & 0x7FFFFFFFu;
+        grouped[start[tgt]++] = (events[i] & 0xFFFFFFFF00000000ULL) | (i | (lo & 0x80000000u));
+    }
+    return SNNCUDA_OK;
+}
+
 }  // extern "C"
+
+
 

@@ -149,6 +149,7 @@ _SIGNATURES = {
                                         POINTER(c_uint32)]),
     "snncuda_sim_profile": (c_int, [c_void_p, c_uint64, POINTER(Profile)]),
     "snncuda_kernel_name": (c_char_p, [c_int32]),
+    "snncuda_group_events": (c_int, [c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]),
 }
 
 # Symbols every implementation of the ABI must export.

@@ -29,6 +29,7 @@ constexpr uint32_t kStatusRasterOverflow = 1u << 2;
 constexpr uint32_t kStatusPostCountOverflow = 1u << 3;
 constexpr uint32_t kStatusRunOverflow = 1u << 4;
 constexpr uint32_t kStatusFireOverflow = 1u << 5;
+constexpr uint32_t kStatusBadEvent = 1u << 6;       // event target out of range (grouping input)
 
 // SynA.meta bit fields.
 constexpr uint32_t kMetaDelayMask = 0xFFFFu;
@@ -238,6 +239,9 @@ void launch_tick(const Engine& e, cudaStream_t stream, cudaEvent_t* marks = null
 const char* kernel_name(int index);
 void launch_inject(const Engine& e, const unsigned long long* ev, const uint32_t* slot_of_group,
                    const uint32_t* group_off, uint32_t groups, cudaStream_t stream);
+// Groups the W == 1 "wheel" of e (a caller's event buffer) by target: the
+// hist / scan / scatter / segment-sort kernels of a tick.
+void launch_group(const Engine& e, cudaStream_t stream);
 // Zeroes the code-pattern records and stores each synapse's `expected`.
 void launch_init_synb(const Engine& e, cudaStream_t stream);
 

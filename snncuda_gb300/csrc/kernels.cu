@@ -560,7 +560,12 @@ __global__ void k_hist(Engine e) {
     uint32_t ext = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t lo = static_cast<uint32_t>(ev[i]);
-        atomicAdd(&e.cnt[lo & ~kExternalBit], 1u);
+        const uint32_t tgt = lo & ~kExternalBit;
+        if (tgt >= e.N) {  // only reachable through snncuda_group_events with bad input
+            raise_status(e, kStatusBadEvent);
+            continue;
+        }
+        atomicAdd(&e.cnt[tgt], 1u);
         ext += lo >> 31;
     }
     ext = __reduce_add_sync(0xffffffffu, ext);
@@ -617,9 +622,9 @@ __global__ void k_scan_out(Engine e) {
 #pragma unroll
         for (int j = 0; j < kItems; ++j) {
             const uint32_t i = base + j;
-            if (i < e.N && c[j] != 0) {
-                e.seg_start[i] = seg;
-                e.touched[pos++] = i;
+            if (i < e.N) {
+                e.seg_start[i] = seg;  // also for targets without events (empty segment)
+                if (c[j] != 0) e.touched[pos++] = i;
             }
             seg += c[j];
         }
@@ -637,6 +642,7 @@ __global__ void k_scatter(Engine e) {
         const unsigned long long v = ev[i];
         const uint32_t lo = static_cast<uint32_t>(v);
         const uint32_t tgt = lo & ~kExternalBit;
+        if (tgt >= e.N) continue;
         const uint32_t pos = e.seg_start[tgt] + atomicSub(&e.cnt[tgt], 1u) - 1u;
         e.grp[pos] = (v & 0xFFFFFFFF00000000ull) | (i | (lo & kExternalBit));
     }
@@ -1103,6 +1109,16 @@ const char* kernel_name(int index) {
                                               "k_segsort", "k_process",  "k_code",      "k_post",
                                               "k_fire_list", "k_fire_count", "k_expand"};
     return index >= 0 && index < kKernelCount ? names[index] : "";
+}
+
+void launch_group(const Engine& e, cudaStream_t stream) {
+    const uint32_t tiles = (e.N + kScanTile - 1) / kScanTile;
+    const uint32_t scan_grid = tiles == 0 ? 1 : (tiles < e.grid_wide ? tiles : e.grid_wide);
+    k_hist<<<e.grid_wide, kThreads, 0, stream>>>(e);
+    k_scan_tile<<<scan_grid, kThreads, 0, stream>>>(e);
+    k_scan_out<<<scan_grid, kThreads, 0, stream>>>(e);
+    k_scatter<<<e.grid_wide, kThreads, 0, stream>>>(e);
+    k_segsort<<<e.grid_wide * 4, kThreads, 0, stream>>>(e);
 }
 
 void launch_init_synb(const Engine& e, cudaStream_t stream) {

@@ -1102,6 +1102,90 @@ int snncuda_sim_profile(snncuda_sim* sim, uint64_t inclusive_tick, snncuda_profi
 
 const char* snncuda_kernel_name(int32_t index) { return kernel_name(index); }
 
+namespace {
+
+// Scratch of one grouping call (device pointers).
+struct GroupScratch {
+    uint32_t* cnt;
+    uint32_t* tiles;      // tile_sum then tile_nz, (tiles + 2) each
+    uint32_t* touched;
+    uint32_t* seg_len;
+    unsigned long long* grp;
+    uint32_t* evt_tgt;
+    uint32_t* slot_count;
+    TickState* ts;
+};
+
+size_t group_tiles(uint32_t n) { return (static_cast<size_t>(n) + kScanTile - 1) / kScanTile + 2; }
+
+// The tick's grouping kernels (k_hist .. k_segsort) on a caller's event
+// buffer seen as a one-slot wheel.  Scratch must hold neuron_count (cnt,
+// touched, seg_len), group_tiles() (tiles, twice) and count (grp, evt_tgt)
+// entries; cnt and the tick state are cleared here.
+void group_run(const uint64_t* events, uint32_t count, uint32_t neuron_count, uint64_t* grouped,
+               uint32_t* segment_start, cudaStream_t st, const GroupScratch& sc) {
+    int dev = 0, sms = 0;
+    check(cudaGetDevice(&dev), "cudaGetDevice");
+    check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+    Engine e{};
+    e.N = neuron_count;
+    e.W = 1;
+    e.wmask = 0;
+    e.slot_cap = count;
+    e.wheel = const_cast<unsigned long long*>(reinterpret_cast<const unsigned long long*>(events));
+    e.slot_count = sc.slot_count;
+    e.cnt = sc.cnt;
+    e.seg_start = segment_start;
+    e.tile_sum = sc.tiles;
+    e.tile_nz = sc.tiles + group_tiles(neuron_count);
+    e.touched = sc.touched;
+    e.grp = sc.grp;
+    e.grp_sorted = reinterpret_cast<unsigned long long*>(grouped);
+    e.evt_tgt = sc.evt_tgt;
+    e.seg_len = sc.seg_len;
+    e.ts = sc.ts;
+    e.grid_wide = static_cast<uint32_t>(std::max(1, sms * 2));
+    check(cudaMemsetAsync(sc.cnt, 0, sizeof(uint32_t) * std::max<uint32_t>(neuron_count, 1), st), "memset");
+    check(cudaMemsetAsync(sc.ts, 0, sizeof(TickState), st), "memset");
+    check(cudaMemsetAsync(sc.tiles, 0, sizeof(uint32_t) * 2 * group_tiles(neuron_count), st), "memset");
+    check(cudaMemcpyAsync(sc.slot_count, &count, sizeof(uint32_t), cudaMemcpyHostToDevice, st), "count");
+    launch_group(e, st);
+    check(cudaGetLastError(), "group launch");
+    check(cudaMemcpyAsync(segment_start + neuron_count, &count, sizeof(uint32_t), cudaMemcpyHostToDevice, st),
+          "segment end");
+    TickState ts;
+    check(cudaMemcpyAsync(&ts, sc.ts, sizeof(ts), cudaMemcpyDeviceToHost, st), "status");
+    check(cudaStreamSynchronize(st), "group synchronize");
+    if (ts.status & kStatusBadEvent) throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "event target >= neuron_count");
+}
+
+}  // namespace
+
+int snncuda_group_events(const uint64_t* events, uint32_t count, uint32_t neuron_count, uint64_t* grouped,
+                         uint32_t* segment_start, void* cuda_stream) {
+    if ((count > 0 && (events == nullptr || grouped == nullptr)) || segment_start == nullptr)
+        return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null array");
+    if (count >= (1u << 31) || neuron_count >= (1u << 31))
+        return set_error(SNNCUDA_ERR_UNSUPPORTED, "at most 2^31-1 events and neurons");
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    std::vector<void*> owned;
+    const int rc = guarded([&] {
+        GroupScratch sc;
+        sc.cnt = dalloc<uint32_t>(owned, neuron_count);
+        sc.tiles = dalloc<uint32_t>(owned, 2 * group_tiles(neuron_count));
+        sc.touched = dalloc<uint32_t>(owned, neuron_count);
+        sc.seg_len = dalloc<uint32_t>(owned, neuron_count);
+        sc.grp = dalloc<unsigned long long>(owned, count);
+        sc.evt_tgt = dalloc<uint32_t>(owned, count);
+        sc.slot_count = dalloc<uint32_t>(owned, 1);
+        sc.ts = dalloc<TickState>(owned, 1);
+        group_run(events, count, neuron_count, grouped, segment_start, st, sc);
+    });
+    if (rc != SNNCUDA_OK) cudaStreamSynchronize(st);
+    for (void* p : owned) cudaFree(p);
+    return rc;
+}
+
 int snncuda_sim_read_raster(snncuda_sim* sim, uint64_t first, uint64_t count, uint64_t* ticks, uint32_t* neurons) {
     if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
     return guarded([&] {

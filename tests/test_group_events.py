@@ -1,0 +1,80 @@
+"""The grouping building block (snncuda_group_events): a tick's due events
+regrouped by target neuron with due order kept inside each target, checked
+against a numpy restatement on random event buffers (CPU oracle here, GPU
+backend under the gpu mark)."""
+
+import numpy as np
+import pytest
+
+EXT = np.uint64(0x80000000)
+
+
+def make_events(rng, count, neurons, external_fraction=0.1):
+    tgt = rng.integers(0, neurons, count, dtype=np.uint64)
+    ext = rng.random(count) < external_fraction
+    payload = rng.integers(0, 1 << 32, count, dtype=np.uint64)
+    return (payload << np.uint64(32)) | tgt | np.where(ext, EXT, np.uint64(0))
+
+
+def expected_grouping(events, neurons):
+    lo = events & np.uint64(0xFFFFFFFF)
+    tgt = (lo & np.uint64(0x7FFFFFFF)).astype(np.int64)
+    order = np.argsort(tgt, kind="stable")
+    idx = np.arange(events.size, dtype=np.uint64)
+    word = (events & np.uint64(0xFFFFFFFF00000000)) | idx | (lo & EXT)
+    start = np.zeros(neurons + 1, np.uint32)
+    np.cumsum(np.bincount(tgt, minlength=neurons), out=start[1:])
+    return word[order], start
+
+
+def run_host(lib, events, neurons):
+    grouped = np.zeros(max(events.size, 1), np.uint64)
+    start = np.zeros(neurons + 1, np.uint32)
+    rc = lib.snncuda_group_events(events.ctypes.data, events.size, neurons, grouped.ctypes.data,
+                                  start.ctypes.data, None)
+    return rc, grouped[:events.size], start
+
+
+@pytest.mark.parametrize("count,neurons", [(0, 5), (1, 1), (1000, 37), (50_000, 4096)])
+def test_oracle_grouping(port_lib, count, neurons):
+    rng = np.random.default_rng(count + neurons)
+    ev = make_events(rng, count, neurons)
+    rc, g, s = run_host(port_lib, ev, neurons)
+    assert rc == 0
+    want_g, want_s = expected_grouping(ev, neurons)
+    assert np.array_equal(g, want_g) and np.array_equal(s, want_s)
+
+
+def test_oracle_rejects_bad_target(port_lib):
+    ev = np.array([5], np.uint64)
+    assert run_host(port_lib, ev, 5)[0] == 1
+
+
+def run_device(lib, events, neurons, fn="snncuda_group_events"):
+    import torch
+    d_ev = torch.from_numpy(events.view(np.int64)).cuda()
+    d_g = torch.zeros(max(events.size, 1), dtype=torch.int64, device="cuda")
+    d_s = torch.zeros(neurons + 1, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    rc = getattr(lib, fn)(d_ev.data_ptr(), events.size, neurons, d_g.data_ptr(), d_s.data_ptr(),
+                          stream.cuda_stream)
+    torch.cuda.synchronize()
+    return rc, d_g.cpu().numpy().view(np.uint64)[:events.size], d_s.cpu().numpy().view(np.uint32)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("count,neurons", [(1, 1), (1000, 37), (300_000, 100_000), (200_000, 50)])
+def test_gpu_grouping(gpu_lib, count, neurons):
+    rng = np.random.default_rng(count * 7 + neurons)
+    ev = make_events(rng, count, neurons)
+    rc, g, s = run_device(gpu_lib, ev, neurons)
+    assert rc == 0
+    want_g, want_s = expected_grouping(ev, neurons)
+    assert np.array_equal(s, want_s)
+    assert np.array_equal(g, want_g)
+
+
+@pytest.mark.gpu
+def test_gpu_grouping_rejects_bad_target(gpu_lib):
+    ev = np.array([3, 9], np.uint64)
+    assert run_device(gpu_lib, ev, 5)[0] == 1
