@@ -253,6 +253,28 @@ const char* snncuda_kernel_name(int32_t index);
 int snncuda_group_events(const uint64_t* events, uint32_t count, uint32_t neuron_count, uint64_t* grouped,
                          uint32_t* segment_start, void* cuda_stream);
 
+/* ---- no-allocation variant of snncuda_group_events -----------------------
+ * Has no counterpart in the reference.  For callers that cannot allocate
+ * device memory at the point of the call: code whose device memory is owned
+ * by another allocator's pool or budget (a host framework's caching
+ * allocator), and latency-critical loops that must not pay cudaMalloc /
+ * cudaFree, which can synchronize the whole device and stall other streams.
+ * Same arguments and results as snncuda_group_events; the caller still
+ * provides the inputs and outputs, but the scratch (per-neuron counters,
+ * scan tiles, the unsorted groups) lives in one static device array compiled
+ * into the library (about 15 MB, held on every GPU that loads the library
+ * until the process exits).  Limits: count <= SNNCUDA_GROUP_STATIC_MAX_EVENTS
+ * and neuron_count <= SNNCUDA_GROUP_STATIC_MAX_NEURONS, otherwise
+ * SNNCUDA_ERR_CAPACITY.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current; make that
+ * first call before any stream capture.  Every call shares the one array:
+ * calls that overlap on the GPU (other streams or host threads) race and must
+ * be serialized by the caller. */
+#define SNNCUDA_GROUP_STATIC_MAX_EVENTS (1u << 20)
+#define SNNCUDA_GROUP_STATIC_MAX_NEURONS (1u << 18)
+int snncuda_group_events_static(const uint64_t* events, uint32_t count, uint32_t neuron_count,
+                                uint64_t* grouped, uint32_t* segment_start, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -681,6 +681,14 @@ int snncuda_group_events(const uint64_t* events, uint32_t count, uint32_t neuron
     return SNNCUDA_OK;
 }
 
+// Same as snncuda_group_events here (the oracle has no device scratch).
+int snncuda_group_events_static(const uint64_t* events, uint32_t count, uint32_t neuron_count,
+                                uint64_t* grouped, uint32_t* segment_start, void* stream) {
+    if (count > SNNCUDA_GROUP_STATIC_MAX_EVENTS || neuron_count > SNNCUDA_GROUP_STATIC_MAX_NEURONS)
+        return fail(SNNCUDA_ERR_CAPACITY, "beyond the static grouping limits");
+    return snncuda_group_events(events, count, neuron_count, grouped, segment_start, stream);
+}
+
 }  // extern "C"
 
 

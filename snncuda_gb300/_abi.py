@@ -150,6 +150,7 @@ _SIGNATURES = {
     "snncuda_sim_profile": (c_int, [c_void_p, c_uint64, POINTER(Profile)]),
     "snncuda_kernel_name": (c_char_p, [c_int32]),
     "snncuda_group_events": (c_int, [c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]),
+    "snncuda_group_events_static": (c_int, [c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]),
 }
 
 # Symbols every implementation of the ABI must export.

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -1184,6 +1185,70 @@ int snncuda_group_events(const uint64_t* events, uint32_t count, uint32_t neuron
     if (rc != SNNCUDA_OK) cudaStreamSynchronize(st);
     for (void* p : owned) cudaFree(p);
     return rc;
+}
+
+namespace {
+
+// Static scratch of snncuda_group_events_static: counters, tiles and groups
+// for at most kStaticEvents events over kStaticNeurons neurons.
+constexpr size_t kStaticEvents = SNNCUDA_GROUP_STATIC_MAX_EVENTS;
+constexpr size_t kStaticNeurons = SNNCUDA_GROUP_STATIC_MAX_NEURONS;
+constexpr size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+constexpr size_t kOffCnt = 0;
+constexpr size_t kOffTouched = kOffCnt + align256(kStaticNeurons * 4);
+constexpr size_t kOffSegLen = kOffTouched + align256(kStaticNeurons * 4);
+constexpr size_t kOffTiles = kOffSegLen + align256(kStaticNeurons * 4);
+constexpr size_t kOffGrp = kOffTiles + align256(2 * ((kStaticNeurons + kScanTile - 1) / kScanTile + 2) * 4);
+constexpr size_t kOffEvtTgt = kOffGrp + align256(kStaticEvents * 8);
+constexpr size_t kOffSlot = kOffEvtTgt + align256(kStaticEvents * 4);
+constexpr size_t kOffTs = kOffSlot + 256;
+constexpr size_t kStaticBytes = kOffTs + align256(sizeof(TickState));
+
+static __device__ __align__(256) unsigned char g_group_scratch[kStaticBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+unsigned char* g_scratch_addr[kMaxDevices] = {};
+
+// Device address of the static scratch on the current device (looked up once
+// per device, with that device current).
+unsigned char* static_scratch() {
+    int dev = 0;
+    check(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "device index too large");
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (g_scratch_addr[dev] == nullptr) {
+        void* p = nullptr;
+        check(cudaGetSymbolAddress(&p, g_group_scratch), "cudaGetSymbolAddress");
+        g_scratch_addr[dev] = static_cast<unsigned char*>(p);
+    }
+    return g_scratch_addr[dev];
+}
+
+}  // namespace
+
+int snncuda_group_events_static(const uint64_t* events, uint32_t count, uint32_t neuron_count,
+                                uint64_t* grouped, uint32_t* segment_start, void* cuda_stream) {
+    if ((count > 0 && (events == nullptr || grouped == nullptr)) || segment_start == nullptr)
+        return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null array");
+    if (count > kStaticEvents || neuron_count > kStaticNeurons)
+        return set_error(SNNCUDA_ERR_CAPACITY,
+                         "snncuda_group_events_static handles at most 2^20 events and 2^18 neurons; "
+                         "use snncuda_group_events");
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    return guarded([&] {
+        unsigned char* base = static_scratch();
+        GroupScratch sc;
+        sc.cnt = reinterpret_cast<uint32_t*>(base + kOffCnt);
+        sc.touched = reinterpret_cast<uint32_t*>(base + kOffTouched);
+        sc.seg_len = reinterpret_cast<uint32_t*>(base + kOffSegLen);
+        sc.tiles = reinterpret_cast<uint32_t*>(base + kOffTiles);
+        sc.grp = reinterpret_cast<unsigned long long*>(base + kOffGrp);
+        sc.evt_tgt = reinterpret_cast<uint32_t*>(base + kOffEvtTgt);
+        sc.slot_count = reinterpret_cast<uint32_t*>(base + kOffSlot);
+        sc.ts = reinterpret_cast<TickState*>(base + kOffTs);
+        group_run(events, count, neuron_count, grouped, segment_start, st, sc);
+    });
 }
 
 int snncuda_sim_read_raster(snncuda_sim* sim, uint64_t first, uint64_t count, uint64_t* ticks, uint32_t* neurons) {
