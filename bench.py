@@ -45,10 +45,18 @@ sys.path.insert(0, str(ROOT))
 METRIC = "synaptic_events_per_s"
 UNIT = "events/s"
 ORACLE = ROOT / "oracle" / "_build" / "liboracle_port.so"
+KERNELS_PER_TICK = 11   # launch_tick in snncuda_gb300/csrc/kernels.cu
+# DRAM bytes (read + write) per launch of the dominant kernel on the default
+# stdp_100k workload, from one ncu capture of this code
+# (profiles/stdp_100k_kernel_launches.md); reported as roofline.traffic.
+MEASURED_TRAFFIC = {("stdp_100k", "k_process"): 186.4e6 + 28.8e6}
 
 # Per-unit algorithmic bytes of each kernel (device layout in
-# snncuda_gb300/csrc/engine.h).  See the design doc for the derivation.
-BYTES_PER_SYN_EVENT_PROCESS = 8 + 64 + 64       # grouped entry, SynA r+w, SynB r+w
+# snncuda_gb300/csrc/engine.h).  k_process walks each target's due events:
+# per synaptic event the grouped entry and the synapse's STDP record, per
+# external event the grouped entry, per touched target its parameters, its
+# dynamic and temporal records (read + write) and one run append.
+BYTES_PER_SYN_EVENT_PROCESS = 8 + 64            # grouped entry, SynA (32 B) read + write
 BYTES_PER_EXT_EVENT_PROCESS = 8
 BYTES_PER_TARGET_PROCESS = 64 + 128 + 64 + 8    # params, NeuronRec r+w, NeuronTp r+w, run append
 
@@ -211,6 +219,9 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
+        if not ORACLE.exists():
+            import __graft_entry__
+            __graft_entry__.build()
         print(json.dumps(run_reference(args, w)), flush=True)
         return
 
@@ -296,7 +307,9 @@ def main():
         avg_ms = km[top] / launches
         achieved = algo / (avg_ms / 1e3) / 1e9 if algo else None
         roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                    "frac": (achieved / peak) if achieved else None, "traffic": None,
+                    "frac": (achieved / peak) if achieved else None,
+                    "traffic": MEASURED_TRAFFIC.get((w.name, top)) if args.neurons is None and args.fanout is None
+                    else None,
                     "peak_source": peak_kind, "avg_launch_us": avg_ms * 1e3,
                     "algorithmic_bytes_per_launch": algo,
                     "kernel_share": {k: v / sum(km.values()) for k, v in km.items()}}
@@ -351,7 +364,7 @@ def main():
             "ticks_per_s": args.steps * tps / (ms_max / 1e3),
             "fires_per_tick": fires / (args.steps * tps),
             "events_per_tick": events / (args.steps * tps),
-            "gpu_launches": args.steps * tps * 8,
+            "gpu_launches": args.steps * tps * KERNELS_PER_TICK,
             "clocks": clocks, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
         }
         print(json.dumps(line), flush=True)
