@@ -45,20 +45,26 @@ sys.path.insert(0, str(ROOT))
 METRIC = "synaptic_events_per_s"
 UNIT = "events/s"
 ORACLE = ROOT / "oracle" / "_build" / "liboracle_port.so"
-KERNELS_PER_TICK = 11   # launch_tick in snncuda_gb300/csrc/kernels.cu
-# DRAM bytes (read + write) per launch of the dominant kernel on the default
-# stdp_100k workload, from one ncu capture of this code
-# (profiles/stdp_100k_kernel_launches.md); reported as roofline.traffic.
-MEASURED_TRAFFIC = {("stdp_100k", "k_process"): 186.4e6 + 28.8e6}
+KERNELS_PER_TICK = 10   # launch_tick in snncuda_gb300/csrc/kernels.cu
+# DRAM bytes (read + write) per launch of a kernel on the default stdp_100k
+# workload, from one ncu capture of this code (profiles/); reported as
+# roofline.traffic for the dominant kernel.
+MEASURED_TRAFFIC = {}
 
-# Per-unit algorithmic bytes of each kernel (device layout in
-# snncuda_gb300/csrc/engine.h).  k_process walks each target's due events:
-# per synaptic event the grouped entry and the synapse's STDP record, per
-# external event the grouped entry, per touched target its parameters, its
-# dynamic and temporal records (read + write) and one run append.
-BYTES_PER_SYN_EVENT_PROCESS = 8 + 64            # grouped entry, SynA (32 B) read + write
-BYTES_PER_EXT_EVENT_PROCESS = 8
-BYTES_PER_TARGET_PROCESS = 64 + 128 + 64 + 8    # params, NeuronRec r+w, NeuronTp r+w, run append
+# Algorithmic bytes of the two per-event kernels (device layout in
+# snncuda_gb300/csrc/engine.h), per synaptic event, per external event and
+# per touched target:
+#   k_events   reads the grouped entry (8) and the synapse record (64), writes
+#              the record (64), the event's input (16) and the STDP snapshot
+#              (32); external events: entry + input; per target its
+#              parameters (64) and segment bounds (12)
+#   k_process  reads each event's input (16); per target its parameters (64),
+#              dynamic and temporal records read + write (128 + 64) and one
+#              run append (8)
+BYTES_MODEL = {
+    "k_events": (8 + 64 + 64 + 16 + 32, 8 + 16, 64 + 12),
+    "k_process": (16, 16, 64 + 128 + 64 + 8),
+}
 
 
 def load_peaks():
@@ -298,10 +304,10 @@ def main():
         top = max(km, key=km.get)
         launches = prof["ticks"]
         peak, peak_kind = load_peaks()
-        if top == "k_process":
-            algo = (BYTES_PER_SYN_EVENT_PROCESS * prof["synaptic_events"] +
-                    BYTES_PER_EXT_EVENT_PROCESS * prof["external_events"] +
-                    BYTES_PER_TARGET_PROCESS * prof["touched_targets"]) / launches
+        if top in BYTES_MODEL:
+            per_syn, per_ext, per_tgt = BYTES_MODEL[top]
+            algo = (per_syn * prof["synaptic_events"] + per_ext * prof["external_events"] +
+                    per_tgt * prof["touched_targets"]) / launches
         else:
             algo = None
         avg_ms = km[top] / launches

@@ -4,8 +4,9 @@
 //   * neurons: NeuronRec (64 B, dynamic state), NeuronTp (32 B, temporal
 //     bookkeeping), NeuronParam (64 B, read-only) -- one per neuron;
 //   * synapses in target-major order (incoming lists of each target
-//     contiguous, Connectome order inside a list): SynA (32 B: weight, STDP
-//     state, static fields) and SynB (32 B: code-pattern state, counters);
+//     contiguous, Connectome order inside a list), one 64 B record each:
+//     SynA (weight, STDP state, static fields) + SynB (code-pattern state,
+//     counters), so the per-event work touches one DRAM line per event;
 //   * pre-expanded outgoing events: for every source, its (synapse, code
 //     offset) events grouped by delivery delay class, each class in
 //     Connectome x offset order -- spike-code expansion is then a copy;
@@ -65,6 +66,24 @@ struct alignas(32) SynB {
     unsigned long long ring_lo;
     unsigned long long ring_hi;
 };
+
+struct alignas(64) SynAB {
+    SynA a;
+    SynB b;
+};
+
+// Per-event input of the neuron walk, written by k_events in due order inside
+// every target's group: the weight after the event's pre-spike STDP (computed
+// as if the target had not fired earlier in the tick), compartment, receptor
+// and flags, the synapse and the due position.
+struct alignas(16) EvIn {
+    float weight;
+    uint32_t bits;  // comp | rec << 2 | external << 4 | repeat << 5
+    uint32_t tm;    // target-major synapse index (synaptic events)
+    uint32_t due;   // position in the tick's due list
+};
+constexpr uint32_t kEvExternal = 1u << 4;
+constexpr uint32_t kEvRepeat = 1u << 5;  // not the first event of its synapse in this tick
 
 __host__ __device__ inline bool inline_code_pattern(uint32_t max_refs, uint32_t code_stride) {
     return max_refs == 1 && code_stride <= 4;
@@ -181,8 +200,7 @@ struct Engine {
     unsigned long long* cand;              // run lists of current windows
     RefMeta* refmeta;
     unsigned long long* ring;              // learned-pattern runs
-    SynA* syna;                            // [S] target-major
-    SynB* synb;                            // [S]
+    SynAB* syn;                            // [S] target-major
     uint16_t* lcode;                       // learned code patterns
     const unsigned long long* pre_base;    // [N] first pre-expanded event of a source
     const uint32_t* pre_off;               // [N*(D+1)] class offsets within a source
@@ -200,9 +218,11 @@ struct Engine {
     uint32_t* tile_nz;
     uint32_t* touched;                     // [N] target ids with due events, ascending
     unsigned long long* grp;               // [slot_cap] (payload << 32) | (due index | ext << 31)
-    unsigned long long* grp_sorted;        // [slot_cap] grp with every target's group in due order
-    uint32_t* evt_tgt;                     // [slot_cap] target of each grp_sorted entry
-    uint32_t* seg_len;                     // [N] due events of each touched target
+    unsigned long long* grp_sorted;        // grouping entry point only: grp with every group in due order
+    uint32_t* evt_tgt;                     // grouping entry point only: target of each grp_sorted entry
+    uint32_t* seg_len;                     // grouping entry point only: due events of each touched target
+    EvIn* evin;                            // [slot_cap] per-event inputs of k_process, grouped, due order
+    SynA* ev_a0;                           // [slot_cap] each synaptic event's SynA before the event
     uint32_t* fire_bits;                   // [slot_cap/32] bitmap of due positions that fired
     uint32_t* fire_at;                     // [slot_cap] firing neuron at a due position
     uint32_t* fire_tile;                   // bitmap tile bases
@@ -234,7 +254,7 @@ constexpr uint32_t kMaxClasses = 256;    // distinct delivery delays
 // Host-side launchers (kernels.cu).
 // `marks` (optional) holds 2 * kKernelCount events recorded around every
 // kernel (before, after) for profiling graphs.
-constexpr int kKernelCount = 11;
+constexpr int kKernelCount = 10;
 void launch_tick(const Engine& e, cudaStream_t stream, cudaEvent_t* marks = nullptr);
 const char* kernel_name(int index);
 void launch_inject(const Engine& e, const unsigned long long* ev, const uint32_t* slot_of_group,
@@ -242,7 +262,8 @@ void launch_inject(const Engine& e, const unsigned long long* ev, const uint32_t
 // Groups the W == 1 "wheel" of e (a caller's event buffer) by target: the
 // hist / scan / scatter / segment-sort kernels of a tick.
 void launch_group(const Engine& e, cudaStream_t stream);
-// Zeroes the code-pattern records and stores each synapse's `expected`.
-void launch_init_synb(const Engine& e, cudaStream_t stream);
+// Builds the synapse records from SynA images (`a`, S entries): code-pattern
+// state zeroed, each synapse's `expected` stored.
+void launch_init_syn(const Engine& e, const SynA* a, cudaStream_t stream);
 
 }  // namespace snngb

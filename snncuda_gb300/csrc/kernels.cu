@@ -4,22 +4,29 @@
 // at t in the exact order the reference scheduler would pop them
 // (SpikeScheduler.cpp:25-47: bucket FIFO order).  Per tick:
 //
-//  1. k_hist      count due events per target (and move far-future injects
-//                 that become reachable into the wheel)
-//  2. k_scan_tile exclusive scan of the per-target counts (+ last block
-//                 scans the tile sums)
-//  3. k_scan_out  segment starts and the ascending list of touched targets
-//  4. k_scatter   group the due events by target (unordered inside a group)
-//  5. k_process   one thread per touched target: restore due order inside its
-//                 group, then run the reference per-event physics in order
-//                 (SynapseDendriteProcessor.cpp:89-212, :294-365) and mark
-//                 fires in a due-position bitmap
-//  6. k_post      post-spike STDP over the in-rows of targets that fired
-//                 (SynapseDendriteProcessor.cpp:138-173) + fire tile counts
-//  7. k_fire_list fires in due order (= reference fire order), raster, class
-//                 sums; the last block scans destinations, finishes the tick
-//  8. k_expand    copy each fire's pre-expanded (synapse, offset) events into
-//                 their delivery slots, order-preserving
+//  1. k_hist       count due events per target (and move far-future injects
+//                  that become reachable into the wheel)
+//  2. k_scan_tile  exclusive scan of the per-target counts (+ last block
+//                  scans the tile sums)
+//  3. k_scan_out   segment starts and the ascending list of touched targets
+//  4. k_scatter    group the due events by target (unordered inside a group)
+//  5. k_events     one warp per touched target: restore due order inside its
+//                  group, then per synapse (lanes in parallel) the event's
+//                  pre-spike STDP, pre-spike count and spike-code pattern
+//                  (SynapseDendriteProcessor.cpp:104-133, :318-365); writes
+//                  each event's input for the neuron walk
+//  6. k_process    one thread per touched target: the neuron's physics over
+//                  its events in due order (:175-229), redoing the STDP of
+//                  events that follow a fire of the target; the temporal
+//                  pattern once per tick (:294-316); fires into a due-position
+//                  bitmap
+//  7. k_post       post-spike STDP over the in-rows of targets that fired
+//                  (:138-173) + fire tile counts
+//  8. k_fire_list  fires in due order (= reference fire order), raster
+//  9. k_fire_count events per (fire block, delay class); the last block scans
+//                  destinations and finishes the tick
+// 10. k_expand     copy each fire's pre-expanded (synapse, offset) events into
+//                  their delivery slots, order-preserving
 //
 // Every wait is a kernel boundary or a "last block" hand-off (an atomic
 // counter, no spinning), so no kernel here can hang.
@@ -651,7 +658,8 @@ __global__ void k_scatter(Engine e) {
 // Restore due order inside every target's group (k_scatter leaves it in
 // arbitrary order; keys are unique due indices).  One warp per target:
 // groups of up to 32 events are bitonic-sorted in registers, longer ones are
-// placed by rank (number of smaller keys).  Output goes to grp_sorted.
+// placed by rank (number of smaller keys).  Output goes to grp_sorted.  Used
+// by the grouping entry point; the tick sorts inside k_events.
 __global__ void __launch_bounds__(kThreads) k_segsort(Engine e) {
     const uint32_t n_touched = e.ts->n_touched;
     const uint32_t n_due = e.ts->n_due;
@@ -697,17 +705,186 @@ __global__ void __launch_bounds__(kThreads) k_segsort(Engine e) {
     }
 }
 
-// The events of one target in due order, then the reference's sequential
-// per-event loop (NetworkPropagator.cpp:80-131) restricted to this target:
-// STDP state of the synapse (SynA) and the neuron's physics.  The synapse's
-// spike-code pattern and pre-spike count (SynB) depend on nothing the loop
-// computes and are updated by k_code.  The next event's SynA is loaded while
-// the current one is processed; a repeat of the same synapse takes the
-// just-updated record.
+// Pre-spike part of one synaptic event on its synapse record, in the
+// reference's order (SynapseDendriteProcessor.cpp:104-133): pre-spike STDP
+// against the last post spike, last_pre, the pre-spike count, and the
+// spike-code pattern (:318-365).  None of it depends on the target's neuron
+// state; only the STDP part depends on whether the target fired earlier in the
+// tick, which k_process handles by redoing it (replay_pre_stdp).
+__device__ __forceinline__ void pre_event(SynAB& r, const NeuronParam& p, uint32_t t, uint16_t* lc,
+                                          const Engine& e, int stdp, int temporal, bool inl) {
+    SynA& a = r.a;
+    const uint32_t delay = a.meta & kMetaDelayMask;
+    const uint32_t pre_tick = t >= delay ? t - delay : t;
+    if (((a.meta >> kMetaPlasticBit) & 1u) && a.last_post1 != 0) stdp_apply(a, pre_tick, a.last_post1 - 1, e, stdp);
+    a.last_pre1 = pre_tick + 1;
+    r.b.pre_count += 1;
+    code_update(r.b, p, t, lc, e.code_stride, temporal, inl);
+}
+
+__device__ __forceinline__ uint32_t ev_bits(const SynA& a) {
+    return ((a.meta >> kMetaCompShift) & 3u) | (((a.meta >> kMetaRecShift) & 3u) << 2);
+}
+
+// All events of synapse tm in one target's group, in due order: `first` is
+// the group position of the first, `more(q)` says whether position q > first
+// is another one.  Snapshots each event's SynA, applies pre_event and writes
+// the event's input record.
+template <typename More, typename DueOf>
+__device__ __forceinline__ void synapse_events(const Engine& e, const NeuronParam& p, uint32_t beg, uint32_t first,
+                                               uint32_t last, uint32_t tm, uint32_t t, int stdp, int temporal,
+                                               More more, DueOf due_of) {
+    uint16_t* lc = e.lcode + p.lcode_base + static_cast<size_t>(tm - p.in_begin) * p.max_refs * e.code_stride;
+    const bool inl = inline_code_pattern(p.max_refs, e.code_stride);
+    SynAB r = e.syn[tm];
+    for (uint32_t q = first; q <= last; ++q) {
+        if (q != first && !more(q)) continue;
+        e.ev_a0[beg + q] = r.a;
+        pre_event(r, p, t, lc, e, stdp, temporal, inl);
+        EvIn in;
+        in.weight = r.a.weight;
+        in.bits = ev_bits(r.a) | (q != first ? kEvRepeat : 0u);
+        in.tm = tm;
+        in.due = due_of[q];
+        e.evin[beg + q] = in;
+    }
+    e.syn[tm] = r;
+}
+
+// Due position of entry q of a group sorted in memory.
+struct SortedDue {
+    const unsigned long long* s;
+    __device__ uint32_t operator[](uint32_t q) const { return static_cast<uint32_t>(s[q]) & ~kExternalBit; }
+};
+
+// One warp per touched target.  Groups of up to 32 events are bitonic-sorted
+// into due order in registers and each synapse's events are found with one
+// match; longer groups are placed by rank into grp_sorted and scanned.  The
+// lane of a synapse's first event processes all of that synapse's events, so
+// repeats within the tick see each other in due order; different synapses
+// (and their random 64-byte records) proceed in parallel across lanes.
+__global__ void __launch_bounds__(kThreads) k_events(Engine e) {
+    __shared__ uint32_t s_due[kThreads];
+    const uint32_t t = e.ts->tick;
+    const uint32_t n_touched = e.ts->n_touched;
+    const uint32_t n_due = e.ts->n_due;
+    const int stdp = e.ts->stdp_enabled;
+    const int temporal = e.ts->temporal_enabled;
+    const int lane = threadIdx.x & 31;
+    uint32_t* wdue = s_due + (threadIdx.x & ~31u);
+    const uint32_t warps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t k = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); k < n_touched; k += warps) {
+        const uint32_t n = e.touched[k];
+        const uint32_t beg = e.seg_start[n];
+        const uint32_t end = k + 1 < n_touched ? e.seg_start[e.touched[k + 1]] : n_due;
+        const uint32_t len = end - beg;
+        const unsigned long long* src = e.grp + beg;
+        if (len <= 32) {
+            unsigned long long v = lane < static_cast<int>(len) ? src[lane] : ~0ull;
+            uint32_t key = lane < static_cast<int>(len) ? static_cast<uint32_t>(v) & ~kExternalBit : 0xFFFFFFFFu;
+#pragma unroll
+            for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+                for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                    const uint32_t ok = __shfl_xor_sync(0xffffffffu, key, stride);
+                    const unsigned long long ov = __shfl_xor_sync(0xffffffffu, v, stride);
+                    const bool up = ((lane & size) == 0);
+                    const bool lower = (lane & stride) == 0;
+                    const bool take_min = (lower == up);
+                    if (take_min ? (ok < key) : (ok > key)) {
+                        key = ok;
+                        v = ov;
+                    }
+                }
+            }
+            const bool valid = lane < static_cast<int>(len);
+            const bool syn = valid && !(static_cast<uint32_t>(v) & kExternalBit);
+            const uint32_t tm = static_cast<uint32_t>(v >> 32);
+            const uint32_t same = __match_any_sync(0xffffffffu, syn ? tm : 0xFFFFFFFFu);
+            wdue[lane] = key;
+            __syncwarp();
+            if (valid && !syn) {
+                EvIn in;
+                in.weight = __uint_as_float(tm);
+                in.bits = kEvExternal;
+                in.tm = 0;
+                in.due = key;
+                e.evin[beg + lane] = in;
+            }
+            if (syn && static_cast<int>(__ffs(same)) - 1 == lane) {
+                const NeuronParam p = e.nparam[n];
+                synapse_events(e, p, beg, lane, 31 - __clz(same), tm, t, stdp, temporal,
+                               [&](uint32_t q) { return ((same >> q) & 1u) != 0; }, static_cast<const uint32_t*>(wdue));
+            }
+            __syncwarp();
+        } else {
+            unsigned long long* srt = e.grp_sorted + beg;
+            for (uint32_t j = lane; j < len; j += 32) {
+                const unsigned long long v = src[j];
+                const uint32_t key = static_cast<uint32_t>(v) & ~kExternalBit;
+                uint32_t rank = 0;
+                for (uint32_t i = 0; i < len; ++i) rank += (static_cast<uint32_t>(src[i]) & ~kExternalBit) < key;
+                srt[rank] = v;
+            }
+            __syncwarp();
+            const NeuronParam p = e.nparam[n];
+            for (uint32_t j = lane; j < len; j += 32) {
+                const unsigned long long v = srt[j];
+                const uint32_t lo = static_cast<uint32_t>(v);
+                const uint32_t tm = static_cast<uint32_t>(v >> 32);
+                if (lo & kExternalBit) {
+                    EvIn in;
+                    in.weight = __uint_as_float(tm);
+                    in.bits = kEvExternal;
+                    in.tm = 0;
+                    in.due = lo & ~kExternalBit;
+                    e.evin[beg + j] = in;
+                    continue;
+                }
+                auto same_syn = [&](uint32_t q) {
+                    const unsigned long long y = srt[q];
+                    return !(static_cast<uint32_t>(y) & kExternalBit) && static_cast<uint32_t>(y >> 32) == tm;
+                };
+                bool first = true;
+                for (uint32_t q = 0; q < j && first; ++q) first = !same_syn(q);
+                if (!first) continue;
+                synapse_events(e, p, beg, j, len - 1, tm, t, stdp, temporal, same_syn, SortedDue{srt});
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// The synapse's state before event i of the walk, after the target's fires so
+// far: k_events' snapshot, unless an earlier event of the same synapse came
+// after the first fire (the walk has rewritten the record then).  Applies the
+// owed post-spike STDP and the event's pre-spike STDP, stores the record and
+// returns the weight.  Only events that follow a fire of their target get here.
+__device__ __noinline__ float replay_pre_stdp(const Engine& e, uint32_t beg, uint32_t i, uint32_t first_fire,
+                                              const EvIn& x, uint32_t t, uint32_t fires, int stdp) {
+    bool rewritten = false;
+    if (x.bits & kEvRepeat) {
+        for (uint32_t q = first_fire + 1; q < i && !rewritten; ++q) {
+            const EvIn y = e.evin[beg + q];
+            rewritten = !(y.bits & kEvExternal) && y.tm == x.tm;
+        }
+    }
+    SynA a = rewritten ? e.syn[x.tm].a : e.ev_a0[beg + i];
+    post_catch_up(a, t, fires, e, stdp);
+    const uint32_t delay = a.meta & kMetaDelayMask;
+    const uint32_t pre_tick = t >= delay ? t - delay : t;
+    if (((a.meta >> kMetaPlasticBit) & 1u) && a.last_post1 != 0) stdp_apply(a, pre_tick, a.last_post1 - 1, e, stdp);
+    a.last_pre1 = pre_tick + 1;
+    e.syn[x.tm].a = a;
+    return a.weight;
+}
+
+// The reference's sequential per-event loop (NetworkPropagator.cpp:80-131)
+// restricted to one target: its events' inputs in due order (from k_events),
+// the neuron's physics, and the temporal pattern once for the tick.
 template <bool kOne>
-__device__ __forceinline__ void process_target(const Engine& e, uint32_t n, const unsigned long long* g,
-                                               uint32_t len, uint32_t stride, uint32_t t, int stdp,
-                                               int temporal) {
+__device__ __forceinline__ void process_target(const Engine& e, uint32_t n, uint32_t beg, uint32_t len, uint32_t t,
+                                               int stdp, int temporal) {
     const NeuronParam p = e.nparam[n];
     const NeuronRec r = e.nrec[n];
     const NeuronTp q = e.ntp[n];
@@ -735,45 +912,19 @@ __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, cons
     if (kOne && s.ref_count > 0) s.one = e.refmeta[p.meta_base];
     s.snap_pending = false;
 
-    uint32_t fires = 0;
-    unsigned long long x = g[0];
-    SynA na{};
-    if (!(static_cast<uint32_t>(x) & kExternalBit)) na = e.syna[static_cast<uint32_t>(x >> 32)];
+    uint32_t fires = 0, first_fire = 0;
+    const EvIn* in = e.evin + beg;
+    EvIn nx = in[0];
     for (uint32_t i = 0; i < len; ++i) {
-        const unsigned long long cur = x;
-        SynA a = na;
-        const bool external = static_cast<uint32_t>(cur) & kExternalBit;
-        const uint32_t payload = static_cast<uint32_t>(cur >> 32);
-        bool same_next = false;
-        if (i + 1 < len) {  // prefetch the next event's synapse records
-            x = g[static_cast<size_t>(i + 1) * stride];
-            if (!(static_cast<uint32_t>(x) & kExternalBit)) {
-                const uint32_t tm = static_cast<uint32_t>(x >> 32);
-                same_next = !external && tm == payload;
-                if (!same_next) na = e.syna[tm];
-            }
-        }
-        const uint32_t due = static_cast<uint32_t>(cur) & ~kExternalBit;
-        bool fired;
-        if (external) {
-            fired = process_input(s, p, 0u, 0u, __uint_as_float(payload), t, e);
-        } else {
-            const uint32_t tm = payload;
-            post_catch_up(a, t, fires, e, stdp);
-            const uint32_t delay = a.meta & kMetaDelayMask;
-            const uint32_t pre_tick = t >= delay ? t - delay : t;
-            const bool plastic = (a.meta >> kMetaPlasticBit) & 1u;
-            if (plastic && a.last_post1 != 0) stdp_apply(a, pre_tick, a.last_post1 - 1, e, stdp);
-            a.last_pre1 = pre_tick + 1;
-            fired = process_input(s, p, (a.meta >> kMetaCompShift) & 3u, (a.meta >> kMetaRecShift) & 3u, a.weight,
-                                  t, e);
-            e.syna[tm] = a;
-            if (same_next) na = a;
-        }
-        if (fired) {
+        const EvIn x = nx;
+        if (i + 1 < len) nx = in[i + 1];
+        float w = x.weight;
+        if (fires > 0 && !(x.bits & kEvExternal)) w = replay_pre_stdp(e, beg, i, first_fire, x, t, fires, stdp);
+        if (process_input(s, p, x.bits & 3u, (x.bits >> 2) & 3u, w, t, e)) {
+            if (fires == 0) first_fire = i;
             fires += 1;
-            atomicOr(&e.fire_bits[due >> 5], 1u << (due & 31));
-            e.fire_at[due] = n;
+            atomicOr(&e.fire_bits[x.due >> 5], 1u << (x.due & 31));
+            e.fire_at[x.due] = n;
         }
     }
     temporal_tick<kOne>(s, p, t, e, temporal, len);
@@ -831,60 +982,22 @@ __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(
         const uint32_t n = e.touched[k];
         const uint32_t beg = e.seg_start[n];
         const uint32_t end = k + 1 < n_touched ? e.seg_start[e.touched[k + 1]] : n_due;
-        const unsigned long long* g = e.grp_sorted + beg;
         if (e.nparam[n].max_refs == 1) {
-            process_target<true>(e, n, g, end - beg, 1, t, stdp, temporal);
+            process_target<true>(e, n, beg, end - beg, t, stdp, temporal);
         } else {
-            process_target<false>(e, n, g, end - beg, 1, t, stdp, temporal);
+            process_target<false>(e, n, beg, end - beg, t, stdp, temporal);
         }
     }
 }
 
-// Spike-code pattern and pre-spike count of every synaptic event
-// (SynapseDendriteProcessor.cpp:126, :133, :318-365), one thread per event.
-// These read and write only the synapse's own SynB record and the target's
-// parameters, so events run in parallel; several events of the same synapse
-// within the tick are applied in due order by the thread of the first one.
-__global__ void __launch_bounds__(kThreads) k_code(Engine e) {
-    const uint32_t t = e.ts->tick;
-    const uint32_t n_due = e.ts->n_due;
-    const int temporal = e.ts->temporal_enabled;
-    for (uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x; pos < n_due; pos += gridDim.x * blockDim.x) {
-        const unsigned long long x = e.grp_sorted[pos];
-        if (static_cast<uint32_t>(x) & kExternalBit) continue;
-        const uint32_t tm = static_cast<uint32_t>(x >> 32);
-        const uint32_t n = e.evt_tgt[pos];
-        const uint32_t beg = e.seg_start[n];
-        const uint32_t end = beg + e.seg_len[n];
-        bool first = true;
-        for (uint32_t q = beg; q < pos && first; ++q) {
-            const unsigned long long y = e.grp_sorted[q];
-            first = !(!(static_cast<uint32_t>(y) & kExternalBit) && static_cast<uint32_t>(y >> 32) == tm);
-        }
-        if (!first) continue;
-        const NeuronParam p = e.nparam[n];
-        uint16_t* lc = e.lcode + p.lcode_base + static_cast<size_t>(tm - p.in_begin) * p.max_refs * e.code_stride;
-        const bool inl = inline_code_pattern(p.max_refs, e.code_stride);
-        SynB b = e.synb[tm];
-        b.pre_count += 1;
-        code_update(b, p, t, lc, e.code_stride, temporal, inl);
-        for (uint32_t q = pos + 1; q < end; ++q) {
-            const unsigned long long y = e.grp_sorted[q];
-            if (!(static_cast<uint32_t>(y) & kExternalBit) && static_cast<uint32_t>(y >> 32) == tm) {
-                b.pre_count += 1;
-                code_update(b, p, t, lc, e.code_stride, temporal, inl);
-            }
-        }
-        e.synb[tm] = b;
-    }
-}
-
-__global__ void k_init_synb(const SynA* syna, SynB* synb, unsigned long long S) {
+__global__ void k_init_syn(SynAB* syn, const SynA* a, unsigned long long S) {
     for (unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; i < S;
          i += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
-        SynB b{};
-        b.flags = static_cast<uint8_t>(((syna[i].meta >> kMetaExpectedShift) & 15u) << 4);
-        synb[i] = b;
+        SynAB r;
+        r.a = a[i];
+        r.b = SynB{};
+        r.b.flags = static_cast<uint8_t>(((r.a.meta >> kMetaExpectedShift) & 15u) << 4);
+        syn[i] = r;
     }
 }
 
@@ -905,8 +1018,8 @@ __global__ void k_post(Engine e) {
         }
         const unsigned long long b = e.in_ptr[n], en = e.in_ptr[n + 1];
         for (unsigned long long tm = b + threadIdx.x; tm < en; tm += blockDim.x) {
-            SynA a = e.syna[tm];
-            if (post_catch_up(a, t, fires, e, stdp)) e.syna[tm] = a;
+            SynA a = e.syn[tm].a;
+            if (post_catch_up(a, t, fires, e, stdp)) e.syn[tm].a = a;
         }
     }
     // fire bitmap tile popcounts (one thread per bitmap word)
@@ -1095,9 +1208,8 @@ void launch_tick(const Engine& e, cudaStream_t stream, cudaEvent_t* marks) {
     mark(false); k_scan_tile<<<scan_grid, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_scan_out<<<scan_grid, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_scatter<<<wide, kThreads, 0, stream>>>(e); mark(true);
-    mark(false); k_segsort<<<e.grid_wide * 4, kThreads, 0, stream>>>(e); mark(true);
+    mark(false); k_events<<<e.grid_wide * 4, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_process<<<e.grid_process, kThreads, 0, stream>>>(e); mark(true);
-    mark(false); k_code<<<e.grid_wide * 4, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_post<<<wide, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_fire_list<<<e.grid_fire, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_fire_count<<<e.grid_wide, kThreads, 0, stream>>>(e); mark(true);
@@ -1105,9 +1217,9 @@ void launch_tick(const Engine& e, cudaStream_t stream, cudaEvent_t* marks) {
 }
 
 const char* kernel_name(int index) {
-    static const char* names[kKernelCount] = {"k_hist",   "k_scan_tile", "k_scan_out",  "k_scatter",
-                                              "k_segsort", "k_process",  "k_code",      "k_post",
-                                              "k_fire_list", "k_fire_count", "k_expand"};
+    static const char* names[kKernelCount] = {"k_hist",    "k_scan_tile", "k_scan_out",   "k_scatter",
+                                              "k_events",  "k_process",   "k_post",       "k_fire_list",
+                                              "k_fire_count", "k_expand"};
     return index >= 0 && index < kKernelCount ? names[index] : "";
 }
 
@@ -1121,9 +1233,9 @@ void launch_group(const Engine& e, cudaStream_t stream) {
     k_segsort<<<e.grid_wide * 4, kThreads, 0, stream>>>(e);
 }
 
-void launch_init_synb(const Engine& e, cudaStream_t stream) {
+void launch_init_syn(const Engine& e, const SynA* a, cudaStream_t stream) {
     if (e.S == 0) return;
-    k_init_synb<<<1024, kThreads, 0, stream>>>(e.syna, e.synb, e.S);
+    k_init_syn<<<1024, kThreads, 0, stream>>>(e.syn, a, e.S);
 }
 
 void launch_inject(const Engine& e, const unsigned long long* ev, const uint32_t* slot_of_group,

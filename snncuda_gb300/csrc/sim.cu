@@ -491,8 +491,7 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.cand = dalloc<unsigned long long>(own, cand_total);
     e.refmeta = dalloc<RefMeta>(own, meta_total);
     e.ring = dalloc<unsigned long long>(own, ring_total);
-    e.syna = dalloc<SynA>(own, S);
-    e.synb = dalloc<SynB>(own, S);
+    e.syn = dalloc<SynAB>(own, S);
     e.lcode = dalloc<uint16_t>(own, lcode_total);
     auto* d_pre_base = dalloc<unsigned long long>(own, N);
     auto* d_pre_off = dalloc<uint32_t>(own, static_cast<size_t>(N) * (D + 1));
@@ -508,8 +507,8 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.touched = dalloc<uint32_t>(own, N);
     e.grp = dalloc<unsigned long long>(own, slot_cap);
     e.grp_sorted = dalloc<unsigned long long>(own, slot_cap);
-    e.evt_tgt = dalloc<uint32_t>(own, slot_cap);
-    e.seg_len = dalloc<uint32_t>(own, N);
+    e.evin = dalloc<EvIn>(own, slot_cap);
+    e.ev_a0 = dalloc<SynA>(own, slot_cap);
     e.fire_bits = dalloc<uint32_t>(own, bit_words);
     e.fire_at = dalloc<uint32_t>(own, slot_cap);
     e.fire_tile = dalloc<uint32_t>(own, fire_tiles + 2);
@@ -537,7 +536,15 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     // NeuronState defaults (NeuronStateCache.h:15-45): every compartment tau 5 (code 0).
     zero(e.nrec, sizeof(NeuronRec) * N);
     zero(e.ntp, sizeof(NeuronTp) * N);
-    h2d(e.syna, syna.data(), syna.size() * sizeof(SynA));
+    // SynA images go through a temporary buffer into the 64-byte records
+    struct Upload {
+        std::vector<void*> v;
+        ~Upload() {
+            for (void* q : v) cudaFree(q);
+        }
+    } upload;
+    SynA* d_syna_img = dalloc<SynA>(upload.v, S);
+    h2d(d_syna_img, syna.data(), syna.size() * sizeof(SynA));
     zero(e.lcode, sizeof(uint16_t) * lcode_total);
     h2d(d_pre_base, pre_base.data(), pre_base.size() * sizeof(unsigned long long));
     h2d(d_pre_off, pre_off.data(), pre_off.size() * sizeof(uint32_t));
@@ -567,7 +574,7 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.tab.ltp = d_ltp;
     e.tab.ltd = d_ltd;
     e.tab.stdp_len = static_cast<uint32_t>(ltp.size());
-    launch_init_synb(e, st);
+    launch_init_syn(e, d_syna_img, st);
     check(cudaGetLastError(), "init launch");
     sim->in_ptr = std::move(in_ptr);
 
@@ -739,8 +746,7 @@ struct HostState {
     std::vector<NeuronTp> ntp;
     std::vector<unsigned long long> cand, ring;
     std::vector<RefMeta> meta;
-    std::vector<SynA> syna;
-    std::vector<SynB> synb;
+    std::vector<SynAB> syn;
     std::vector<uint16_t> lcode;
 };
 
@@ -763,12 +769,12 @@ void synapse_learned(const snncuda_sim* sim, const HostState& h, uint64_t tm, ui
     const NeuronParam& p = sim->nparam[n];
     if (inline_code_pattern(p.max_refs, sim->e.code_stride)) {
         out.clear();
-        for (uint32_t j = 0; j < expected_of(h.syna[tm]); ++j) out.push_back(ring_get(h.synb[tm].ring_hi, 0, j));
+        for (uint32_t j = 0; j < expected_of(h.syn[tm].a); ++j) out.push_back(ring_get(h.syn[tm].b.ring_hi, 0, j));
         return;
     }
     const uint16_t* lc = h.lcode.data() + p.lcode_base + (tm - p.in_begin) * p.max_refs * sim->e.code_stride +
                          static_cast<size_t>(which) * sim->e.code_stride;
-    out.assign(lc, lc + expected_of(h.syna[tm]));
+    out.assign(lc, lc + expected_of(h.syn[tm].a));
 }
 
 HostState fetch_all(snncuda_sim* sim, bool temporal) {
@@ -776,8 +782,7 @@ HostState fetch_all(snncuda_sim* sim, bool temporal) {
     Engine& e = sim->e;
     h.nrec = sim->d2h(e.nrec, sim->N);
     h.ntp = sim->d2h(e.ntp, sim->N);
-    h.syna = sim->d2h(e.syna, sim->S);
-    h.synb = sim->d2h(e.synb, sim->S);
+    h.syn = sim->d2h(e.syn, sim->S);
     if (temporal) {
         uint64_t cand = 0, ring = 0, meta = 0, lcode = 0;
         for (uint32_t n = 0; n < sim->N; ++n) {
@@ -961,21 +966,22 @@ int snncuda_sim_read_neurons(snncuda_sim* sim, const snncuda_neuron_state* o) {
 int snncuda_sim_read_synapses(snncuda_sim* sim, const snncuda_synapse_state* o) {
     if (sim == nullptr || o == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
     return guarded([&] {
-        const std::vector<SynA> a = sim->d2h(sim->e.syna, sim->S);
-        const std::vector<SynB> b = sim->d2h(sim->e.synb, sim->S);
+        const std::vector<SynAB> rec = sim->d2h(sim->e.syn, sim->S);
         for (uint64_t tm = 0; tm < sim->S; ++tm) {
             const uint64_t i = sim->c_of_tm[tm];
-            if (o->weight) o->weight[i] = a[tm].weight;
-            if (o->last_pre_spike_tick) o->last_pre_spike_tick[i] = a[tm].last_pre1 ? static_cast<int64_t>(a[tm].last_pre1) - 1 : -1;
-            if (o->last_post_spike_tick) o->last_post_spike_tick[i] = a[tm].last_post1 ? static_cast<int64_t>(a[tm].last_post1) - 1 : -1;
-            if (o->pre_spike_count) o->pre_spike_count[i] = b[tm].pre_count;
-            if (o->plasticity_update_count) o->plasticity_update_count[i] = a[tm].updates;
-            if (o->last_weight_delta) o->last_weight_delta[i] = a[tm].last_delta;
-            if (o->code_window_start_tick) o->code_window_start_tick[i] = b[tm].code_ws;
-            if (o->code_offset_count) o->code_offset_count[i] = b[tm].code_len;
-            if (o->learned_code_count) o->learned_code_count[i] = b[tm].learned_count;
-            if (o->code_match_count) o->code_match_count[i] = b[tm].code_matches;
-            if (o->last_code_match) o->last_code_match[i] = b[tm].flags & 1u;
+            const SynA& a = rec[tm].a;
+            const SynB& b = rec[tm].b;
+            if (o->weight) o->weight[i] = a.weight;
+            if (o->last_pre_spike_tick) o->last_pre_spike_tick[i] = a.last_pre1 ? static_cast<int64_t>(a.last_pre1) - 1 : -1;
+            if (o->last_post_spike_tick) o->last_post_spike_tick[i] = a.last_post1 ? static_cast<int64_t>(a.last_post1) - 1 : -1;
+            if (o->pre_spike_count) o->pre_spike_count[i] = b.pre_count;
+            if (o->plasticity_update_count) o->plasticity_update_count[i] = a.updates;
+            if (o->last_weight_delta) o->last_weight_delta[i] = a.last_delta;
+            if (o->code_window_start_tick) o->code_window_start_tick[i] = b.code_ws;
+            if (o->code_offset_count) o->code_offset_count[i] = b.code_len;
+            if (o->learned_code_count) o->learned_code_count[i] = b.learned_count;
+            if (o->code_match_count) o->code_match_count[i] = b.code_matches;
+            if (o->last_code_match) o->last_code_match[i] = b.flags & 1u;
         }
     });
 }
@@ -1003,8 +1009,9 @@ int snncuda_sim_read_pattern(snncuda_sim* sim, int32_t kind, uint64_t index, uin
         } else if (kind == 2 || kind == 3) {
             if (index >= sim->S) throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "synapse out of range");
             const uint64_t tm = sim->tm_of_c[index];
-            const SynA a = sim->d2h(sim->e.syna + tm, 1)[0];
-            const SynB b = sim->d2h(sim->e.synb + tm, 1)[0];
+            const SynAB rec = sim->d2h(sim->e.syn + tm, 1)[0];
+            const SynA& a = rec.a;
+            const SynB& b = rec.b;
             if (kind == 2) {
                 for (uint32_t j = 0; j < b.code_len; ++j) v.push_back(ring_get(b.ring_lo, b.ring_hi, j));  // code_len <= 4 when inline
             } else {
@@ -1068,8 +1075,8 @@ int snncuda_sim_state_digest(snncuda_sim* sim, uint64_t* neuron_digest, uint64_t
             Digest d;
             for (uint64_t c = 0; c < sim->S; ++c) {
                 const uint64_t tm = tm_of_c[c];
-                const SynA& a = h.syna[tm];
-                const SynB& b = h.synb[tm];
+                const SynA& a = h.syn[tm].a;
+                const SynB& b = h.syn[tm].b;
                 d.f32(a.weight);
                 d.word(a.last_pre1 ? static_cast<uint64_t>(a.last_pre1 - 1) : ~0ULL);
                 d.word(a.last_post1 ? static_cast<uint64_t>(a.last_post1 - 1) : ~0ULL);
