@@ -31,6 +31,7 @@ constexpr uint32_t kStatusPostCountOverflow = 1u << 3;
 constexpr uint32_t kStatusRunOverflow = 1u << 4;
 constexpr uint32_t kStatusFireOverflow = 1u << 5;
 constexpr uint32_t kStatusBadEvent = 1u << 6;       // event target out of range (grouping input)
+constexpr uint32_t kStatusStageTimeout = 1u << 7;   // a bounded wait for a bulk copy ran out
 
 // SynA.meta bit fields.
 constexpr uint32_t kMetaDelayMask = 0xFFFFu;
@@ -217,6 +218,7 @@ struct Engine {
     uint32_t* tile_sum;                    // scan partials
     uint32_t* tile_nz;
     uint32_t* touched;                     // [N] target ids with due events, ascending
+    uint32_t* tbeg;                        // [N] group start of the k-th touched target (tick only)
     unsigned long long* grp;               // [slot_cap] (payload << 32) | (due index | ext << 31)
     unsigned long long* grp_sorted;        // grouping entry point only: grp with every group in due order
     uint32_t* evt_tgt;                     // grouping entry point only: target of each grp_sorted entry
@@ -262,6 +264,9 @@ void launch_inject(const Engine& e, const unsigned long long* ev, const uint32_t
 // Groups the W == 1 "wheel" of e (a caller's event buffer) by target: the
 // hist / scan / scatter / segment-sort kernels of a tick.
 void launch_group(const Engine& e, cudaStream_t stream);
+// One-time kernel attributes (dynamic shared memory of k_process); call with
+// the device current before the first tick.
+void configure_kernels();
 // Builds the synapse records from SynA images (`a`, S entries): code-pattern
 // state zeroed, each synapse's `expected` stored.
 void launch_init_syn(const Engine& e, const SynA* a, cudaStream_t stream);

@@ -42,16 +42,70 @@ namespace snngb {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr uint32_t kStageEvents = 4096;  // event inputs k_process stages per block (64 KB)
 
-// Minimum resident blocks per SM requested for k_process (register budget).
+// Minimum resident blocks per SM requested for k_process and k_events
+// (register budget).
 #ifndef SNNGB_PROCESS_MIN_BLOCKS
-#define SNNGB_PROCESS_MIN_BLOCKS 2
+#define SNNGB_PROCESS_MIN_BLOCKS 3
+#endif
+#ifndef SNNGB_EVENTS_MIN_BLOCKS
+#define SNNGB_EVENTS_MIN_BLOCKS 4
 #endif
 
 __device__ __forceinline__ float rec_gain(uint32_t r) { return r == 1 ? 0.55f : (r == 3 ? 0.65f : 1.0f); }
 __device__ __forceinline__ float rec_sign(uint32_t r) { return r >= 2 ? -1.0f : 1.0f; }
 
 __device__ __forceinline__ void raise_status(const Engine& e, uint32_t bit) { atomicOr(&e.ts->status, bit); }
+
+// ---------------------------------------------------------------------------
+// bulk copies into shared memory (TMA, cp.async.bulk) with an mbarrier
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t arrivals) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(arrivals) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// One thread: expect `bytes` on the barrier and copy them from global memory
+// (16-byte aligned, a multiple of 16 bytes) into shared memory.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, unsigned long long* bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long v;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(v));
+    return v;
+}
+
+// Waits for phase `parity` of the barrier to complete, for at most about
+// 100 ms; returns false if it did not.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity) {
+    const uint32_t a = smem_addr(bar);
+    const unsigned long long t0 = global_ns();
+    for (uint32_t it = 0; it < (1u << 24); ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if ((it & 255u) == 255u && global_ns() - t0 > 100000000ull) break;
+    }
+    return false;
+}
 
 // ---------------------------------------------------------------------------
 // block-level helpers
@@ -237,7 +291,7 @@ __device__ void temporal_tick(NState& s, const NeuronParam& p, uint32_t t, const
         }
     }
     const uint32_t o = t - s.ws;
-    const unsigned long long oo = static_cast<unsigned long long>(o) * o;
+    const uint32_t oo = o * o;  // o < 2^16, so o * o fits 32 bits
     for (uint32_t j = 0; j < k; ++j) {
         if (s.len >= 1 && s.ref_count > 0 && s.nruns > 0 && run_value(s.last_run) == o) {
             bool frozen = true;
@@ -257,7 +311,7 @@ __device__ void temporal_tick(NState& s, const NeuronParam& p, uint32_t t, const
                 const uint32_t n = k - j;
                 s.last_run += static_cast<unsigned long long>(n) << 16;
                 s.len += n;
-                s.cn += oo * n;
+                s.cn += static_cast<unsigned long long>(oo) * n;
                 s.match_count += n;
                 s.flags |= (1u << 8);
                 return;
@@ -286,8 +340,8 @@ __device__ void temporal_tick(NState& s, const NeuronParam& p, uint32_t t, const
                     m.cur_run += 1;
                     m.cur_pos = 0;
                 }
-                m.dot += v * o;
-                m.rn += v * v;
+                m.dot += static_cast<uint32_t>(v) * o;  // 16-bit values: 32-bit products
+                m.rn += static_cast<uint32_t>(v) * static_cast<uint32_t>(v);
                 m.cn += oo;
                 m.match = 2;
             }
@@ -495,8 +549,8 @@ __device__ void code_update(SynB& b, const NeuronParam& p, uint32_t t, uint16_t*
     bool match = 0.0f >= p.similarity;
     unsigned long long cn = 0;
     for (uint32_t j = 0; j < expected; ++j) {
-        const unsigned long long v = ring_get(b.ring_lo, inline_pattern ? 0ull : b.ring_hi, j);
-        cn += v * v;
+        const uint32_t v = ring_get(b.ring_lo, inline_pattern ? 0ull : b.ring_hi, j);
+        cn += v * v;  // 16-bit offsets: 32-bit products, 64-bit sums
     }
     for (uint32_t i = 0; i < b.learned_count && !match; ++i) {
         unsigned long long plo, phi = 0;
@@ -507,7 +561,7 @@ __device__ void code_update(SynB& b, const NeuronParam& p, uint32_t t, uint16_t*
         }
         unsigned long long dot = 0, rn = 0;
         for (uint32_t j = 0; j < expected; ++j) {
-            const unsigned long long pv = ring_get(plo, phi, j);
+            const uint32_t pv = ring_get(plo, phi, j);
             dot += pv * ring_get(b.ring_lo, inline_pattern ? 0ull : b.ring_hi, j);
             rn += pv * pv;
         }
@@ -631,7 +685,10 @@ __global__ void k_scan_out(Engine e) {
             const uint32_t i = base + j;
             if (i < e.N) {
                 e.seg_start[i] = seg;  // also for targets without events (empty segment)
-                if (c[j] != 0) e.touched[pos++] = i;
+                if (c[j] != 0) {
+                    if (e.tbeg) e.tbeg[pos] = seg;
+                    e.touched[pos++] = i;
+                }
             }
             seg += c[j];
         }
@@ -757,101 +814,122 @@ struct SortedDue {
     __device__ uint32_t operator[](uint32_t q) const { return static_cast<uint32_t>(s[q]) & ~kExternalBit; }
 };
 
-// One warp per touched target.  Groups of up to 32 events are bitonic-sorted
-// into due order in registers and each synapse's events are found with one
-// match; longer groups are placed by rank into grp_sorted and scanned.  The
-// lane of a synapse's first event processes all of that synapse's events, so
-// repeats within the tick see each other in due order; different synapses
-// (and their random 64-byte records) proceed in parallel across lanes.
-__global__ void __launch_bounds__(kThreads) k_events(Engine e) {
-    __shared__ uint32_t s_due[kThreads];
+// One target's group in k_events.  Groups of up to 32 events stay in lanes:
+// each event's position in due order is its rank among the group's due
+// indices, and the events of each synapse are found with one match; the
+// synapse's earliest event's lane then processes all of them in due order.
+// Longer groups are placed by rank into grp_sorted and scanned.
+__device__ __forceinline__ void events_of_target(const Engine& e, uint32_t n, uint32_t beg, uint32_t len, uint32_t t,
+                                                 int stdp, int temporal, uint32_t* wdue, uint32_t* wrank) {
+    const uint32_t lane = threadIdx.x & 31;
+    if (len <= 32) {
+        const bool valid = lane < len;
+        const unsigned long long v = valid ? e.grp[beg + lane] : 0ull;
+        const uint32_t lo = static_cast<uint32_t>(v);
+        const uint32_t key = lo & ~kExternalBit;
+        uint32_t rank = 0;
+        for (uint32_t i = 0; i < len; ++i) rank += __shfl_sync(0xffffffffu, key, i) < key;
+        const bool syn = valid && !(lo & kExternalBit);
+        const uint32_t tm = static_cast<uint32_t>(v >> 32);
+        const uint32_t same = __match_any_sync(0xffffffffu, syn ? tm : 0xFFFFFFFFu);
+        wdue[lane] = key;
+        wrank[lane] = rank;
+        __syncwarp();
+        if (valid && !syn) {
+            EvIn in;
+            in.weight = __uint_as_float(tm);
+            in.bits = kEvExternal;
+            in.tm = 0;
+            in.due = key;
+            e.evin[beg + rank] = in;
+        }
+        bool leader = syn;
+        if (syn && same != (1u << lane)) {
+            for (uint32_t m = same; m; m &= m - 1) leader = leader && wrank[__ffs(m) - 1] >= rank;
+        }
+        if (leader) {
+            const NeuronParam p = e.nparam[n];
+            uint16_t* lc = e.lcode + p.lcode_base + static_cast<size_t>(tm - p.in_begin) * p.max_refs * e.code_stride;
+            const bool inl = inline_code_pattern(p.max_refs, e.code_stride);
+            SynAB r = e.syn[tm];
+            uint32_t rest = same, repeat = 0;
+            while (rest) {  // the synapse's events in due order (rank order)
+                uint32_t j = __ffs(rest) - 1, best = wrank[j];
+                for (uint32_t m = rest & (rest - 1); m; m &= m - 1) {
+                    const uint32_t c = __ffs(m) - 1;
+                    if (wrank[c] < best) {
+                        best = wrank[c];
+                        j = c;
+                    }
+                }
+                rest &= ~(1u << j);
+                e.ev_a0[beg + best] = r.a;
+                pre_event(r, p, t, lc, e, stdp, temporal, inl);
+                EvIn in;
+                in.weight = r.a.weight;
+                in.bits = ev_bits(r.a) | repeat;
+                in.tm = tm;
+                in.due = wdue[j];
+                e.evin[beg + best] = in;
+                repeat = kEvRepeat;
+            }
+            e.syn[tm] = r;
+        }
+        __syncwarp();
+        return;
+    }
+    const unsigned long long* src = e.grp + beg;
+    unsigned long long* srt = e.grp_sorted + beg;
+    for (uint32_t j = lane; j < len; j += 32) {
+        const unsigned long long x = src[j];
+        const uint32_t key = static_cast<uint32_t>(x) & ~kExternalBit;
+        uint32_t rank = 0;
+        for (uint32_t i = 0; i < len; ++i) rank += (static_cast<uint32_t>(src[i]) & ~kExternalBit) < key;
+        srt[rank] = x;
+    }
+    __syncwarp();
+    const NeuronParam p = e.nparam[n];
+    for (uint32_t j = lane; j < len; j += 32) {
+        const unsigned long long x = srt[j];
+        const uint32_t lo = static_cast<uint32_t>(x);
+        const uint32_t tm = static_cast<uint32_t>(x >> 32);
+        if (lo & kExternalBit) {
+            EvIn in;
+            in.weight = __uint_as_float(tm);
+            in.bits = kEvExternal;
+            in.tm = 0;
+            in.due = lo & ~kExternalBit;
+            e.evin[beg + j] = in;
+            continue;
+        }
+        auto same_syn = [&](uint32_t q) {
+            const unsigned long long y = srt[q];
+            return !(static_cast<uint32_t>(y) & kExternalBit) && static_cast<uint32_t>(y >> 32) == tm;
+        };
+        bool first = true;
+        for (uint32_t q = 0; q < j && first; ++q) first = !same_syn(q);
+        if (!first) continue;
+        synapse_events(e, p, beg, j, len - 1, tm, t, stdp, temporal, same_syn, SortedDue{srt});
+    }
+    __syncwarp();
+}
+
+// One warp per touched target (events_of_target): the synapses of a target
+// proceed in parallel across lanes, each a random 64-byte record.
+__global__ void __launch_bounds__(kThreads, SNNGB_EVENTS_MIN_BLOCKS) k_events(Engine e) {
+    __shared__ uint32_t s_due[kThreads], s_rank[kThreads];
     const uint32_t t = e.ts->tick;
     const uint32_t n_touched = e.ts->n_touched;
     const uint32_t n_due = e.ts->n_due;
     const int stdp = e.ts->stdp_enabled;
     const int temporal = e.ts->temporal_enabled;
-    const int lane = threadIdx.x & 31;
-    uint32_t* wdue = s_due + (threadIdx.x & ~31u);
+    const uint32_t wbase = threadIdx.x & ~31u;
     const uint32_t warps = gridDim.x * (blockDim.x / 32);
     for (uint32_t k = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); k < n_touched; k += warps) {
         const uint32_t n = e.touched[k];
-        const uint32_t beg = e.seg_start[n];
-        const uint32_t end = k + 1 < n_touched ? e.seg_start[e.touched[k + 1]] : n_due;
-        const uint32_t len = end - beg;
-        const unsigned long long* src = e.grp + beg;
-        if (len <= 32) {
-            unsigned long long v = lane < static_cast<int>(len) ? src[lane] : ~0ull;
-            uint32_t key = lane < static_cast<int>(len) ? static_cast<uint32_t>(v) & ~kExternalBit : 0xFFFFFFFFu;
-#pragma unroll
-            for (int size = 2; size <= 32; size <<= 1) {
-#pragma unroll
-                for (int stride = size >> 1; stride > 0; stride >>= 1) {
-                    const uint32_t ok = __shfl_xor_sync(0xffffffffu, key, stride);
-                    const unsigned long long ov = __shfl_xor_sync(0xffffffffu, v, stride);
-                    const bool up = ((lane & size) == 0);
-                    const bool lower = (lane & stride) == 0;
-                    const bool take_min = (lower == up);
-                    if (take_min ? (ok < key) : (ok > key)) {
-                        key = ok;
-                        v = ov;
-                    }
-                }
-            }
-            const bool valid = lane < static_cast<int>(len);
-            const bool syn = valid && !(static_cast<uint32_t>(v) & kExternalBit);
-            const uint32_t tm = static_cast<uint32_t>(v >> 32);
-            const uint32_t same = __match_any_sync(0xffffffffu, syn ? tm : 0xFFFFFFFFu);
-            wdue[lane] = key;
-            __syncwarp();
-            if (valid && !syn) {
-                EvIn in;
-                in.weight = __uint_as_float(tm);
-                in.bits = kEvExternal;
-                in.tm = 0;
-                in.due = key;
-                e.evin[beg + lane] = in;
-            }
-            if (syn && static_cast<int>(__ffs(same)) - 1 == lane) {
-                const NeuronParam p = e.nparam[n];
-                synapse_events(e, p, beg, lane, 31 - __clz(same), tm, t, stdp, temporal,
-                               [&](uint32_t q) { return ((same >> q) & 1u) != 0; }, static_cast<const uint32_t*>(wdue));
-            }
-            __syncwarp();
-        } else {
-            unsigned long long* srt = e.grp_sorted + beg;
-            for (uint32_t j = lane; j < len; j += 32) {
-                const unsigned long long v = src[j];
-                const uint32_t key = static_cast<uint32_t>(v) & ~kExternalBit;
-                uint32_t rank = 0;
-                for (uint32_t i = 0; i < len; ++i) rank += (static_cast<uint32_t>(src[i]) & ~kExternalBit) < key;
-                srt[rank] = v;
-            }
-            __syncwarp();
-            const NeuronParam p = e.nparam[n];
-            for (uint32_t j = lane; j < len; j += 32) {
-                const unsigned long long v = srt[j];
-                const uint32_t lo = static_cast<uint32_t>(v);
-                const uint32_t tm = static_cast<uint32_t>(v >> 32);
-                if (lo & kExternalBit) {
-                    EvIn in;
-                    in.weight = __uint_as_float(tm);
-                    in.bits = kEvExternal;
-                    in.tm = 0;
-                    in.due = lo & ~kExternalBit;
-                    e.evin[beg + j] = in;
-                    continue;
-                }
-                auto same_syn = [&](uint32_t q) {
-                    const unsigned long long y = srt[q];
-                    return !(static_cast<uint32_t>(y) & kExternalBit) && static_cast<uint32_t>(y >> 32) == tm;
-                };
-                bool first = true;
-                for (uint32_t q = 0; q < j && first; ++q) first = !same_syn(q);
-                if (!first) continue;
-                synapse_events(e, p, beg, j, len - 1, tm, t, stdp, temporal, same_syn, SortedDue{srt});
-            }
-            __syncwarp();
-        }
+        const uint32_t beg = e.tbeg[k];
+        const uint32_t end = k + 1 < n_touched ? e.tbeg[k + 1] : n_due;
+        events_of_target(e, n, beg, end - beg, t, stdp, temporal, s_due + wbase, s_rank + wbase);
     }
 }
 
@@ -882,9 +960,16 @@ __device__ __noinline__ float replay_pre_stdp(const Engine& e, uint32_t beg, uin
 // The reference's sequential per-event loop (NetworkPropagator.cpp:80-131)
 // restricted to one target: its events' inputs in due order (from k_events),
 // the neuron's physics, and the temporal pattern once for the tick.
-template <bool kOne>
+// The block's event inputs: entries [lo, lo + cnt) of evin staged in shared
+// memory once `ready()` returns true; the rest read from global memory.
+struct Staged {
+    const EvIn* s;
+    uint32_t lo, cnt;
+};
+
+template <bool kOne, typename Ready>
 __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, uint32_t beg, uint32_t len, uint32_t t,
-                                               int stdp, int temporal) {
+                                               int stdp, int temporal, Staged st, Ready ready) {
     const NeuronParam p = e.nparam[n];
     const NeuronRec r = e.nrec[n];
     const NeuronTp q = e.ntp[n];
@@ -913,11 +998,10 @@ __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, uint
     s.snap_pending = false;
 
     uint32_t fires = 0, first_fire = 0;
-    const EvIn* in = e.evin + beg;
-    EvIn nx = in[0];
+    if (!ready()) st.cnt = 0;
     for (uint32_t i = 0; i < len; ++i) {
-        const EvIn x = nx;
-        if (i + 1 < len) nx = in[i + 1];
+        const uint32_t o = beg + i - st.lo;
+        const EvIn x = o < st.cnt ? st.s[o] : e.evin[beg + i];
         float w = x.weight;
         if (fires > 0 && !(x.bits & kEvExternal)) w = replay_pre_stdp(e, beg, i, first_fire, x, t, fires, stdp);
         if (process_input(s, p, x.bits & 3u, (x.bits >> 2) & 3u, w, t, e)) {
@@ -972,21 +1056,66 @@ __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, uint
 // or writes belongs to its target (the target's neuron state and the
 // target's incoming synapses); post-spike STDP of a fire is applied lazily
 // to synapses touched later in the tick and in bulk by k_post for the rest.
+// A block's targets are consecutive touched targets, so their event inputs
+// are one contiguous range: one thread copies it into shared memory with a
+// bulk copy while every thread loads its neuron's records.
 __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(Engine e) {
+    extern __shared__ __align__(128) EvIn s_ev[];  // kStageEvents entries
+    __shared__ __align__(8) unsigned long long s_bar;
+    __shared__ uint32_t s_lo, s_cnt;
     const uint32_t t = e.ts->tick;
     const uint32_t n_touched = e.ts->n_touched;
     const uint32_t n_due = e.ts->n_due;
     const int stdp = e.ts->stdp_enabled;
     const int temporal = e.ts->temporal_enabled;
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n_touched; k += gridDim.x * blockDim.x) {
-        const uint32_t n = e.touched[k];
-        const uint32_t beg = e.seg_start[n];
-        const uint32_t end = k + 1 < n_touched ? e.seg_start[e.touched[k + 1]] : n_due;
-        if (e.nparam[n].max_refs == 1) {
-            process_target<true>(e, n, beg, end - beg, t, stdp, temporal);
-        } else {
-            process_target<false>(e, n, beg, end - beg, t, stdp, temporal);
+    if (threadIdx.x == 0) mbar_init(&s_bar, 1);
+    __syncthreads();
+    uint32_t parity = 0;
+    bool staging = true;  // false after a copy outlived its wait: shared memory is no longer used
+    for (uint32_t k0 = blockIdx.x * blockDim.x; k0 < n_touched; k0 += gridDim.x * blockDim.x) {
+        if (threadIdx.x == 0) {
+            const uint32_t k1 = k0 + blockDim.x < n_touched ? k0 + blockDim.x : n_touched;
+            const uint32_t lo = e.tbeg[k0];
+            const uint32_t hi = k1 < n_touched ? e.tbeg[k1] : n_due;
+            const uint32_t cnt = staging ? (hi - lo < kStageEvents ? hi - lo : kStageEvents) : 0u;
+            s_lo = lo;
+            s_cnt = cnt;
+            if (cnt > 0) bulk_load(s_ev, e.evin + lo, cnt * static_cast<uint32_t>(sizeof(EvIn)), &s_bar);
         }
+        __syncthreads();
+        const Staged st{s_ev, s_lo, s_cnt};
+        bool waited = st.cnt == 0;
+        bool ok = true;
+        auto ready = [&]() {
+            if (!waited) {
+                ok = mbar_wait(&s_bar, parity);
+                waited = true;
+            }
+            return ok;
+        };
+        const uint32_t k = k0 + threadIdx.x;
+        if (k < n_touched) {
+            const uint32_t n = e.touched[k];
+            const uint32_t beg = e.tbeg[k];
+            const uint32_t end = k + 1 < n_touched ? e.tbeg[k + 1] : n_due;
+            if (e.nparam[n].max_refs == 1) {
+                process_target<true>(e, n, beg, end - beg, t, stdp, temporal, st, ready);
+            } else {
+                process_target<false>(e, n, beg, end - beg, t, stdp, temporal, st, ready);
+            }
+        }
+        ready();
+        const bool failed = __syncthreads_or(!ok);
+        if (st.cnt > 0) {
+            if (failed) {
+                // the block read its inputs from global memory; wait once more
+                // for the copy before the buffer is reused or the block exits
+                if (threadIdx.x == 0) raise_status(e, kStatusStageTimeout);
+                if (!__syncthreads_and(mbar_wait(&s_bar, parity))) return;
+            }
+            parity ^= 1u;
+        }
+        if (failed) staging = false;
     }
 }
 
@@ -1209,7 +1338,7 @@ void launch_tick(const Engine& e, cudaStream_t stream, cudaEvent_t* marks) {
     mark(false); k_scan_out<<<scan_grid, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_scatter<<<wide, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_events<<<e.grid_wide * 4, kThreads, 0, stream>>>(e); mark(true);
-    mark(false); k_process<<<e.grid_process, kThreads, 0, stream>>>(e); mark(true);
+    mark(false); k_process<<<e.grid_process, kThreads, kStageEvents * sizeof(EvIn), stream>>>(e); mark(true);
     mark(false); k_post<<<wide, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_fire_list<<<e.grid_fire, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_fire_count<<<e.grid_wide, kThreads, 0, stream>>>(e); mark(true);
@@ -1231,6 +1360,11 @@ void launch_group(const Engine& e, cudaStream_t stream) {
     k_scan_out<<<scan_grid, kThreads, 0, stream>>>(e);
     k_scatter<<<e.grid_wide, kThreads, 0, stream>>>(e);
     k_segsort<<<e.grid_wide * 4, kThreads, 0, stream>>>(e);
+}
+
+void configure_kernels() {
+    cudaFuncSetAttribute(k_process, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(kStageEvents * sizeof(EvIn)));
 }
 
 void launch_init_syn(const Engine& e, const SynA* a, cudaStream_t stream) {

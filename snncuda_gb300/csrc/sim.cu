@@ -505,6 +505,7 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.tile_sum = dalloc<uint32_t>(own, scan_tiles + 2);
     e.tile_nz = dalloc<uint32_t>(own, scan_tiles + 2);
     e.touched = dalloc<uint32_t>(own, N);
+    e.tbeg = dalloc<uint32_t>(own, N);
     e.grp = dalloc<unsigned long long>(own, slot_cap);
     e.grp_sorted = dalloc<unsigned long long>(own, slot_cap);
     e.evin = dalloc<EvIn>(own, slot_cap);
@@ -575,6 +576,7 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.tab.ltd = d_ltd;
     e.tab.stdp_len = static_cast<uint32_t>(ltp.size());
     launch_init_syn(e, d_syna_img, st);
+    configure_kernels();
     check(cudaGetLastError(), "init launch");
     sim->in_ptr = std::move(in_ptr);
 
@@ -595,6 +597,10 @@ int status_to_error(uint32_t status, std::string& msg) {
     if (status & kStatusPostCountOverflow) msg += "a neuron fired 65536+ times in one tick; ";
     if (status & kStatusRunOverflow) msg += "temporal run list overflow; ";
     if (status & kStatusFireOverflow) msg += "fires per tick exceeded the fire capacity; ";
+    if (status & kStatusStageTimeout) {
+        msg += "a bulk copy into shared memory did not complete within its wait limit; ";
+        return SNNCUDA_ERR_TIMEOUT;
+    }
     return SNNCUDA_ERR_CAPACITY;
 }
 
