@@ -128,6 +128,27 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def tick_roofline(w, events, fires, ext, prof, ticks, ms):
+    """Whole-tick roofline: minimal algorithmic bytes of the tick loop (a
+    compact structure-of-arrays design, per-term below) over the timed ticks,
+    against the measured HBM bandwidth.  Touched targets per tick come from the
+    profiled ticks that follow the timed region."""
+    if prof is None or prof["ticks"] == 0 or ms <= 0:
+        return None
+    fanout = fanin = w.fanout  # synapses per source and per target
+    touched = prof["touched_targets"] / prof["ticks"] * ticks
+    b = (fires * (8 + 7 * fanout)        # out-row pointers + per out-synapse index, delay, packed offsets
+         + events * (8 + 8)             # event written into its wheel slot, read at delivery
+         + events * (1 + 4 + 4 + 4 + 16)  # flags, weight, last_post, last_pre, code state read
+         + events * 4 + events * 16     # weight and code-state writes
+         + touched * 48 + ext * 8       # touched neurons' state read-modify-write, external inputs
+         + fires * fanin * 16)          # post-spike STDP over the fired neurons' incoming synapses
+    peak, kind = load_peaks()
+    achieved = b / (ms / 1e3) / 1e9
+    return {"bytes_per_event": b / max(events, 1), "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": kind}
+
+
 def workload_from_args(args):
     from snncuda_gb300 import synthetic
     w = synthetic.WORKLOADS[args.workload]
@@ -282,6 +303,7 @@ def main():
     c1 = sim.counters()
     ms = ev0.elapsed_time(ev1)
     events = c1["synaptic_events"] - c0["synaptic_events"]
+    ext_events = c1["external_events"] - c0["external_events"]
     fires = c1["fired_spikes"] - c0["fired_spikes"]
     if world > 1:
         t = torch.tensor([ms, float(events)], dtype=torch.float64, device=dev)
@@ -371,6 +393,7 @@ def main():
             "fires_per_tick": fires / (args.steps * tps),
             "events_per_tick": events / (args.steps * tps),
             "gpu_launches": args.steps * tps * KERNELS_PER_TICK,
+            "tick_roofline": tick_roofline(w, events, fires, ext_events, prof, args.steps * tps, ms_max),
             "clocks": clocks, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
         }
         print(json.dumps(line), flush=True)

@@ -215,6 +215,34 @@ int snncuda_sim_state_digest(snncuda_sim* sim, uint64_t* neuron_digest, uint64_t
 int snncuda_sim_read_raster(snncuda_sim* sim, uint64_t first, uint64_t count, uint64_t* ticks,
                             uint32_t* neurons);
 
+/* ---- batched form: many independent networks in one handle --------------
+ * The reference runs one NetworkPropagator per network, one after the other
+ * (or one CudaInferenceSession per network, CudaBackend.h:97-126).  A batch
+ * holds `count` networks and advances all of them in one tick loop; every
+ * network evolves exactly as it would alone under snncuda_sim_* (bit for
+ * bit), with its own neuron and synapse numbering (0-based, in its own
+ * Connectome order).  stdp_enabled[i] (NULL = all 1) is network i's
+ * StdpConfig::enabled; the other config fields are shared.  The runtime
+ * toggles apply to all networks (a network created with its rule disabled
+ * stays disabled).  max_slot_events in the counters is batch-wide. */
+typedef struct snncuda_batch snncuda_batch;
+int snncuda_batch_create(uint32_t count, const snncuda_network* networks, const int32_t* stdp_enabled,
+                         const snncuda_config* config, snncuda_batch** out);
+int snncuda_batch_destroy(snncuda_batch* batch);
+int snncuda_batch_inject(snncuda_batch* batch, uint32_t network, uint64_t count, const uint32_t* neurons,
+                         const uint64_t* ticks, const float* weights);
+int snncuda_batch_run_until(snncuda_batch* batch, uint64_t inclusive_tick);
+int snncuda_batch_set_plasticity(snncuda_batch* batch, int32_t enabled);
+int snncuda_batch_set_temporal_learning(snncuda_batch* batch, int32_t enabled);
+int snncuda_batch_counters(snncuda_batch* batch, uint32_t network, snncuda_counters* out);
+int snncuda_batch_read_neurons(snncuda_batch* batch, uint32_t network, const snncuda_neuron_state* out);
+int snncuda_batch_read_synapses(snncuda_batch* batch, uint32_t network, const snncuda_synapse_state* out);
+/* Digests of every network (arrays of `count`), as snncuda_sim_state_digest. */
+int snncuda_batch_state_digests(snncuda_batch* batch, uint64_t* neuron_digests, uint64_t* synapse_digests);
+/* Network's fire records [first, first + count) in its own processing order. */
+int snncuda_batch_read_raster(snncuda_batch* batch, uint32_t network, uint64_t first, uint64_t count,
+                              uint64_t* ticks, uint32_t* neurons);
+
 /* ---- engine extension: per-kernel device time ----------------------------
  * No counterpart in the reference (which times the whole tick loop on the
  * host clock, spike_throughput_benchmark.cpp:137-140).  Processes ticks like

@@ -539,3 +539,5 @@ int snncuda_group_events_static(const uint64_t* events, uint32_t count, uint32_t
 
 
 
+
+#include "../batch_of_sims.inc"

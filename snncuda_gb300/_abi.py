@@ -149,6 +149,20 @@ _SIGNATURES = {
                                         POINTER(c_uint32)]),
     "snncuda_sim_profile": (c_int, [c_void_p, c_uint64, POINTER(Profile)]),
     "snncuda_kernel_name": (c_char_p, [c_int32]),
+    "snncuda_batch_create": (c_int, [c_uint32, POINTER(Network), POINTER(c_int32), POINTER(Config),
+                                     POINTER(c_void_p)]),
+    "snncuda_batch_destroy": (c_int, [c_void_p]),
+    "snncuda_batch_inject": (c_int, [c_void_p, c_uint32, c_uint64, POINTER(c_uint32), POINTER(c_uint64),
+                                     POINTER(c_float)]),
+    "snncuda_batch_run_until": (c_int, [c_void_p, c_uint64]),
+    "snncuda_batch_set_plasticity": (c_int, [c_void_p, c_int32]),
+    "snncuda_batch_set_temporal_learning": (c_int, [c_void_p, c_int32]),
+    "snncuda_batch_counters": (c_int, [c_void_p, c_uint32, POINTER(Counters)]),
+    "snncuda_batch_read_neurons": (c_int, [c_void_p, c_uint32, POINTER(NeuronState)]),
+    "snncuda_batch_read_synapses": (c_int, [c_void_p, c_uint32, POINTER(SynapseState)]),
+    "snncuda_batch_state_digests": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64)]),
+    "snncuda_batch_read_raster": (c_int, [c_void_p, c_uint32, c_uint64, c_uint64, POINTER(c_uint64),
+                                          POINTER(c_uint32)]),
     "snncuda_group_events": (c_int, [c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]),
     "snncuda_group_events_static": (c_int, [c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]),
 }

@@ -39,6 +39,7 @@ constexpr int kMetaCompShift = 16;      // 2 bits
 constexpr int kMetaRecShift = 18;       // 2 bits
 constexpr int kMetaPlasticBit = 20;     // 1 bit
 constexpr int kMetaExpectedShift = 21;  // 4 bits: max(2, #code offsets), <= 8
+constexpr int kMetaRuleOffBit = 25;     // the synapse's network runs with the STDP rule disabled
 
 constexpr int kMaxExpected = 8;
 
@@ -264,6 +265,14 @@ void launch_inject(const Engine& e, const unsigned long long* ev, const uint32_t
 // Groups the W == 1 "wheel" of e (a caller's event buffer) by target: the
 // hist / scan / scatter / segment-sort kernels of a tick.
 void launch_group(const Engine& e, cudaStream_t stream);
+// Batched form: one handle simulates several networks side by side.
+// Sets kMetaRuleOffBit on target-major synapses [tm_begin, tm_end).
+void launch_rule_off(const Engine& e, unsigned long long tm_begin, unsigned long long tm_end, cudaStream_t stream);
+// out[0] += spike counts of neurons [n_begin, n_end); out[1] += pre-spike
+// counts of target-major synapses [tm_begin, tm_end); out[2] += wheel events
+// (all slots) whose target is in [n_begin, n_end).  out must start at zero.
+void launch_range_counts(const Engine& e, uint32_t n_begin, uint32_t n_end, unsigned long long tm_begin,
+                         unsigned long long tm_end, unsigned long long* out, cudaStream_t stream);
 // One-time kernel attributes (dynamic shared memory of k_process); call with
 // the device current before the first tick.
 void configure_kernels();

@@ -445,7 +445,7 @@ __device__ bool process_input(NState& s, const NeuronParam& p, uint32_t comp, ui
 __device__ void stdp_apply(SynA& a, uint32_t pre, uint32_t post, const Engine& e, int stdp) {
     const float before = a.weight;
     float delta = 0.0f;
-    if (stdp) {
+    if (stdp && !((a.meta >> kMetaRuleOffBit) & 1u)) {
         if (post > pre) {
             const uint32_t dt = post - pre;
             delta = e.tab.ltp[dt < e.tab.stdp_len ? dt : e.tab.stdp_len - 1];
@@ -1322,7 +1322,42 @@ __global__ void k_inject(Engine e, const unsigned long long* ev, const uint32_t*
     }
 }
 
+__global__ void k_rule_off(SynAB* syn, unsigned long long b, unsigned long long en) {
+    for (unsigned long long i = b + blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; i < en;
+         i += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
+        syn[i].a.meta |= 1u << kMetaRuleOffBit;
+}
+
+__global__ void k_range_counts(Engine e, uint32_t nb, uint32_t ne, unsigned long long tb, unsigned long long te,
+                               unsigned long long* out) {
+    const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+    const unsigned long long first = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+    unsigned long long spikes = 0, pre = 0, wheel = 0;
+    for (unsigned long long n = nb + first; n < ne; n += stride) spikes += e.nrec[n].spike_count;
+    for (unsigned long long i = tb + first; i < te; i += stride) pre += e.syn[i].b.pre_count;
+    for (uint32_t slot = 0; slot < e.W; ++slot) {
+        const uint32_t cnt = e.slot_count[slot];
+        const unsigned long long* ev = e.wheel + static_cast<size_t>(slot) * e.slot_cap;
+        for (unsigned long long i = first; i < cnt; i += stride) {
+            const uint32_t tgt = static_cast<uint32_t>(ev[i]) & ~kExternalBit;
+            wheel += tgt >= nb && tgt < ne;
+        }
+    }
+    if (spikes) atomicAdd(out, spikes);
+    if (pre) atomicAdd(out + 1, pre);
+    if (wheel) atomicAdd(out + 2, wheel);
+}
+
 }  // namespace
+
+void launch_rule_off(const Engine& e, unsigned long long tm_begin, unsigned long long tm_end, cudaStream_t stream) {
+    if (tm_end > tm_begin) k_rule_off<<<1024, kThreads, 0, stream>>>(e.syn, tm_begin, tm_end);
+}
+
+void launch_range_counts(const Engine& e, uint32_t n_begin, uint32_t n_end, unsigned long long tm_begin,
+                         unsigned long long tm_end, unsigned long long* out, cudaStream_t stream) {
+    k_range_counts<<<e.grid_wide, kThreads, 0, stream>>>(e, n_begin, n_end, tm_begin, tm_end, out);
+}
 
 void launch_tick(const Engine& e, cudaStream_t stream, cudaEvent_t* marks) {
     const uint32_t tiles = (e.N + kScanTile - 1) / kScanTile;

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <stdexcept>
@@ -945,51 +946,60 @@ int snncuda_sim_idle(snncuda_sim* sim, int32_t* out) {
     return rc;
 }
 
+// Neurons [n0, n1) into o[0 .. n1-n0).
+static void read_neurons_range(snncuda_sim* sim, uint32_t n0, uint32_t n1, const snncuda_neuron_state* o) {
+    const std::vector<NeuronRec> r = sim->d2h(sim->e.nrec + n0, n1 - n0);
+    const std::vector<NeuronTp> q = sim->d2h(sim->e.ntp + n0, n1 - n0);
+    for (uint32_t i = 0; i < n1 - n0; ++i) {
+        if (o->membrane_potential) o->membrane_potential[i] = r[i].membrane;
+        if (o->spike_count) o->spike_count[i] = r[i].spike_count;
+        if (o->last_fired_tick) o->last_fired_tick[i] = r[i].last_fired1 ? static_cast<int64_t>(r[i].last_fired1) - 1 : -1;
+        if (o->last_active_tick) o->last_active_tick[i] = r[i].last_active;
+        for (int k = 0; k < 4; ++k) {
+            if (o->compartment_current) o->compartment_current[i * 4 + k] = r[i].cur[k];
+            if (o->compartment_last_update) o->compartment_last_update[i * 4 + k] = r[i].upd[k];
+            if (o->compartment_tau) o->compartment_tau[i * 4 + k] = kTauValue[(r[i].flags >> (2 * k)) & 3u];
+        }
+        if (o->window_start_tick) o->window_start_tick[i] = r[i].ws;
+        if (o->offset_count) o->offset_count[i] = r[i].len;
+        if (o->learned_count) o->learned_count[i] = q[i].ref_count;
+        if (o->match_count) o->match_count[i] = r[i].match_count;
+        if (o->last_match) o->last_match[i] = (r[i].flags >> 8) & 1u;
+    }
+}
+
 int snncuda_sim_read_neurons(snncuda_sim* sim, const snncuda_neuron_state* o) {
     if (sim == nullptr || o == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
-    return guarded([&] {
-        const std::vector<NeuronRec> r = sim->d2h(sim->e.nrec, sim->N);
-        const std::vector<NeuronTp> q = sim->d2h(sim->e.ntp, sim->N);
-        for (uint32_t i = 0; i < sim->N; ++i) {
-            if (o->membrane_potential) o->membrane_potential[i] = r[i].membrane;
-            if (o->spike_count) o->spike_count[i] = r[i].spike_count;
-            if (o->last_fired_tick) o->last_fired_tick[i] = r[i].last_fired1 ? static_cast<int64_t>(r[i].last_fired1) - 1 : -1;
-            if (o->last_active_tick) o->last_active_tick[i] = r[i].last_active;
-            for (int k = 0; k < 4; ++k) {
-                if (o->compartment_current) o->compartment_current[i * 4 + k] = r[i].cur[k];
-                if (o->compartment_last_update) o->compartment_last_update[i * 4 + k] = r[i].upd[k];
-                if (o->compartment_tau) o->compartment_tau[i * 4 + k] = kTauValue[(r[i].flags >> (2 * k)) & 3u];
-            }
-            if (o->window_start_tick) o->window_start_tick[i] = r[i].ws;
-            if (o->offset_count) o->offset_count[i] = r[i].len;
-            if (o->learned_count) o->learned_count[i] = q[i].ref_count;
-            if (o->match_count) o->match_count[i] = r[i].match_count;
-            if (o->last_match) o->last_match[i] = (r[i].flags >> 8) & 1u;
-        }
-    });
+    return guarded([&] { read_neurons_range(sim, 0, sim->N, o); });
+}
+
+// Synapses of Connectome indices [c0, c1), whose target-major slots are
+// [t0, t1), into o[0 .. c1-c0).
+static void read_synapses_range(snncuda_sim* sim, uint64_t c0, uint64_t c1, uint64_t t0, uint64_t t1,
+                         const snncuda_synapse_state* o) {
+    const std::vector<SynAB> rec = sim->d2h(sim->e.syn + t0, t1 - t0);
+    for (uint64_t tm = t0; tm < t1; ++tm) {
+        const uint64_t i = sim->c_of_tm[tm] - c0;
+        const SynA& a = rec[tm - t0].a;
+        const SynB& b = rec[tm - t0].b;
+        if (o->weight) o->weight[i] = a.weight;
+        if (o->last_pre_spike_tick) o->last_pre_spike_tick[i] = a.last_pre1 ? static_cast<int64_t>(a.last_pre1) - 1 : -1;
+        if (o->last_post_spike_tick) o->last_post_spike_tick[i] = a.last_post1 ? static_cast<int64_t>(a.last_post1) - 1 : -1;
+        if (o->pre_spike_count) o->pre_spike_count[i] = b.pre_count;
+        if (o->plasticity_update_count) o->plasticity_update_count[i] = a.updates;
+        if (o->last_weight_delta) o->last_weight_delta[i] = a.last_delta;
+        if (o->code_window_start_tick) o->code_window_start_tick[i] = b.code_ws;
+        if (o->code_offset_count) o->code_offset_count[i] = b.code_len;
+        if (o->learned_code_count) o->learned_code_count[i] = b.learned_count;
+        if (o->code_match_count) o->code_match_count[i] = b.code_matches;
+        if (o->last_code_match) o->last_code_match[i] = b.flags & 1u;
+    }
+    (void)c1;
 }
 
 int snncuda_sim_read_synapses(snncuda_sim* sim, const snncuda_synapse_state* o) {
     if (sim == nullptr || o == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
-    return guarded([&] {
-        const std::vector<SynAB> rec = sim->d2h(sim->e.syn, sim->S);
-        for (uint64_t tm = 0; tm < sim->S; ++tm) {
-            const uint64_t i = sim->c_of_tm[tm];
-            const SynA& a = rec[tm].a;
-            const SynB& b = rec[tm].b;
-            if (o->weight) o->weight[i] = a.weight;
-            if (o->last_pre_spike_tick) o->last_pre_spike_tick[i] = a.last_pre1 ? static_cast<int64_t>(a.last_pre1) - 1 : -1;
-            if (o->last_post_spike_tick) o->last_post_spike_tick[i] = a.last_post1 ? static_cast<int64_t>(a.last_post1) - 1 : -1;
-            if (o->pre_spike_count) o->pre_spike_count[i] = b.pre_count;
-            if (o->plasticity_update_count) o->plasticity_update_count[i] = a.updates;
-            if (o->last_weight_delta) o->last_weight_delta[i] = a.last_delta;
-            if (o->code_window_start_tick) o->code_window_start_tick[i] = b.code_ws;
-            if (o->code_offset_count) o->code_offset_count[i] = b.code_len;
-            if (o->learned_code_count) o->learned_code_count[i] = b.learned_count;
-            if (o->code_match_count) o->code_match_count[i] = b.code_matches;
-            if (o->last_code_match) o->last_code_match[i] = b.flags & 1u;
-        }
-    });
+    return guarded([&] { read_synapses_range(sim, 0, sim->S, 0, sim->S, o); });
 }
 
 int snncuda_sim_read_pattern(snncuda_sim* sim, int32_t kind, uint64_t index, uint64_t which, uint32_t* values,
@@ -1043,66 +1053,73 @@ int snncuda_sim_read_pattern(snncuda_sim* sim, int32_t kind, uint64_t index, uin
 }
 
 // Same digest definition as every other implementation of this ABI.
+// State digests of neurons [n0, n1) and Connectome synapses [c0, c1): the
+// same words, in the same order, a network alone would hash.
+static void digest_range(snncuda_sim* sim, const HostState& h, uint32_t n0, uint32_t n1, uint64_t c0, uint64_t c1,
+                  uint64_t* neuron_digest, uint64_t* synapse_digest) {
+    std::vector<uint32_t> v;
+    if (neuron_digest) {
+        Digest d;
+        for (uint32_t n = n0; n < n1; ++n) {
+            const NeuronRec& r = h.nrec[n];
+            d.f32(r.membrane);
+            d.word(r.spike_count);
+            d.word(r.last_fired1 ? static_cast<uint64_t>(r.last_fired1 - 1) : ~0ULL);
+            d.word(r.last_active);
+            for (int k = 0; k < 4; ++k) {
+                d.f32(r.cur[k]);
+                d.word(r.upd[k]);
+                d.f32(kTauValue[(r.flags >> (2 * k)) & 3u]);
+            }
+            d.word(r.ws);
+            neuron_offsets(sim, h, n, v);
+            d.word(v.size());
+            for (uint32_t x : v) d.word(x);
+            d.word(h.ntp[n].ref_count);
+            for (uint32_t j = 0; j < h.ntp[n].ref_count; ++j) {
+                neuron_learned(sim, h, n, j, v);
+                d.word(v.size());
+                for (uint32_t x : v) d.word(x);
+            }
+            d.word((r.flags >> 8) & 1u);
+            d.word(r.match_count);
+        }
+        *neuron_digest = d.h;
+    }
+    if (synapse_digest) {
+        const std::vector<uint32_t>& tm_of_c = sim->tm_of_c;
+        Digest d;
+        for (uint64_t c = c0; c < c1; ++c) {
+            const uint64_t tm = tm_of_c[c];
+            const SynA& a = h.syn[tm].a;
+            const SynB& b = h.syn[tm].b;
+            d.f32(a.weight);
+            d.word(a.last_pre1 ? static_cast<uint64_t>(a.last_pre1 - 1) : ~0ULL);
+            d.word(a.last_post1 ? static_cast<uint64_t>(a.last_post1 - 1) : ~0ULL);
+            d.word(b.pre_count);
+            d.word(a.updates);
+            d.f32(a.last_delta);
+            d.word(b.code_ws);
+            d.word(b.code_len);
+            for (uint32_t j = 0; j < b.code_len; ++j) d.word(ring_get(b.ring_lo, b.ring_hi, j));
+            d.word(b.learned_count);
+            for (uint32_t j = 0; j < b.learned_count; ++j) {
+                synapse_learned(sim, h, tm, j, v);
+                d.word(v.size());
+                for (uint32_t x : v) d.word(x);
+            }
+            d.word(b.code_matches);
+            d.word(b.flags & 1u);
+        }
+        *synapse_digest = d.h;
+    }
+}
+
 int snncuda_sim_state_digest(snncuda_sim* sim, uint64_t* neuron_digest, uint64_t* synapse_digest) {
     if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
     return guarded([&] {
         const HostState h = fetch_all(sim, true);
-        std::vector<uint32_t> v;
-        if (neuron_digest) {
-            Digest d;
-            for (uint32_t n = 0; n < sim->N; ++n) {
-                const NeuronRec& r = h.nrec[n];
-                d.f32(r.membrane);
-                d.word(r.spike_count);
-                d.word(r.last_fired1 ? static_cast<uint64_t>(r.last_fired1 - 1) : ~0ULL);
-                d.word(r.last_active);
-                for (int k = 0; k < 4; ++k) {
-                    d.f32(r.cur[k]);
-                    d.word(r.upd[k]);
-                    d.f32(kTauValue[(r.flags >> (2 * k)) & 3u]);
-                }
-                d.word(r.ws);
-                neuron_offsets(sim, h, n, v);
-                d.word(v.size());
-                for (uint32_t x : v) d.word(x);
-                d.word(h.ntp[n].ref_count);
-                for (uint32_t j = 0; j < h.ntp[n].ref_count; ++j) {
-                    neuron_learned(sim, h, n, j, v);
-                    d.word(v.size());
-                    for (uint32_t x : v) d.word(x);
-                }
-                d.word((r.flags >> 8) & 1u);
-                d.word(r.match_count);
-            }
-            *neuron_digest = d.h;
-        }
-        if (synapse_digest) {
-            const std::vector<uint32_t>& tm_of_c = sim->tm_of_c;
-            Digest d;
-            for (uint64_t c = 0; c < sim->S; ++c) {
-                const uint64_t tm = tm_of_c[c];
-                const SynA& a = h.syn[tm].a;
-                const SynB& b = h.syn[tm].b;
-                d.f32(a.weight);
-                d.word(a.last_pre1 ? static_cast<uint64_t>(a.last_pre1 - 1) : ~0ULL);
-                d.word(a.last_post1 ? static_cast<uint64_t>(a.last_post1 - 1) : ~0ULL);
-                d.word(b.pre_count);
-                d.word(a.updates);
-                d.f32(a.last_delta);
-                d.word(b.code_ws);
-                d.word(b.code_len);
-                for (uint32_t j = 0; j < b.code_len; ++j) d.word(ring_get(b.ring_lo, b.ring_hi, j));
-                d.word(b.learned_count);
-                for (uint32_t j = 0; j < b.learned_count; ++j) {
-                    synapse_learned(sim, h, tm, j, v);
-                    d.word(v.size());
-                    for (uint32_t x : v) d.word(x);
-                }
-                d.word(b.code_matches);
-                d.word(b.flags & 1u);
-            }
-            *synapse_digest = d.h;
-        }
+        digest_range(sim, h, 0, sim->N, 0, sim->S, neuron_digest, synapse_digest);
     });
 }
 
@@ -1274,6 +1291,235 @@ int snncuda_sim_read_raster(snncuda_sim* sim, uint64_t first, uint64_t count, ui
         for (uint64_t i = 0; i < count; ++i) {
             if (ticks) ticks[i] = r[2 * i];
             if (neurons) neurons[i] = r[2 * i + 1];
+        }
+    });
+}
+
+
+// ---------------------------------------------------------------------------
+// batched form: the networks of a batch are one disjoint union inside a
+// single simulation.  Network i owns neurons [nbase[i], nbase[i+1]) and
+// Connectome synapses [sbase[i], sbase[i+1]); since its synapses only target
+// its own neurons, its target-major synapses are one range too.  Nothing in a
+// tick couples two networks: each target's events keep their network's own
+// order (fires in due order, expansion in Connectome x offset order, the
+// network's injections in call order), so every network follows its solo
+// trajectory exactly.
+// ---------------------------------------------------------------------------
+
+struct snncuda_batch {
+    snncuda_sim* sim{nullptr};
+    uint32_t count{0};
+    std::vector<uint32_t> nbase;                   // [count + 1]
+    std::vector<uint64_t> sbase;                   // [count + 1]
+    std::vector<std::vector<uint64_t>> inj_ticks;  // per network: clamped delivery tick of each injection
+    unsigned long long* d_counts{nullptr};         // [3] scratch of launch_range_counts
+    ~snncuda_batch() {
+        if (d_counts) cudaFree(d_counts);
+        delete sim;
+    }
+    uint64_t tm_begin(uint32_t i) const { return sim->in_ptr[nbase[i]]; }
+    uint64_t tm_end(uint32_t i) const { return sim->in_ptr[nbase[i + 1]]; }
+};
+
+static snncuda_batch* batch_create_impl(uint32_t count, const snncuda_network* nets, const int32_t* stdp_enabled,
+                                        const snncuda_config& cfg) {
+    std::unique_ptr<snncuda_batch> b(new snncuda_batch());
+    b->count = count;
+    b->nbase.assign(count + 1, 0);
+    b->sbase.assign(count + 1, 0);
+    b->inj_ticks.resize(count);
+    uint64_t codes_total = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        const snncuda_network& n = nets[i];
+        if (static_cast<uint64_t>(b->nbase[i]) + n.neuron_count >= (1u << 31))
+            throw_fail(SNNCUDA_ERR_UNSUPPORTED, "at most 2^31-1 neurons per batch");
+        b->nbase[i + 1] = b->nbase[i] + n.neuron_count;
+        b->sbase[i + 1] = b->sbase[i] + n.synapse_count;
+        if (n.code_offset_ptr && n.code_offsets) codes_total += n.code_offset_ptr[n.synapse_count];
+    }
+    const uint32_t N = b->nbase[count];
+    const uint64_t S = b->sbase[count];
+    std::vector<float> thr(N), sim_thr(N), w(S), mw(S);
+    std::vector<uint64_t> win(N), refs(N), cptr(S + 1, 0);
+    std::vector<uint32_t> src(S), tgt(S), dly(S), codes;
+    std::vector<uint8_t> comp(S), rec(S), plast(S);
+    codes.reserve(codes_total);
+    for (uint32_t i = 0; i < count; ++i) {
+        const snncuda_network& n = nets[i];
+        const uint32_t nb = b->nbase[i];
+        const uint64_t sb = b->sbase[i];
+        if (n.neuron_count > 0 && (!n.threshold || !n.pattern_window_ticks || !n.similarity_threshold ||
+                                   !n.max_reference_patterns))
+            throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "neuron parameter arrays are required");
+        if (n.synapse_count > 0 && (!n.source || !n.target || !n.weight || !n.max_weight || !n.delay_ticks ||
+                                    !n.compartment || !n.receptor || !n.plasticity_enabled))
+            throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "synapse arrays are required");
+        std::copy(n.threshold, n.threshold + n.neuron_count, thr.begin() + nb);
+        std::copy(n.pattern_window_ticks, n.pattern_window_ticks + n.neuron_count, win.begin() + nb);
+        std::copy(n.similarity_threshold, n.similarity_threshold + n.neuron_count, sim_thr.begin() + nb);
+        std::copy(n.max_reference_patterns, n.max_reference_patterns + n.neuron_count, refs.begin() + nb);
+        const bool has_codes = n.code_offset_ptr && n.code_offsets;
+        for (uint64_t k = 0; k < n.synapse_count; ++k) {
+            if (n.source[k] >= n.neuron_count || n.target[k] >= n.neuron_count)
+                throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "synapse endpoint out of range");
+            src[sb + k] = nb + n.source[k];
+            tgt[sb + k] = nb + n.target[k];
+            if (has_codes)
+                codes.insert(codes.end(), n.code_offsets + n.code_offset_ptr[k], n.code_offsets + n.code_offset_ptr[k + 1]);
+            cptr[sb + k + 1] = codes.size();
+        }
+        std::copy(n.weight, n.weight + n.synapse_count, w.begin() + sb);
+        std::copy(n.max_weight, n.max_weight + n.synapse_count, mw.begin() + sb);
+        std::copy(n.delay_ticks, n.delay_ticks + n.synapse_count, dly.begin() + sb);
+        std::copy(n.compartment, n.compartment + n.synapse_count, comp.begin() + sb);
+        std::copy(n.receptor, n.receptor + n.synapse_count, rec.begin() + sb);
+        std::copy(n.plasticity_enabled, n.plasticity_enabled + n.synapse_count, plast.begin() + sb);
+    }
+    snncuda_network u{N,        thr.data(), win.data(),  sim_thr.data(), refs.data(),  S,
+                      src.data(), tgt.data(), w.data(),   mw.data(),      dly.data(),   comp.data(),
+                      rec.data(), plast.data(), cptr.data(), codes.data()};
+    b->sim = new snncuda_sim();
+    create_impl(&u, cfg, b->sim);
+    for (uint32_t i = 0; i < count; ++i)
+        if (stdp_enabled && !stdp_enabled[i]) launch_rule_off(b->sim->e, b->tm_begin(i), b->tm_end(i), b->sim->stream);
+    check(cudaGetLastError(), "batch rule launch");
+    check(cudaMalloc(&b->d_counts, 3 * sizeof(unsigned long long)), "cudaMalloc");
+    check(cudaStreamSynchronize(b->sim->stream), "batch create synchronize");
+    return b.release();
+}
+
+// The network's fire records, in order, from the batch's raster.
+static void batch_raster(snncuda_batch* b, uint32_t i, std::vector<uint64_t>& ticks, std::vector<uint32_t>& neurons) {
+    snncuda_sim* sim = b->sim;
+    const TickState ts = sim->read_ts();
+    const uint64_t have = std::min<uint64_t>(ts.raster_count, sim->e.raster_cap);
+    const std::vector<uint32_t> r = sim->d2h(sim->e.raster, 2 * have);
+    ticks.clear();
+    neurons.clear();
+    for (uint64_t j = 0; j < have; ++j) {
+        const uint32_t n = r[2 * j + 1];
+        if (n >= b->nbase[i] && n < b->nbase[i + 1]) {
+            ticks.push_back(r[2 * j]);
+            neurons.push_back(n - b->nbase[i]);
+        }
+    }
+}
+
+int snncuda_batch_create(uint32_t count, const snncuda_network* networks, const int32_t* stdp_enabled,
+                         const snncuda_config* config, snncuda_batch** out) {
+    if ((count > 0 && networks == nullptr) || out == nullptr)
+        return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
+    snncuda_config def;
+    snncuda_config_default(&def);
+    const snncuda_config& cfg = config ? *config : def;
+    snncuda_batch* b = nullptr;
+    const int rc = guarded([&] { b = batch_create_impl(count, networks, stdp_enabled, cfg); });
+    if (rc == SNNCUDA_OK) *out = b;
+    return rc;
+}
+
+int snncuda_batch_destroy(snncuda_batch* batch) {
+    delete batch;
+    return SNNCUDA_OK;
+}
+
+int snncuda_batch_inject(snncuda_batch* b, uint32_t network, uint64_t count, const uint32_t* neurons,
+                         const uint64_t* ticks, const float* weights) {
+    if (b == nullptr || network >= b->count) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "bad batch or network");
+    if (count > 0 && (!neurons || !ticks || !weights)) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null array");
+    const uint32_t nb = b->nbase[network], nn = b->nbase[network + 1] - nb;
+    std::vector<uint32_t> g(count);
+    for (uint64_t k = 0; k < count; ++k) {
+        if (neurons[k] >= nn) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "inject neuron out of range");
+        g[k] = nb + neurons[k];
+    }
+    const int rc = snncuda_sim_inject(b->sim, count, g.data(), ticks, weights);
+    if (rc == SNNCUDA_OK) {
+        auto& v = b->inj_ticks[network];
+        for (uint64_t k = 0; k < count; ++k) v.push_back(std::max<uint64_t>(ticks[k], b->sim->next_tick));
+    }
+    return rc;
+}
+
+int snncuda_batch_run_until(snncuda_batch* b, uint64_t inclusive_tick) {
+    if (b == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null batch");
+    return snncuda_sim_run_until(b->sim, inclusive_tick);
+}
+
+int snncuda_batch_set_plasticity(snncuda_batch* b, int32_t enabled) {
+    if (b == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null batch");
+    return snncuda_sim_set_plasticity(b->sim, enabled);
+}
+
+int snncuda_batch_set_temporal_learning(snncuda_batch* b, int32_t enabled) {
+    if (b == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null batch");
+    return snncuda_sim_set_temporal_learning(b->sim, enabled);
+}
+
+int snncuda_batch_counters(snncuda_batch* b, uint32_t i, snncuda_counters* out) {
+    if (b == nullptr || out == nullptr || i >= b->count) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "bad argument");
+    return guarded([&] {
+        snncuda_sim* sim = b->sim;
+        cudaStream_t st = sim->stream;
+        check(cudaMemsetAsync(b->d_counts, 0, 3 * sizeof(unsigned long long), st), "memset");
+        launch_range_counts(sim->e, b->nbase[i], b->nbase[i + 1], b->tm_begin(i), b->tm_end(i), b->d_counts, st);
+        check(cudaGetLastError(), "count launch");
+        unsigned long long c[3];
+        check(cudaMemcpyAsync(c, b->d_counts, sizeof(c), cudaMemcpyDeviceToHost, st), "counts");
+        const TickState ts = sim->read_ts();  // synchronizes the stream
+        uint64_t external = 0;
+        for (uint64_t t : b->inj_ticks[i]) external += t < sim->next_tick;
+        uint64_t pending = c[2];
+        for (size_t k = sim->pend_head; k < sim->pending.size(); ++k) {
+            const uint32_t n = static_cast<uint32_t>(sim->pending[k].event) & ~kExternalBit;
+            pending += n >= b->nbase[i] && n < b->nbase[i + 1];
+        }
+        std::vector<uint64_t> rt;
+        std::vector<uint32_t> rn;
+        batch_raster(b, i, rt, rn);
+        out->fired_spikes = c[0];
+        out->synaptic_events = c[1];
+        out->external_events = external;
+        out->delivered_spikes = c[1] + external;
+        out->next_tick = sim->next_tick;
+        out->pending_events = pending;
+        out->raster_count = rt.size();
+        out->max_slot_events = ts.max_slot_events;
+    });
+}
+
+int snncuda_batch_read_neurons(snncuda_batch* b, uint32_t i, const snncuda_neuron_state* out) {
+    if (b == nullptr || out == nullptr || i >= b->count) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "bad argument");
+    return guarded([&] { read_neurons_range(b->sim, b->nbase[i], b->nbase[i + 1], out); });
+}
+
+int snncuda_batch_read_synapses(snncuda_batch* b, uint32_t i, const snncuda_synapse_state* out) {
+    if (b == nullptr || out == nullptr || i >= b->count) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "bad argument");
+    return guarded([&] { read_synapses_range(b->sim, b->sbase[i], b->sbase[i + 1], b->tm_begin(i), b->tm_end(i), out); });
+}
+
+int snncuda_batch_state_digests(snncuda_batch* b, uint64_t* neuron_digests, uint64_t* synapse_digests) {
+    if (b == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null batch");
+    return guarded([&] {
+        const HostState h = fetch_all(b->sim, true);
+        for (uint32_t i = 0; i < b->count; ++i)
+            digest_range(b->sim, h, b->nbase[i], b->nbase[i + 1], b->sbase[i], b->sbase[i + 1],
+                         neuron_digests ? neuron_digests + i : nullptr, synapse_digests ? synapse_digests + i : nullptr);
+    });
+}
+
+int snncuda_batch_read_raster(snncuda_batch* b, uint32_t i, uint64_t first, uint64_t count, uint64_t* ticks,
+                              uint32_t* neurons) {
+    if (b == nullptr || i >= b->count) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "bad argument");
+    return guarded([&] {
+        std::vector<uint64_t> rt;
+        std::vector<uint32_t> rn;
+        batch_raster(b, i, rt, rn);
+        if (first + count > rt.size()) throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "raster range out of bounds");
+        for (uint64_t k = 0; k < count; ++k) {
+            if (ticks) ticks[k] = rt[first + k];
+            if (neurons) neurons[k] = rn[first + k];
         }
     });
 }

@@ -17,7 +17,7 @@ import os
 import pathlib
 from ctypes import c_float, c_int32, c_int64, c_uint8, c_uint32, c_uint64, c_void_p
 from dataclasses import dataclass
-from typing import Dict, List, Optional
+from typing import Dict, List, Optional, Sequence
 
 import numpy as np
 
@@ -66,6 +66,79 @@ def _check(lib, status: int) -> None:
         raise SNNCudaError(status, lib.snncuda_last_error().decode("utf-8", "replace"))
 
 
+def _network_struct(c: Connectome):
+    """snncuda_network view of a Connectome plus the arrays it points into
+    (keep them alive until the create call returns)."""
+    keep = [np.ascontiguousarray(a) for a in (
+        c.threshold.astype(np.float32), c.pattern_window_ticks.astype(np.uint64),
+        c.similarity_threshold.astype(np.float32), c.max_reference_patterns.astype(np.uint64),
+        c.source.astype(np.uint32), c.target.astype(np.uint32), c.weight.astype(np.float32),
+        c.max_weight.astype(np.float32), c.delay_ticks.astype(np.uint32),
+        c.compartment.astype(np.uint8), c.receptor.astype(np.uint8),
+        c.plasticity_enabled.astype(np.uint8))]
+    (thr, win, sim, refs, src, tgt, w, mw, dly, comp, rec, pl) = keep
+    code_ptr = code = None
+    if c.code_offset_ptr is not None:
+        code_ptr = np.ascontiguousarray(c.code_offset_ptr.astype(np.uint64))
+        code = np.ascontiguousarray(c.code_offsets.astype(np.uint32))
+        if code.size == 0:
+            code = np.zeros(1, dtype=np.uint32)
+        keep += [code_ptr, code]
+    net = _abi.Network(
+        c.neuron_count, _abi.ptr(thr, c_float), _abi.ptr(win, c_uint64), _abi.ptr(sim, c_float),
+        _abi.ptr(refs, c_uint64), c.synapse_count, _abi.ptr(src, c_uint32),
+        _abi.ptr(tgt, c_uint32), _abi.ptr(w, c_float), _abi.ptr(mw, c_float),
+        _abi.ptr(dly, c_uint32), _abi.ptr(comp, c_uint8), _abi.ptr(rec, c_uint8),
+        _abi.ptr(pl, c_uint8), _abi.ptr(code_ptr, c_uint64), _abi.ptr(code, c_uint32))
+    return net, keep
+
+
+def _neuron_arrays(n: int):
+    arrays = {
+        "membrane_potential": np.zeros(n, np.float32), "spike_count": np.zeros(n, np.uint64),
+        "last_fired_tick": np.zeros(n, np.int64), "last_active_tick": np.zeros(n, np.uint64),
+        "compartment_current": np.zeros(n * 4, np.float32),
+        "compartment_last_update": np.zeros(n * 4, np.uint64),
+        "compartment_tau": np.zeros(n * 4, np.float32),
+        "window_start_tick": np.zeros(n, np.uint64), "offset_count": np.zeros(n, np.uint64),
+        "learned_count": np.zeros(n, np.uint64), "match_count": np.zeros(n, np.uint64),
+        "last_match": np.zeros(n, np.uint8),
+    }
+    types = dict(_abi.NeuronState._fields_)
+    view = _abi.NeuronState(**{k: _abi.ptr(v, types[k]._type_) for k, v in arrays.items()})
+    return arrays, view
+
+
+def _finish_neurons(arrays, n: int):
+    for k in ("compartment_current", "compartment_last_update", "compartment_tau"):
+        arrays[k] = arrays[k].reshape(n, 4)
+    return arrays
+
+
+def _synapse_arrays(s: int):
+    arrays = {
+        "weight": np.zeros(s, np.float32), "last_pre_spike_tick": np.zeros(s, np.int64),
+        "last_post_spike_tick": np.zeros(s, np.int64), "pre_spike_count": np.zeros(s, np.uint64),
+        "plasticity_update_count": np.zeros(s, np.uint64),
+        "last_weight_delta": np.zeros(s, np.float32),
+        "code_window_start_tick": np.zeros(s, np.uint64),
+        "code_offset_count": np.zeros(s, np.uint64), "learned_code_count": np.zeros(s, np.uint64),
+        "code_match_count": np.zeros(s, np.uint64), "last_code_match": np.zeros(s, np.uint8),
+    }
+    types = dict(_abi.SynapseState._fields_)
+    view = _abi.SynapseState(**{k: _abi.ptr(v, types[k]._type_) for k, v in arrays.items()})
+    return arrays, view
+
+
+def _inject_arrays(neurons, ticks, weights):
+    n = np.ascontiguousarray(np.asarray(neurons, dtype=np.uint32).ravel())
+    t = np.ascontiguousarray(np.asarray(ticks, dtype=np.uint64).ravel())
+    w = np.ascontiguousarray(np.asarray(weights, dtype=np.float32).ravel())
+    if not (n.size == t.size == w.size):
+        raise ValueError("inject arrays must have equal length")
+    return n, t, w
+
+
 class Simulation:
     """One simulation handle over a Connectome (0-based neuron indices)."""
 
@@ -75,28 +148,8 @@ class Simulation:
         self.lib = lib or backend()
         self.connectome = connectome
         self.config = config if config is not None else default_config(self.lib)
+        net, self._keep = _network_struct(connectome)
         c = connectome
-        self._keep = [np.ascontiguousarray(a) for a in (
-            c.threshold.astype(np.float32), c.pattern_window_ticks.astype(np.uint64),
-            c.similarity_threshold.astype(np.float32), c.max_reference_patterns.astype(np.uint64),
-            c.source.astype(np.uint32), c.target.astype(np.uint32), c.weight.astype(np.float32),
-            c.max_weight.astype(np.float32), c.delay_ticks.astype(np.uint32),
-            c.compartment.astype(np.uint8), c.receptor.astype(np.uint8),
-            c.plasticity_enabled.astype(np.uint8))]
-        (thr, win, sim, refs, src, tgt, w, mw, dly, comp, rec, pl) = self._keep
-        code_ptr = code = None
-        if c.code_offset_ptr is not None:
-            code_ptr = np.ascontiguousarray(c.code_offset_ptr.astype(np.uint64))
-            code = np.ascontiguousarray(c.code_offsets.astype(np.uint32))
-            if code.size == 0:
-                code = np.zeros(1, dtype=np.uint32)
-            self._keep += [code_ptr, code]
-        net = _abi.Network(
-            c.neuron_count, _abi.ptr(thr, c_float), _abi.ptr(win, c_uint64), _abi.ptr(sim, c_float),
-            _abi.ptr(refs, c_uint64), c.synapse_count, _abi.ptr(src, c_uint32),
-            _abi.ptr(tgt, c_uint32), _abi.ptr(w, c_float), _abi.ptr(mw, c_float),
-            _abi.ptr(dly, c_uint32), _abi.ptr(comp, c_uint8), _abi.ptr(rec, c_uint8),
-            _abi.ptr(pl, c_uint8), _abi.ptr(code_ptr, c_uint64), _abi.ptr(code, c_uint32))
         handle = c_void_p()
         _check(self.lib, self.lib.snncuda_sim_create(ctypes.byref(net), ctypes.byref(self.config),
                                                      ctypes.byref(handle)))
@@ -125,11 +178,7 @@ class Simulation:
 
     # -- stepping --------------------------------------------------------------
     def inject(self, neurons, ticks, weights) -> None:
-        n = np.ascontiguousarray(np.asarray(neurons, dtype=np.uint32).ravel())
-        t = np.ascontiguousarray(np.asarray(ticks, dtype=np.uint64).ravel())
-        w = np.ascontiguousarray(np.asarray(weights, dtype=np.float32).ravel())
-        if not (n.size == t.size == w.size):
-            raise ValueError("inject arrays must have equal length")
+        n, t, w = _inject_arrays(neurons, ticks, weights)
         if n.size == 0:
             return
         _check(self.lib, self.lib.snncuda_sim_inject(self.handle, n.size, _abi.ptr(n, c_uint32),
@@ -156,37 +205,12 @@ class Simulation:
         return bool(out.value)
 
     def neurons(self) -> Dict[str, np.ndarray]:
-        n = self.neuron_count
-        arrays = {
-            "membrane_potential": np.zeros(n, np.float32), "spike_count": np.zeros(n, np.uint64),
-            "last_fired_tick": np.zeros(n, np.int64), "last_active_tick": np.zeros(n, np.uint64),
-            "compartment_current": np.zeros(n * 4, np.float32),
-            "compartment_last_update": np.zeros(n * 4, np.uint64),
-            "compartment_tau": np.zeros(n * 4, np.float32),
-            "window_start_tick": np.zeros(n, np.uint64), "offset_count": np.zeros(n, np.uint64),
-            "learned_count": np.zeros(n, np.uint64), "match_count": np.zeros(n, np.uint64),
-            "last_match": np.zeros(n, np.uint8),
-        }
-        types = dict(_abi.NeuronState._fields_)
-        view = _abi.NeuronState(**{k: _abi.ptr(v, types[k]._type_) for k, v in arrays.items()})
+        arrays, view = _neuron_arrays(self.neuron_count)
         _check(self.lib, self.lib.snncuda_sim_read_neurons(self.handle, ctypes.byref(view)))
-        for k in ("compartment_current", "compartment_last_update", "compartment_tau"):
-            arrays[k] = arrays[k].reshape(n, 4)
-        return arrays
+        return _finish_neurons(arrays, self.neuron_count)
 
     def synapses(self) -> Dict[str, np.ndarray]:
-        s = self.synapse_count
-        arrays = {
-            "weight": np.zeros(s, np.float32), "last_pre_spike_tick": np.zeros(s, np.int64),
-            "last_post_spike_tick": np.zeros(s, np.int64), "pre_spike_count": np.zeros(s, np.uint64),
-            "plasticity_update_count": np.zeros(s, np.uint64),
-            "last_weight_delta": np.zeros(s, np.float32),
-            "code_window_start_tick": np.zeros(s, np.uint64),
-            "code_offset_count": np.zeros(s, np.uint64), "learned_code_count": np.zeros(s, np.uint64),
-            "code_match_count": np.zeros(s, np.uint64), "last_code_match": np.zeros(s, np.uint8),
-        }
-        types = dict(_abi.SynapseState._fields_)
-        view = _abi.SynapseState(**{k: _abi.ptr(v, types[k]._type_) for k, v in arrays.items()})
+        arrays, view = _synapse_arrays(self.synapse_count)
         _check(self.lib, self.lib.snncuda_sim_read_synapses(self.handle, ctypes.byref(view)))
         return arrays
 
@@ -226,6 +250,102 @@ class Simulation:
         if count:
             _check(self.lib, self.lib.snncuda_sim_read_raster(
                 self.handle, first, count, _abi.ptr(ticks, c_uint64), _abi.ptr(neurons, c_uint32)))
+        return ticks, neurons
+
+
+class Batch:
+    """Several independent networks advanced together in one handle (batched
+    form).  Network i keeps its own 0-based neuron and synapse indices and
+    evolves exactly as a Simulation of it alone would; stdp_enabled[i] is its
+    StdpConfig::enabled, the rest of `config` is shared."""
+
+    def __init__(self, connectomes: Sequence[Connectome], config: Optional[_abi.Config] = None,
+                 lib: Optional[ctypes.CDLL] = None, stdp_enabled: Optional[Sequence[bool]] = None):
+        self.lib = lib or backend()
+        self.config = config if config is not None else default_config(self.lib)
+        nets, keep = [], []
+        for c in connectomes:
+            c.validate()
+            net, k = _network_struct(c)
+            nets.append(net)
+            keep.append(k)
+        self.count = len(nets)
+        arr = (_abi.Network * max(self.count, 1))(*nets)
+        rule = None
+        if stdp_enabled is not None:
+            rule = np.ascontiguousarray(np.asarray([1 if x else 0 for x in stdp_enabled], dtype=np.int32))
+            if rule.size != self.count:
+                raise ValueError("stdp_enabled needs one entry per network")
+        handle = c_void_p()
+        _check(self.lib, self.lib.snncuda_batch_create(self.count, arr, _abi.ptr(rule, c_int32),
+                                                       ctypes.byref(self.config), ctypes.byref(handle)))
+        self.handle = handle
+        self.neuron_counts = [c.neuron_count for c in connectomes]
+        self.synapse_counts = [c.synapse_count for c in connectomes]
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.snncuda_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def inject(self, network: int, neurons, ticks, weights) -> None:
+        n, t, w = _inject_arrays(neurons, ticks, weights)
+        if n.size == 0:
+            return
+        _check(self.lib, self.lib.snncuda_batch_inject(self.handle, network, n.size, _abi.ptr(n, c_uint32),
+                                                       _abi.ptr(t, c_uint64), _abi.ptr(w, c_float)))
+
+    def run_until(self, inclusive_tick: int) -> None:
+        _check(self.lib, self.lib.snncuda_batch_run_until(self.handle, int(inclusive_tick)))
+
+    def set_plasticity(self, enabled: bool) -> None:
+        _check(self.lib, self.lib.snncuda_batch_set_plasticity(self.handle, 1 if enabled else 0))
+
+    def set_temporal_learning(self, enabled: bool) -> None:
+        _check(self.lib, self.lib.snncuda_batch_set_temporal_learning(self.handle, 1 if enabled else 0))
+
+    def counters(self, network: int) -> Dict[str, int]:
+        out = _abi.Counters()
+        _check(self.lib, self.lib.snncuda_batch_counters(self.handle, network, ctypes.byref(out)))
+        return {name: int(getattr(out, name)) for name, _ in _abi.Counters._fields_}
+
+    def neurons(self, network: int) -> Dict[str, np.ndarray]:
+        n = self.neuron_counts[network]
+        arrays, view = _neuron_arrays(n)
+        _check(self.lib, self.lib.snncuda_batch_read_neurons(self.handle, network, ctypes.byref(view)))
+        return _finish_neurons(arrays, n)
+
+    def synapses(self, network: int) -> Dict[str, np.ndarray]:
+        arrays, view = _synapse_arrays(self.synapse_counts[network])
+        _check(self.lib, self.lib.snncuda_batch_read_synapses(self.handle, network, ctypes.byref(view)))
+        return arrays
+
+    def digests(self) -> List[tuple]:
+        a = np.zeros(max(self.count, 1), np.uint64)
+        b = np.zeros(max(self.count, 1), np.uint64)
+        _check(self.lib, self.lib.snncuda_batch_state_digests(self.handle, _abi.ptr(a, c_uint64),
+                                                              _abi.ptr(b, c_uint64)))
+        return [(int(a[i]), int(b[i])) for i in range(self.count)]
+
+    def raster(self, network: int) -> tuple:
+        count = self.counters(network)["raster_count"]
+        ticks = np.zeros(count, np.uint64)
+        neurons = np.zeros(count, np.uint32)
+        if count:
+            _check(self.lib, self.lib.snncuda_batch_read_raster(
+                self.handle, network, 0, count, _abi.ptr(ticks, c_uint64), _abi.ptr(neurons, c_uint32)))
         return ticks, neurons
 
 
