@@ -49,7 +49,7 @@ KERNELS_PER_TICK = 10   # launch_tick in snncuda_gb300/csrc/kernels.cu
 # DRAM bytes (read + write) per launch of a kernel on the default stdp_100k
 # workload, from one ncu capture of this code (profiles/); reported as
 # roofline.traffic for the dominant kernel.
-MEASURED_TRAFFIC = {}
+MEASURED_TRAFFIC = {("stdp_100k", "k_events"): 159.0e6 + 96.6e6, ("stdp_100k", "k_process"): 55.3e6 + 0.1e6}
 
 # Algorithmic bytes of the two per-event kernels (device layout in
 # snncuda_gb300/csrc/engine.h), per synaptic event, per external event and
