@@ -216,6 +216,90 @@ def config_block(args, w):
             "parallelism": f"replicas x{args.gpus}"}
 
 
+def batch_members(count, nmin, nmax, ticks):
+    """Networks of the batched comparison: N log-uniform in [nmin, nmax],
+    fan-out uniform in {100..1000} (at most N), stdp_100k distributions
+    otherwise, seeds 1000 + i, the STDP rule on for even i."""
+    from snncuda_gb300 import synthetic
+    rng = np.random.default_rng(7)
+    out = []
+    for i in range(count):
+        n = int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax)))))
+        fan = int(min(n, rng.integers(100, 1001)))
+        w = synthetic.STDP_100K.scaled(name=f"member{i}", neurons=n, fanout=fan, ticks=ticks, seed=1000 + i,
+                                       weight_scale=0.01 * 1000 / fan, max_weight=0.01 * 1000 / fan)
+        out.append((w, i % 2 == 0))
+    return out
+
+
+def run_batched(args):
+    """Synaptic events/s of `--batched` networks advanced together in one
+    batch handle, against the same networks run one after another, one
+    handle each (the reference's one-propagator-per-network usage).  Both
+    legs time the tick loop only (networks built and drives injected before
+    the timed region) with CUDA events; the batch's per-network digests must
+    equal the solo runs'."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from snncuda_gb300 import synthetic
+    from snncuda_gb300.simulation import Batch, Simulation, backend
+    lib = backend()
+    nmin, nmax = (int(x) for x in args.batch_neurons.split(","))
+    T = args.batch_ticks
+    members = batch_members(args.batched, nmin, nmax, T)
+    nets = [synthetic.build_network(w) for w, _ in members]
+    drives = [synthetic.build_drive(w, T) for w, _ in members]
+    stream = torch.cuda.Stream()
+    warm = min(50, T // 4)
+
+    def cfg_for(rule):
+        c = sim_config(lib, members[0][0], cuda_stream=stream.cuda_stream)
+        c.stdp_enabled = 1 if rule else 0
+        return c
+
+    def timed(run):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    # batched leg
+    b = Batch(nets, cfg_for(True), lib, stdp_enabled=[r for _, r in members])
+    for i, d in enumerate(drives):
+        b.inject(i, *d)
+    b.run_until(warm - 1)
+    before = [b.counters(i)["synaptic_events"] for i in range(len(nets))]
+    ms_batch = timed(lambda: b.run_until(T - 1))
+    ev_batch = sum(b.counters(i)["synaptic_events"] - before[i] for i in range(len(nets)))
+    dig_batch = b.digests()
+    b.close()
+    # sequential leg
+    ms_seq, ev_seq, dig_seq = 0.0, 0, []
+    for (w, rule), net, d in zip(members, nets, drives):
+        sim = Simulation(net, cfg_for(rule), lib)
+        sim.inject(*d)
+        sim.run_until(warm - 1)
+        c0 = sim.counters()["synaptic_events"]
+        ms_seq += timed(lambda: sim.run_until(T - 1))
+        ev_seq += sim.counters()["synaptic_events"] - c0
+        dig_seq.append(sim.digest())
+        sim.close()
+    return {
+        "metric": METRIC, "value": ev_batch / (ms_batch / 1e3), "unit": UNIT, "n_gpus": 1,
+        "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batched x{len(nets)}", "neurons": [w.neurons for w, _ in members],
+                   "fanout": [w.fanout for w, _ in members], "ticks": T, "timed_ticks": T - warm,
+                   "stdp_rule_on_even": True, "synapses_total": int(sum(w.synapses for w, _ in members))},
+        "ms_batched": ms_batch, "sequential": {"value": ev_seq / (ms_seq / 1e3), "ms": ms_seq},
+        "speedup_vs_sequential": (ev_batch / ms_batch) / (ev_seq / ms_seq) if ev_seq else None,
+        "events": ev_batch, "parity_per_network": dig_batch == dig_seq,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -231,7 +315,14 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--batched", type=int, default=0,
+                    help="batched form: this many networks in one handle vs one handle per network")
+    ap.add_argument("--batch-ticks", type=int, default=500)
+    ap.add_argument("--batch-neurons", type=str, default="1000,20000", help="log-uniform range of N")
     args = ap.parse_args()
+    if args.batched:
+        print(json.dumps(run_batched(args)), flush=True)
+        return
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
 
