@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "pack.h"
 #include "snncuda_gb300.h"
 
 using namespace snngb;
@@ -275,14 +276,13 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     if (cfg.timing_wheel_slots == 0)
         throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "Spike scheduler timing wheel must have at least one slot");
     if (N >= (1u << 31)) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "at most 2^31-1 neurons");
-    if (S >= 0xFFFFFFFFull) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "at most 2^32-2 synapses per simulation");
+    if (S >= (1ull << 31)) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "at most 2^31-1 synapses per simulation");
     if (N > 0 && (!net->threshold || !net->pattern_window_ticks || !net->similarity_threshold ||
                   !net->max_reference_patterns))
         throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "neuron parameter arrays are required");
     if (S > 0 && (!net->source || !net->target || !net->weight || !net->max_weight || !net->delay_ticks ||
                   !net->compartment || !net->receptor || !net->plasticity_enabled))
         throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "synapse arrays are required");
-    const bool has_codes = net->code_offset_ptr != nullptr && net->code_offsets != nullptr;
 
     check(cudaGetDevice(&sim->device), "cudaGetDevice");
     if (cfg.cuda_stream != nullptr) {
@@ -299,35 +299,23 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.S = S;
     e.min_weight = cfg.min_weight;
 
-    // ---- validation + target-major order (stable in Connectome order) ----
-    std::vector<uint64_t> in_ptr(static_cast<size_t>(N) + 1, 0);
-    uint32_t max_expected = 2;
-    for (uint64_t s = 0; s < S; ++s) {
-        if (net->source[s] >= N || net->target[s] >= N)
-            throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "synapse endpoint out of range");
-        if (net->compartment[s] > 3 || net->receptor[s] > 3)
-            throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "compartment/receptor out of range");
-        if (net->delay_ticks[s] > kMetaDelayMask)
-            throw_fail(SNNCUDA_ERR_UNSUPPORTED, "delays above 65535 ticks are not supported");
-        const uint64_t k = has_codes ? net->code_offset_ptr[s + 1] - net->code_offset_ptr[s] : 1;
-        if (k > static_cast<uint64_t>(kMaxExpected))
-            throw_fail(SNNCUDA_ERR_UNSUPPORTED, "more than 8 spike-code offsets per synapse");
-        max_expected = std::max<uint32_t>(max_expected, static_cast<uint32_t>(std::max<uint64_t>(2, k)));
-        in_ptr[net->target[s] + 1] += 1;
-    }
-    for (uint32_t n = 0; n < N; ++n) in_ptr[n + 1] += in_ptr[n];
-    std::vector<uint32_t> tm_of_c(S);
-    sim->c_of_tm.assign(S, 0);
+    // ---- synapse side, packed on the device: validation, target-major
+    // order, synapse records, pre-expanded outgoing events ----
+    PackOut pk;
     {
-        std::vector<uint64_t> cursor(in_ptr.begin(), in_ptr.end() - 1);
-        for (uint64_t s = 0; s < S; ++s) {
-            const uint64_t tm = cursor[net->target[s]]++;
-            tm_of_c[s] = static_cast<uint32_t>(tm);
-            sim->c_of_tm[tm] = static_cast<uint32_t>(s);
-        }
+        std::string msg;
+        const int rc = pack_network_device(net, cfg.max_weight, sim->stream, sim->owned, pk, msg);
+        if (rc != SNNCUDA_OK) throw_fail(rc, msg);
     }
+    std::vector<uint64_t>& in_ptr = pk.in_ptr;
+    const uint32_t max_expected = pk.max_expected;
     e.code_stride = max_expected;
-    sim->tm_of_c = tm_of_c;
+    sim->c_of_tm.resize(S);
+    sim->tm_of_c.resize(S);
+    if (S > 0) {
+        check(cudaMemcpyAsync(sim->c_of_tm.data(), pk.c_of_tm_d, S * 4, cudaMemcpyDeviceToHost, sim->stream), "copy");
+        check(cudaMemcpyAsync(sim->tm_of_c.data(), pk.tm_of_c_d, S * 4, cudaMemcpyDeviceToHost, sim->stream), "copy");
+    }
 
     // ---- neuron parameters and temporal storage ----
     sim->nparam.resize(N);
@@ -359,66 +347,10 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
             lcode_total += (in_ptr[n + 1] - in_ptr[n]) * refs * max_expected;
     }
 
-    // ---- synapse records, target-major ----
-    std::vector<SynA> syna(S);
-    for (uint64_t s = 0; s < S; ++s) {
-        SynA& a = syna[tm_of_c[s]];
-        a.weight = net->weight[s];
-        a.last_pre1 = 0;
-        a.last_post1 = 0;
-        const uint64_t k = has_codes ? net->code_offset_ptr[s + 1] - net->code_offset_ptr[s] : 1;
-        const uint32_t expected = static_cast<uint32_t>(std::max<uint64_t>(2, k == 0 ? 1 : k));
-        a.meta = net->delay_ticks[s] | (static_cast<uint32_t>(net->compartment[s]) << kMetaCompShift) |
-                 (static_cast<uint32_t>(net->receptor[s]) << kMetaRecShift) |
-                 (static_cast<uint32_t>(net->plasticity_enabled[s] ? 1 : 0) << kMetaPlasticBit) |
-                 (expected << kMetaExpectedShift);
-        // std::min(config.max_weight, synapse.max_weight) (STDP.cpp:38)
-        a.clamp_hi = net->max_weight[s] < cfg.max_weight ? net->max_weight[s] : cfg.max_weight;
-        a.updates = 0;
-        a.last_delta = 0.0F;
-        a.post_cnt = 0;
-    }
-
-    // ---- pre-expanded outgoing events, grouped by delivery delay class ----
-    // delivery = tick + delay + offset, clamped to tick + 1 (SpikeScheduler.cpp:17-19)
-    std::vector<uint64_t> out_ptr(static_cast<size_t>(N) + 1, 0);
-    for (uint64_t s = 0; s < S; ++s) out_ptr[net->source[s] + 1] += 1;
-    for (uint32_t n = 0; n < N; ++n) out_ptr[n + 1] += out_ptr[n];
-    std::vector<uint64_t> out_list(S);
-    {
-        std::vector<uint64_t> cursor(out_ptr.begin(), out_ptr.end() - 1);
-        for (uint64_t s = 0; s < S; ++s) out_list[cursor[net->source[s]]++] = s;
-    }
-    auto codes_of = [&](uint64_t s, const uint32_t*& ptr, uint64_t& count) {
-        static const uint32_t zero = 0;
-        if (has_codes && net->code_offset_ptr[s + 1] > net->code_offset_ptr[s]) {
-            ptr = net->code_offsets + net->code_offset_ptr[s];
-            count = net->code_offset_ptr[s + 1] - net->code_offset_ptr[s];
-        } else {
-            ptr = &zero;
-            count = 1;
-        }
-    };
-    std::map<uint64_t, uint32_t> class_of;
-    uint64_t pre_total = 0;
-    for (uint64_t s = 0; s < S; ++s) {
-        const uint32_t* c;
-        uint64_t k;
-        codes_of(s, c, k);
-        for (uint64_t j = 0; j < k; ++j) {
-            const uint64_t d = std::max<uint64_t>(1, static_cast<uint64_t>(net->delay_ticks[s]) + c[j]);
-            class_of.emplace(d, 0);
-        }
-        pre_total += k;
-    }
-    if (class_of.size() > kMaxClasses)
-        throw_fail(SNNCUDA_ERR_UNSUPPORTED, "more than 256 distinct delivery delays");
-    const uint32_t D = static_cast<uint32_t>(class_of.size());
-    std::vector<uint32_t> cls_delta;
-    for (auto& kv : class_of) {
-        kv.second = static_cast<uint32_t>(cls_delta.size());
-        cls_delta.push_back(static_cast<uint32_t>(kv.first));
-    }
+    // ---- delivery delay classes and the wheel ----
+    const std::vector<uint32_t>& cls_delta = pk.cls_delta;
+    const uint32_t D = static_cast<uint32_t>(cls_delta.size());
+    const uint64_t pre_total = pk.pre_total;
     const uint64_t max_delta = cls_delta.empty() ? 1 : cls_delta.back();
     uint32_t W = 2;
     while (W <= max_delta) W <<= 1;
@@ -426,42 +358,6 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.W = W;
     e.wmask = W - 1;
     e.D = D;
-    std::vector<unsigned long long> pre_base(N);
-    std::vector<uint32_t> pre_off(static_cast<size_t>(N) * (D + 1), 0);
-    std::vector<unsigned long long> pre_ev(pre_total > 0 ? pre_total : 1);
-    {
-        uint64_t pos = 0;
-        std::vector<uint32_t> cnt(D + 1);
-        for (uint32_t n = 0; n < N; ++n) {
-            pre_base[n] = pos;
-            std::fill(cnt.begin(), cnt.end(), 0);
-            for (uint64_t i = out_ptr[n]; i < out_ptr[n + 1]; ++i) {
-                const uint64_t s = out_list[i];
-                const uint32_t* c;
-                uint64_t k;
-                codes_of(s, c, k);
-                for (uint64_t j = 0; j < k; ++j)
-                    cnt[class_of[std::max<uint64_t>(1, static_cast<uint64_t>(net->delay_ticks[s]) + c[j])] + 1] += 1;
-            }
-            uint32_t* row = &pre_off[static_cast<size_t>(n) * (D + 1)];
-            for (uint32_t d = 0; d < D; ++d) row[d + 1] = row[d] + cnt[d + 1];
-            if (row[D] >= (1u << 30)) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "too many outgoing events per neuron");
-            std::vector<uint32_t> fill(row, row + D);
-            for (uint64_t i = out_ptr[n]; i < out_ptr[n + 1]; ++i) {
-                const uint64_t s = out_list[i];
-                const uint32_t* c;
-                uint64_t k;
-                codes_of(s, c, k);
-                for (uint64_t j = 0; j < k; ++j) {
-                    const uint32_t cls =
-                        class_of[std::max<uint64_t>(1, static_cast<uint64_t>(net->delay_ticks[s]) + c[j])];
-                    pre_ev[pos + fill[cls]++] =
-                        (static_cast<unsigned long long>(tm_of_c[s]) << 32) | net->target[s];
-                }
-            }
-            pos += row[D];
-        }
-    }
 
     // ---- capacities ----
     uint64_t slot_cap = cfg.slot_event_capacity;
@@ -485,18 +381,13 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
 
     // ---- device allocation ----
     auto& own = sim->owned;
-    auto* d_in_ptr = dalloc<unsigned long long>(own, N + 1);
     auto* d_nparam = dalloc<NeuronParam>(own, N);
     e.nrec = dalloc<NeuronRec>(own, N);
     e.ntp = dalloc<NeuronTp>(own, N);
     e.cand = dalloc<unsigned long long>(own, cand_total);
     e.refmeta = dalloc<RefMeta>(own, meta_total);
     e.ring = dalloc<unsigned long long>(own, ring_total);
-    e.syn = dalloc<SynAB>(own, S);
     e.lcode = dalloc<uint16_t>(own, lcode_total);
-    auto* d_pre_base = dalloc<unsigned long long>(own, N);
-    auto* d_pre_off = dalloc<uint32_t>(own, static_cast<size_t>(N) * (D + 1));
-    auto* d_pre_ev = dalloc<unsigned long long>(own, pre_ev.size());
     auto* d_cls = dalloc<uint32_t>(own, D);
     e.wheel = dalloc<unsigned long long>(own, static_cast<size_t>(W) * slot_cap);
     e.slot_count = dalloc<uint32_t>(own, W);
@@ -533,24 +424,11 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     auto zero = [&](void* dst, size_t bytes) {
         if (bytes) check(cudaMemsetAsync(dst, 0, bytes, st), "memset");
     };
-    h2d(d_in_ptr, in_ptr.data(), in_ptr.size() * sizeof(uint64_t));
     h2d(d_nparam, sim->nparam.data(), sim->nparam.size() * sizeof(NeuronParam));
     // NeuronState defaults (NeuronStateCache.h:15-45): every compartment tau 5 (code 0).
     zero(e.nrec, sizeof(NeuronRec) * N);
     zero(e.ntp, sizeof(NeuronTp) * N);
-    // SynA images go through a temporary buffer into the 64-byte records
-    struct Upload {
-        std::vector<void*> v;
-        ~Upload() {
-            for (void* q : v) cudaFree(q);
-        }
-    } upload;
-    SynA* d_syna_img = dalloc<SynA>(upload.v, S);
-    h2d(d_syna_img, syna.data(), syna.size() * sizeof(SynA));
     zero(e.lcode, sizeof(uint16_t) * lcode_total);
-    h2d(d_pre_base, pre_base.data(), pre_base.size() * sizeof(unsigned long long));
-    h2d(d_pre_off, pre_off.data(), pre_off.size() * sizeof(uint32_t));
-    h2d(d_pre_ev, pre_ev.data(), pre_ev.size() * sizeof(unsigned long long));
     h2d(d_cls, cls_delta.data(), cls_delta.size() * sizeof(uint32_t));
     zero(e.slot_count, sizeof(uint32_t) * W);
     zero(e.cnt, sizeof(uint32_t) * N);
@@ -565,18 +443,18 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     ts.stdp_enabled = cfg.stdp_enabled ? 1 : 0;
     ts.temporal_enabled = cfg.temporal_learning_enabled ? 1 : 0;
     h2d(e.ts, &ts, sizeof(ts));
-    e.in_ptr = d_in_ptr;
+    e.in_ptr = pk.in_ptr_d;
     e.nparam = d_nparam;
-    e.pre_base = d_pre_base;
-    e.pre_off = d_pre_off;
-    e.pre_ev = d_pre_ev;
+    e.syn = pk.syn;
+    e.pre_base = pk.pre_base;
+    e.pre_off = pk.pre_off;
+    e.pre_ev = pk.pre_ev;
     e.cls_delta = d_cls;
     e.tab.decay = d_decay;
     e.tab.decay_len = decay_len;
     e.tab.ltp = d_ltp;
     e.tab.ltd = d_ltd;
     e.tab.stdp_len = static_cast<uint32_t>(ltp.size());
-    launch_init_syn(e, d_syna_img, st);
     configure_kernels();
     check(cudaGetLastError(), "init launch");
     sim->in_ptr = std::move(in_ptr);
