@@ -161,8 +161,13 @@ def workload_from_args(args):
     return w
 
 
+SLOT_CAPACITY = 0  # --slot-capacity
+
+
 def sim_config(lib, w, **extra):
     from snncuda_gb300.simulation import default_config
+    if SLOT_CAPACITY:
+        extra.setdefault("slot_event_capacity", SLOT_CAPACITY)
     cfg = default_config(lib, **extra)
     cfg.stdp_enabled = 1 if w.stdp_enabled else 0
     cfg.max_weight = 1.0  # StdpConfig clip [0, 1]; synapses carry their own max_weight
@@ -315,6 +320,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--slot-capacity", type=int, default=0, help="events one wheel slot holds (0 = default)")
     ap.add_argument("--batched", type=int, default=0,
                     help="batched form: this many networks in one handle vs one handle per network")
     ap.add_argument("--batch-ticks", type=int, default=500)
@@ -325,6 +331,8 @@ def main():
         return
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
+    global SLOT_CAPACITY
+    SLOT_CAPACITY = args.slot_capacity
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

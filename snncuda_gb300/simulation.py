@@ -70,17 +70,17 @@ def _network_struct(c: Connectome):
     """snncuda_network view of a Connectome plus the arrays it points into
     (keep them alive until the create call returns)."""
     keep = [np.ascontiguousarray(a) for a in (
-        c.threshold.astype(np.float32), c.pattern_window_ticks.astype(np.uint64),
-        c.similarity_threshold.astype(np.float32), c.max_reference_patterns.astype(np.uint64),
-        c.source.astype(np.uint32), c.target.astype(np.uint32), c.weight.astype(np.float32),
-        c.max_weight.astype(np.float32), c.delay_ticks.astype(np.uint32),
-        c.compartment.astype(np.uint8), c.receptor.astype(np.uint8),
-        c.plasticity_enabled.astype(np.uint8))]
+        c.threshold.astype(np.float32, copy=False), c.pattern_window_ticks.astype(np.uint64, copy=False),
+        c.similarity_threshold.astype(np.float32, copy=False), c.max_reference_patterns.astype(np.uint64, copy=False),
+        c.source.astype(np.uint32, copy=False), c.target.astype(np.uint32, copy=False), c.weight.astype(np.float32, copy=False),
+        c.max_weight.astype(np.float32, copy=False), c.delay_ticks.astype(np.uint32, copy=False),
+        c.compartment.astype(np.uint8, copy=False), c.receptor.astype(np.uint8, copy=False),
+        c.plasticity_enabled.astype(np.uint8, copy=False))]
     (thr, win, sim, refs, src, tgt, w, mw, dly, comp, rec, pl) = keep
     code_ptr = code = None
     if c.code_offset_ptr is not None:
-        code_ptr = np.ascontiguousarray(c.code_offset_ptr.astype(np.uint64))
-        code = np.ascontiguousarray(c.code_offsets.astype(np.uint32))
+        code_ptr = np.ascontiguousarray(c.code_offset_ptr.astype(np.uint64, copy=False))
+        code = np.ascontiguousarray(c.code_offsets.astype(np.uint32, copy=False))
         if code.size == 0:
             code = np.zeros(1, dtype=np.uint32)
         keep += [code_ptr, code]
