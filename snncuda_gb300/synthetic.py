@@ -29,7 +29,10 @@ tick):
   recog_1m     1,000,000 neurons, fan-out 1,000 (1e9 synapses), stdp_100k
                distributions, plus 16 fixed 8-offset codes (offsets in
                U{0..31}) presented every 64 ticks to the first half of the
-               neurons over the 5 Hz background, 2,000 ticks.
+               neurons over the 5 Hz background, 2,000 ticks.  Each code
+               input has weight 0.1: at 0.25, coinciding offsets make the
+               stimulated half fire in the same tick and the network runs
+               away (measured on a 10,000-neuron version).
 Any of them can be scaled down (neurons, fan-out, ticks) for parity tests.
 """
 
@@ -147,7 +150,7 @@ STDP_100K = Workload("stdp_100k", 100_000, 0.8, 1000, 1, weight_scale=0.01, code
                      pattern_window_ticks=32, similarity_threshold=0.9, max_reference_patterns=1,
                      drive_rate_hz=5.0, ticks=10_000, seed=1, stdp_enabled=True)
 RECOG_1M = STDP_100K.scaled(name="recog_1m", neurons=1_000_000, ticks=2000, seed=2,
-                            stimulus_codes=16)
+                            stimulus_codes=16, stimulus_weight=0.1)
 WORKLOADS = {w.name: w for w in (PLAIN_1K, STDP_100K, RECOG_1M)}
 
 

@@ -323,7 +323,8 @@ def sc_toggles():
 
 def sc_recog_small():
     """recog_1m distributions (temporal-code stimulus) at 2,000 neurons."""
-    w = synthetic.RECOG_1M.scaled(neurons=2000, fanout=100, weight_scale=0.06, max_weight=1.0, seed=9)
+    w = synthetic.RECOG_1M.scaled(neurons=2000, fanout=100, weight_scale=0.06, max_weight=1.0, seed=9,
+                                  stimulus_weight=0.25)
     s = _synthetic(w, 256, STDP_CFG)
     s.default_processor = False
     return s

@@ -59,7 +59,8 @@ def test_stdp_network_matches_oracle(gpu_lib, port_lib, neurons, fanout, ticks, 
 
 
 def test_recognition_network_with_toggles_matches_oracle(gpu_lib, port_lib):
-    w = synthetic.RECOG_1M.scaled(neurons=10_000, fanout=200, weight_scale=0.03, max_weight=1.0, seed=23)
+    w = synthetic.RECOG_1M.scaled(neurons=10_000, fanout=200, weight_scale=0.03, max_weight=1.0, seed=23,
+                                  stimulus_weight=0.25)
     net = synthetic.build_network(w)
     _compare(gpu_lib, port_lib, net, synthetic.build_drive(w, 300), 300, STDP_CFG,
              toggles=[(99, "stdp", False), (149, "temporal", False), (199, "stdp", True),
