@@ -41,6 +41,10 @@ import numpy as np
 
 ROOT = pathlib.Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
+if "--serve" in sys.argv:
+    # one hardware work queue per concurrently running job's stream (read at
+    # CUDA context creation; the default of 8 would serialize the streams)
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = "synaptic_events_per_s"
 UNIT = "events/s"
@@ -305,6 +309,102 @@ def run_batched(args):
     }
 
 
+def serving_jobs(args):
+    """Arrival times (Poisson, seed 7) and workloads of the serving run: N
+    log-uniform, fan-out uniform in {200..1000} (at most N), ticks uniform,
+    recog_1m distributions (the 16-code stimulus over a 5 Hz background)
+    with the initial and per-synapse max weights scaled by 1000 / fan-out."""
+    from snncuda_gb300 import synthetic
+    rng = np.random.default_rng(7)
+    nmin, nmax = (int(x) for x in args.serve_neurons.split(","))
+    tmin, tmax = (int(x) for x in args.serve_ticks.split(","))
+    t, jobs = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / args.serve_rate)
+        if t > args.serve_seconds:
+            break
+        n = int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax)))))
+        fan = int(min(n, rng.integers(200, 1001)))
+        ticks = int(rng.integers(tmin, tmax + 1))
+        w = synthetic.RECOG_1M.scaled(name=f"job{len(jobs)}", neurons=n, fanout=fan, ticks=ticks,
+                                      seed=7000 + len(jobs), weight_scale=0.01 * 1000 / fan,
+                                      max_weight=0.01 * 1000 / fan)
+        jobs.append((t, w))
+    return jobs
+
+
+def run_serving(args):
+    """Serving run: jobs arrive as a Poisson process and are submitted to one
+    Server (device-memory budget, jobs advanced side by side on their own
+    streams) at their arrival times; latency = completion - submission on the
+    server's clock.  Networks and drives are generated before the clock
+    starts.  A few of the smallest jobs are then served again with state
+    digests and compared with solo runs (solo-vs-mix equality)."""
+    import __graft_entry__
+    __graft_entry__.build()
+    from snncuda_gb300 import synthetic
+    from snncuda_gb300.simulation import Server, Simulation, backend
+    lib = backend()
+    plan = serving_jobs(args)
+    built = [(t, w, synthetic.build_network(w), synthetic.build_drive(w, w.ticks)) for t, w in plan]
+
+    def cfg():
+        return sim_config(lib, plan[0][1])
+
+    sv = Server(memory_budget_bytes=int(args.serve_budget_gb * (1 << 30)), max_running=args.serve_running,
+                slice_ticks=args.serve_slice, lib=lib)
+    ids = [None] * len(built)
+    start = time.perf_counter()
+    nxt = 0
+    while True:
+        now = time.perf_counter() - start
+        while nxt < len(built) and built[nxt][0] <= now:
+            _, w, net, drive = built[nxt]
+            ids[nxt] = sv.submit(net, cfg(), drive, w.ticks)
+            nxt += 1
+        active = sv.step()
+        if nxt == len(built) and active == 0:
+            break
+        if active == 0:
+            time.sleep(0.0005)
+    wall = time.perf_counter() - start
+    res = [sv.job(j) for j in ids]
+    sv.close()
+    failed = [i for i, r in enumerate(res) if r["state"] != 2]
+    lat = np.array([r["finished_s"] - r["submitted_s"] for r in res if r["state"] == 2])
+    events = sum(r["counters"]["synaptic_events"] for r in res if r["state"] == 2)
+    first = min(r["submitted_s"] for r in res)
+    last = max(r["finished_s"] for r in res)
+    # solo-vs-mix on the three smallest jobs
+    small = sorted(range(len(built)), key=lambda i: built[i][1].synapses)[:3]
+    sv2 = Server(digests=True, lib=lib)
+    mix = [sv2.submit(built[i][2], cfg(), built[i][3], built[i][1].ticks) for i in small]
+    while sv2.step():
+        pass
+    mixed = [sv2.job(j)["digest"] for j in mix]
+    sv2.close()
+    solo = []
+    for i in small:
+        sim = Simulation(built[i][2], cfg(), lib)
+        sim.inject(*built[i][3])
+        sim.run_until(built[i][1].ticks - 1)
+        solo.append(sim.digest())
+        sim.close()
+    return {
+        "metric": METRIC, "value": events / (last - first), "unit": UNIT, "n_gpus": 1, "higher_is_better": True,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "serving", "jobs": len(built), "arrival_rate_per_s": args.serve_rate,
+                   "arrival_seconds": args.serve_seconds, "neurons": args.serve_neurons,
+                   "ticks": args.serve_ticks, "budget_gb": args.serve_budget_gb,
+                   "synapses_total": int(sum(w.synapses for _, w, _, _ in built))},
+        "latency_s": {"p50": float(np.percentile(lat, 50)) if lat.size else None,
+                      "p99": float(np.percentile(lat, 99)) if lat.size else None,
+                      "max": float(lat.max()) if lat.size else None},
+        "events": int(events), "wall_s": wall, "failed_jobs": failed,
+        "solo_vs_mix_equal": mixed == solo,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -325,7 +425,18 @@ def main():
                     help="batched form: this many networks in one handle vs one handle per network")
     ap.add_argument("--batch-ticks", type=int, default=500)
     ap.add_argument("--batch-neurons", type=str, default="1000,20000", help="log-uniform range of N")
+    ap.add_argument("--serve", action="store_true", help="serving: Poisson arrivals under a memory budget")
+    ap.add_argument("--serve-rate", type=float, default=4.0, help="job arrivals per second")
+    ap.add_argument("--serve-seconds", type=float, default=15.0, help="arrival window")
+    ap.add_argument("--serve-neurons", type=str, default="10000,100000", help="log-uniform range of N")
+    ap.add_argument("--serve-ticks", type=str, default="500,2000", help="uniform range of ticks per job")
+    ap.add_argument("--serve-budget-gb", type=float, default=120.0)
+    ap.add_argument("--serve-slice", type=int, default=32, help="ticks per job and scheduling round")
+    ap.add_argument("--serve-running", type=int, default=32, help="jobs advanced side by side")
     args = ap.parse_args()
+    if args.serve:
+        print(json.dumps(run_serving(args)), flush=True)
+        return
     if args.batched:
         print(json.dumps(run_batched(args)), flush=True)
         return

@@ -243,6 +243,49 @@ int snncuda_batch_state_digests(snncuda_batch* batch, uint64_t* neuron_digests, 
 int snncuda_batch_read_raster(snncuda_batch* batch, uint32_t network, uint64_t first, uint64_t count,
                               uint64_t* ticks, uint32_t* neurons);
 
+/* ---- serving: jobs admitted under a device-memory budget -----------------
+ * No counterpart in the reference, whose per-request path is one
+ * NetworkPropagator (or CudaInferenceSession) built and run per request
+ * (CudaBackend.h:97-126) with an LRU of neuron states for what does not fit
+ * (NeuronStateCache.cpp:22-43).  A server takes jobs (a network, its
+ * config, its injections, a tick count), admits them in submission order
+ * while their estimated device bytes fit the budget, and advances every
+ * admitted job by `slice_ticks` per scheduling round, each on its own CUDA
+ * stream, so the GPU runs many jobs at once; a finished job's memory goes
+ * back to the budget.  Every job's results equal a solo run of it.
+ * Single host thread; the caller drives it with snncuda_server_step. */
+typedef struct snncuda_server snncuda_server;
+typedef struct snncuda_server_config {
+    uint64_t memory_budget_bytes;  /* device bytes running jobs may hold (0 = 120 GB) */
+    uint32_t max_running;          /* jobs advanced side by side (0 = 64) */
+    uint32_t slice_ticks;          /* ticks per job and scheduling round (0 = 64) */
+    int32_t digests;               /* compute state digests of finished jobs */
+} snncuda_server_config;
+int snncuda_server_create(const snncuda_server_config* config, snncuda_server** out);
+int snncuda_server_destroy(snncuda_server* server);
+/* Queues a job that runs ticks 0 .. ticks-1.  The network's arrays are read
+ * when the job is admitted and must stay valid until then; the injections
+ * are copied.  *job_id numbers jobs from 0 in submission order. */
+int snncuda_server_submit(snncuda_server* server, const snncuda_network* network, const snncuda_config* config,
+                          uint64_t inject_count, const uint32_t* neurons, const uint64_t* ticks,
+                          const float* weights, uint64_t run_ticks, uint64_t* job_id);
+/* One scheduling round: finished slices are checked, finished jobs retired,
+ * the next slice of every running job enqueued, then queued jobs admitted
+ * while they fit.  *active = jobs queued or running afterwards. */
+int snncuda_server_step(snncuda_server* server, uint32_t* active);
+typedef struct snncuda_job_result {
+    int32_t state;                 /* 0 queued, 1 running, 2 done, 3 failed */
+    int32_t error;                 /* SNNCUDA_ERR_* of a failed job */
+    snncuda_counters counters;     /* of a finished job */
+    uint64_t neuron_digest, synapse_digest;  /* when config.digests */
+    uint64_t device_bytes;         /* the admission estimate */
+    double submitted_s, admitted_s, finished_s;  /* seconds since server creation */
+} snncuda_job_result;
+int snncuda_server_job(snncuda_server* server, uint64_t job_id, snncuda_job_result* out);
+/* Device bytes a simulation of `network` under `config` holds at most
+ * (creation included); the admission estimate of the server. */
+int snncuda_sim_estimate_bytes(const snncuda_network* network, const snncuda_config* config, uint64_t* bytes);
+
 /* ---- engine extension: per-kernel device time ----------------------------
  * No counterpart in the reference (which times the whole tick loop on the
  * host clock, spike_throughput_benchmark.cpp:137-140).  Processes ticks like

@@ -7,7 +7,7 @@ This package holds the host-side mirror of the reference interface.
 
 from .connectome import (AMPA, APICAL, BASAL, GABA_A, GABA_B, INHIBITORY, NMDA, SOMA, Connectome,
                          ExplicitConnection, NetworkBuilder, NeuronParams, Projection)
-from .simulation import (BACKEND_LIBRARY, Batch, NetworkPropagator, SNNCudaError, Simulation, backend,
+from .simulation import (BACKEND_LIBRARY, Batch, NetworkPropagator, SNNCudaError, Server, Simulation, backend,
                          default_config)
 
 
@@ -24,6 +24,6 @@ def cuda_available() -> bool:
 __all__ = [
     "AMPA", "APICAL", "BASAL", "GABA_A", "GABA_B", "INHIBITORY", "NMDA", "SOMA", "Connectome",
     "ExplicitConnection", "NetworkBuilder", "NeuronParams", "Projection", "BACKEND_LIBRARY",
-    "Batch", "NetworkPropagator", "SNNCudaError", "Simulation", "backend", "default_config", "version",
+    "Batch", "NetworkPropagator", "SNNCudaError", "Server", "Simulation", "backend", "default_config", "version",
     "cuda_available",
 ]

@@ -79,6 +79,29 @@ class Counters(Structure):
     ]
 
 
+class ServerConfig(Structure):
+    _fields_ = [
+        ("memory_budget_bytes", c_uint64),
+        ("max_running", c_uint32),
+        ("slice_ticks", c_uint32),
+        ("digests", c_int32),
+    ]
+
+
+class JobResult(Structure):
+    _fields_ = [
+        ("state", c_int32),
+        ("error", c_int32),
+        ("counters", Counters),
+        ("neuron_digest", c_uint64),
+        ("synapse_digest", c_uint64),
+        ("device_bytes", c_uint64),
+        ("submitted_s", ctypes.c_double),
+        ("admitted_s", ctypes.c_double),
+        ("finished_s", ctypes.c_double),
+    ]
+
+
 class NeuronState(Structure):
     _fields_ = [
         ("membrane_potential", POINTER(c_float)),
@@ -163,6 +186,13 @@ _SIGNATURES = {
     "snncuda_batch_state_digests": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64)]),
     "snncuda_batch_read_raster": (c_int, [c_void_p, c_uint32, c_uint64, c_uint64, POINTER(c_uint64),
                                           POINTER(c_uint32)]),
+    "snncuda_server_create": (c_int, [POINTER(ServerConfig), POINTER(c_void_p)]),
+    "snncuda_server_destroy": (c_int, [c_void_p]),
+    "snncuda_server_submit": (c_int, [c_void_p, POINTER(Network), POINTER(Config), c_uint64, POINTER(c_uint32),
+                                      POINTER(c_uint64), POINTER(c_float), c_uint64, POINTER(c_uint64)]),
+    "snncuda_server_step": (c_int, [c_void_p, POINTER(c_uint32)]),
+    "snncuda_server_job": (c_int, [c_void_p, c_uint64, POINTER(JobResult)]),
+    "snncuda_sim_estimate_bytes": (c_int, [POINTER(Network), POINTER(Config), POINTER(c_uint64)]),
     "snncuda_group_events": (c_int, [c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]),
     "snncuda_group_events_static": (c_int, [c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]),
 }

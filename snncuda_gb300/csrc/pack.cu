@@ -274,7 +274,7 @@ int pack_network_device(const snncuda_network* net, float cfg_max_weight, cudaSt
     };
     auto persist = [&](size_t bytes) -> void* {
         void* p = nullptr;
-        if (cudaMalloc(&p, bytes ? bytes : 1) != cudaSuccess) return nullptr;
+        if (cudaMallocAsync(&p, bytes ? bytes : 1, st) != cudaSuccess) return nullptr;
         owned.push_back(p);
         return p;
     };

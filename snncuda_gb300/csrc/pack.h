@@ -29,8 +29,8 @@ struct PackOut {
 };
 
 // Validates the synapse arrays of `net` and builds the engine's synapse-side
-// layout on the device (stream `st`).  Persistent buffers are cudaMalloc'ed
-// and appended to `owned`.  Returns SNNCUDA_OK or an SNNCUDA_ERR_* code with
+// layout on the device (stream `st`).  Persistent buffers are allocated
+// stream-ordered on `st` (cudaMallocAsync) and appended to `owned`.  Returns SNNCUDA_OK or an SNNCUDA_ERR_* code with
 // `msg` set.
 int pack_network_device(const snncuda_network* net, float cfg_max_weight, cudaStream_t st,
                         std::vector<void*>& owned, PackOut& out, std::string& msg);

@@ -15,8 +15,12 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <chrono>
+#include <deque>
 #include <memory>
 #include <mutex>
+#include <thread>
+#include <condition_variable>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -158,19 +162,29 @@ struct snncuda_sim {
     cudaEvent_t marks[2 * kKernelCount]{};
     static constexpr int kTicksPerGraph = 16;
 
+    // asynchronous runs (run_enqueue / run_complete)
+    TickState* ts_pinned{nullptr};  // tick state copied back at the end of a run
+    cudaEvent_t run_done{nullptr};
+    uint64_t run_target{0};         // inclusive tick of the run in flight
+    bool run_in_flight{false};
+
     ~snncuda_sim() {
+        if (run_done) cudaEventDestroy(run_done);
+        if (ts_pinned) cudaFreeHost(ts_pinned);
         if (graph_many) cudaGraphExecDestroy(graph_many);
         if (graph_one) cudaGraphExecDestroy(graph_one);
         if (graph_prof) cudaGraphExecDestroy(graph_prof);
         for (cudaEvent_t ev : marks)
             if (ev) cudaEventDestroy(ev);
+        // device buffers are stream-ordered: freeing them does not stall
+        // other streams (a server runs many simulations side by side)
         if (stream) cudaStreamSynchronize(stream);
-        for (void* p : owned) cudaFree(p);
-        if (far_ev) cudaFree(far_ev);
-        if (far_idx) cudaFree(far_idx);
-        if (inj_ev) cudaFree(inj_ev);
-        if (inj_slot) cudaFree(inj_slot);
-        if (inj_off) cudaFree(inj_off);
+        for (void* p : owned) cudaFreeAsync(p, stream);
+        if (far_ev) cudaFreeAsync(far_ev, stream);
+        if (far_idx) cudaFreeAsync(far_idx, stream);
+        if (inj_ev) cudaFreeAsync(inj_ev, stream);
+        if (inj_slot) cudaFreeAsync(inj_slot, stream);
+        if (inj_off) cudaFreeAsync(inj_off, stream);
         if (host_ev) cudaFreeHost(host_ev);
         if (host_idx) cudaFreeHost(host_idx);
         if (own_stream && stream) cudaStreamDestroy(stream);
@@ -215,17 +229,17 @@ struct snncuda_sim {
 
     void ensure_far(size_t events, size_t idx) {
         if (events > far_ev_cap) {
-            if (far_ev) cudaFree(far_ev);
+            if (far_ev) cudaFreeAsync(far_ev, stream);
             far_ev = nullptr;
             far_ev_cap = std::max<size_t>(events, 2 * far_ev_cap);
-            check(cudaMalloc(&far_ev, far_ev_cap * sizeof(unsigned long long)), "far events");
+            check(cudaMallocAsync(&far_ev, far_ev_cap * sizeof(unsigned long long), stream), "far events");
             drop_graphs();
         }
         if (idx > far_idx_cap) {
-            if (far_idx) cudaFree(far_idx);
+            if (far_idx) cudaFreeAsync(far_idx, stream);
             far_idx = nullptr;
             far_idx_cap = std::max<size_t>(idx, 2 * far_idx_cap);
-            check(cudaMalloc(&far_idx, far_idx_cap * sizeof(uint32_t)), "far index");
+            check(cudaMallocAsync(&far_idx, far_idx_cap * sizeof(uint32_t), stream), "far index");
             drop_graphs();
         }
         e.far_ev = far_ev;
@@ -234,19 +248,19 @@ struct snncuda_sim {
 
     void ensure_inject(size_t events, size_t groups) {
         if (events > inj_cap) {
-            if (inj_ev) cudaFree(inj_ev);
+            if (inj_ev) cudaFreeAsync(inj_ev, stream);
             inj_ev = nullptr;
             inj_cap = std::max<size_t>(events, 2 * inj_cap);
-            check(cudaMalloc(&inj_ev, inj_cap * sizeof(unsigned long long)), "inject events");
+            check(cudaMallocAsync(&inj_ev, inj_cap * sizeof(unsigned long long), stream), "inject events");
         }
         if (groups + 1 > inj_groups_cap) {
-            if (inj_slot) cudaFree(inj_slot);
-            if (inj_off) cudaFree(inj_off);
+            if (inj_slot) cudaFreeAsync(inj_slot, stream);
+            if (inj_off) cudaFreeAsync(inj_off, stream);
             inj_slot = nullptr;
             inj_off = nullptr;
             inj_groups_cap = std::max<size_t>(groups + 1, 2 * inj_groups_cap);
-            check(cudaMalloc(&inj_slot, inj_groups_cap * sizeof(uint32_t)), "inject slots");
-            check(cudaMalloc(&inj_off, inj_groups_cap * sizeof(uint32_t)), "inject offsets");
+            check(cudaMallocAsync(&inj_slot, inj_groups_cap * sizeof(uint32_t), stream), "inject slots");
+            check(cudaMallocAsync(&inj_off, inj_groups_cap * sizeof(uint32_t), stream), "inject offsets");
         }
     }
 
@@ -269,6 +283,16 @@ struct snncuda_sim {
 };
 
 namespace {
+
+// A persistent device buffer of the simulation, stream-ordered on its stream.
+template <typename T>
+T* salloc(snncuda_sim* sim, size_t count) {
+    void* p = nullptr;
+    if (count == 0) count = 1;
+    check(cudaMallocAsync(&p, count * sizeof(T), sim->stream), "device allocation");
+    sim->owned.push_back(p);
+    return static_cast<T*>(p);
+}
 
 void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_sim* sim) {
     const uint32_t N = net->neuron_count;
@@ -380,42 +404,41 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     build_stdp_tables(cfg, ltp, ltd);
 
     // ---- device allocation ----
-    auto& own = sim->owned;
-    auto* d_nparam = dalloc<NeuronParam>(own, N);
-    e.nrec = dalloc<NeuronRec>(own, N);
-    e.ntp = dalloc<NeuronTp>(own, N);
-    e.cand = dalloc<unsigned long long>(own, cand_total);
-    e.refmeta = dalloc<RefMeta>(own, meta_total);
-    e.ring = dalloc<unsigned long long>(own, ring_total);
-    e.lcode = dalloc<uint16_t>(own, lcode_total);
-    auto* d_cls = dalloc<uint32_t>(own, D);
-    e.wheel = dalloc<unsigned long long>(own, static_cast<size_t>(W) * slot_cap);
-    e.slot_count = dalloc<uint32_t>(own, W);
-    e.cnt = dalloc<uint32_t>(own, N);
-    e.seg_start = dalloc<uint32_t>(own, N);
+    auto* d_nparam = salloc<NeuronParam>(sim, N);
+    e.nrec = salloc<NeuronRec>(sim, N);
+    e.ntp = salloc<NeuronTp>(sim, N);
+    e.cand = salloc<unsigned long long>(sim, cand_total);
+    e.refmeta = salloc<RefMeta>(sim, meta_total);
+    e.ring = salloc<unsigned long long>(sim, ring_total);
+    e.lcode = salloc<uint16_t>(sim, lcode_total);
+    auto* d_cls = salloc<uint32_t>(sim, D);
+    e.wheel = salloc<unsigned long long>(sim, static_cast<size_t>(W) * slot_cap);
+    e.slot_count = salloc<uint32_t>(sim, W);
+    e.cnt = salloc<uint32_t>(sim, N);
+    e.seg_start = salloc<uint32_t>(sim, N);
     const uint32_t scan_tiles = (N + kScanTile - 1) / kScanTile;
-    e.tile_sum = dalloc<uint32_t>(own, scan_tiles + 2);
-    e.tile_nz = dalloc<uint32_t>(own, scan_tiles + 2);
-    e.touched = dalloc<uint32_t>(own, N);
-    e.tbeg = dalloc<uint32_t>(own, N);
-    e.grp = dalloc<unsigned long long>(own, slot_cap);
-    e.grp_sorted = dalloc<unsigned long long>(own, slot_cap);
-    e.evin = dalloc<EvIn>(own, slot_cap);
-    e.ev_a0 = dalloc<SynA>(own, slot_cap);
-    e.fire_bits = dalloc<uint32_t>(own, bit_words);
-    e.fire_at = dalloc<uint32_t>(own, slot_cap);
-    e.fire_tile = dalloc<uint32_t>(own, fire_tiles + 2);
-    e.fire_list = dalloc<uint32_t>(own, fire_cap);
-    e.fired_tgt = dalloc<uint32_t>(own, N);
-    e.fired_cnt = dalloc<uint32_t>(own, N);
-    e.xsum = dalloc<uint32_t>(own, xblocks * std::max<uint32_t>(D, 1));
-    e.xdst = dalloc<unsigned long long>(own, xblocks * std::max<uint32_t>(D, 1));
-    e.xdst_ok = dalloc<uint32_t>(own, std::max<uint32_t>(D, 1));
-    e.raster = dalloc<uint32_t>(own, cfg.raster_capacity > 0 ? 2 * cfg.raster_capacity : 1);
-    e.ts = dalloc<TickState>(own, 1);
-    auto* d_decay = dalloc<float>(own, decay.size());
-    auto* d_ltp = dalloc<float>(own, ltp.size());
-    auto* d_ltd = dalloc<float>(own, ltd.size());
+    e.tile_sum = salloc<uint32_t>(sim, scan_tiles + 2);
+    e.tile_nz = salloc<uint32_t>(sim, scan_tiles + 2);
+    e.touched = salloc<uint32_t>(sim, N);
+    e.tbeg = salloc<uint32_t>(sim, N);
+    e.grp = salloc<unsigned long long>(sim, slot_cap);
+    e.grp_sorted = salloc<unsigned long long>(sim, slot_cap);
+    e.evin = salloc<EvIn>(sim, slot_cap);
+    e.ev_a0 = salloc<SynA>(sim, slot_cap);
+    e.fire_bits = salloc<uint32_t>(sim, bit_words);
+    e.fire_at = salloc<uint32_t>(sim, slot_cap);
+    e.fire_tile = salloc<uint32_t>(sim, fire_tiles + 2);
+    e.fire_list = salloc<uint32_t>(sim, fire_cap);
+    e.fired_tgt = salloc<uint32_t>(sim, N);
+    e.fired_cnt = salloc<uint32_t>(sim, N);
+    e.xsum = salloc<uint32_t>(sim, xblocks * std::max<uint32_t>(D, 1));
+    e.xdst = salloc<unsigned long long>(sim, xblocks * std::max<uint32_t>(D, 1));
+    e.xdst_ok = salloc<uint32_t>(sim, std::max<uint32_t>(D, 1));
+    e.raster = salloc<uint32_t>(sim, cfg.raster_capacity > 0 ? 2 * cfg.raster_capacity : 1);
+    e.ts = salloc<TickState>(sim, 1);
+    auto* d_decay = salloc<float>(sim, decay.size());
+    auto* d_ltp = salloc<float>(sim, ltp.size());
+    auto* d_ltd = salloc<float>(sim, ltd.size());
 
     cudaStream_t st = sim->stream;
     auto h2d = [&](void* dst, const void* src, size_t bytes) {
@@ -483,8 +506,25 @@ int status_to_error(uint32_t status, std::string& msg) {
     return SNNCUDA_ERR_CAPACITY;
 }
 
-void run_impl(snncuda_sim* sim, uint64_t T, snncuda_profile* prof = nullptr) {
+// Queued injections in (delivery, call order): new ones are sorted on their
+// own (stable: call order kept), then merged behind the earlier ones they tie
+// with.
+void sort_pending(snncuda_sim* sim) {
+    auto& pend = sim->pending;
+    if (sim->pend_sorted < pend.size()) {
+        auto by_tick = [](const Pending& a, const Pending& b) { return a.tick < b.tick; };
+        const auto mid = pend.begin() + static_cast<std::ptrdiff_t>(sim->pend_sorted);
+        std::stable_sort(mid, pend.end(), by_tick);
+        std::inplace_merge(pend.begin() + static_cast<std::ptrdiff_t>(sim->pend_head), mid, pend.end(), by_tick);
+        sim->pend_sorted = pend.size();
+    }
+}
+
+// Enqueues ticks next_tick .. T on the simulation's stream and returns
+// without waiting; run_complete() waits and checks the device status.
+void run_enqueue(snncuda_sim* sim, uint64_t T, snncuda_profile* prof = nullptr) {
     const uint64_t p = sim->next_tick;
+    if (sim->run_in_flight) throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "a run is already in flight");
     if (T < p) return;
     if (T >= 0xFFFF0000ull) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "ticks beyond 2^32 - 2^16");
     Engine& e = sim->e;
@@ -493,15 +533,7 @@ void run_impl(snncuda_sim* sim, uint64_t T, snncuda_profile* prof = nullptr) {
     // their slots now, behind everything scheduled before this call; later
     // ones are moved in by k_hist the tick their slot frees up; the rest wait.
     auto& pend = sim->pending;
-    if (sim->pend_sorted < pend.size()) {
-        // new injections are sorted on their own (stable: call order kept),
-        // then merged behind the earlier ones they tie with
-        auto by_tick = [](const Pending& a, const Pending& b) { return a.tick < b.tick; };
-        const auto mid = pend.begin() + static_cast<std::ptrdiff_t>(sim->pend_sorted);
-        std::stable_sort(mid, pend.end(), by_tick);
-        std::inplace_merge(pend.begin() + static_cast<std::ptrdiff_t>(sim->pend_head), mid, pend.end(), by_tick);
-        sim->pend_sorted = pend.size();
-    }
+    sort_pending(sim);
     const Pending* base = pend.data() + sim->pend_head;
     const size_t live = pend.size() - sim->pend_head;
     auto first_at_or_after = [&](uint64_t tick) {
@@ -605,7 +637,28 @@ void run_impl(snncuda_sim* sim, uint64_t T, snncuda_profile* prof = nullptr) {
     const uint32_t zero = 0;
     check(cudaMemcpyAsync(reinterpret_cast<char*>(e.ts) + offsetof(TickState, far_ticks), &zero, 4,
                           cudaMemcpyHostToDevice, st), "run params");
-    const TickState ts = sim->read_ts();
+    if (sim->ts_pinned == nullptr) check(cudaMallocHost(&sim->ts_pinned, sizeof(TickState)), "pinned tick state");
+    if (sim->run_done == nullptr) check(cudaEventCreateWithFlags(&sim->run_done, cudaEventDisableTiming), "event");
+    check(cudaMemcpyAsync(sim->ts_pinned, e.ts, sizeof(TickState), cudaMemcpyDeviceToHost, st), "read tick state");
+    check(cudaEventRecord(sim->run_done, st), "event record");
+    sim->run_target = T;
+    sim->run_in_flight = true;
+}
+
+// True once the run in flight (if any) has finished; then checks it.
+// `wait` blocks until it has.
+bool run_complete(snncuda_sim* sim, bool wait) {
+    if (!sim->run_in_flight) return true;
+    if (wait) {
+        check(cudaEventSynchronize(sim->run_done), "run synchronize");
+    } else {
+        const cudaError_t q = cudaEventQuery(sim->run_done);
+        if (q == cudaErrorNotReady) return false;
+        check(q, "run query");
+    }
+    sim->run_in_flight = false;
+    const TickState ts = *sim->ts_pinned;
+    const uint64_t T = sim->run_target;
     sim->next_tick = T + 1;
     if (ts.tick != static_cast<uint32_t>(T + 1)) throw_fail(SNNCUDA_ERR_DEVICE, "device tick counter out of step");
     if (ts.status != 0) {
@@ -614,6 +667,12 @@ void run_impl(snncuda_sim* sim, uint64_t T, snncuda_profile* prof = nullptr) {
         const int code = status_to_error(ts.status, msg);
         throw_fail(code, msg);
     }
+    return true;
+}
+
+void run_impl(snncuda_sim* sim, uint64_t T, snncuda_profile* prof = nullptr) {
+    run_enqueue(sim, T, prof);
+    run_complete(sim, true);
 }
 
 // Rebuild the offsets of a run list.
@@ -1400,6 +1459,273 @@ int snncuda_batch_read_raster(snncuda_batch* b, uint32_t i, uint64_t first, uint
             if (neurons) neurons[k] = rn[first + k];
         }
     });
+}
+
+
+// ---------------------------------------------------------------------------
+// serving: jobs admitted under a device-memory budget, each simulation on its
+// own stream, advanced slice by slice so that many run side by side
+// ---------------------------------------------------------------------------
+
+// Device bytes of a simulation of `net` (persistent buffers plus the
+// transient buffers of creation), from one host pass over its synapses.
+static uint64_t estimate_bytes_impl(const snncuda_network* net, const snncuda_config& cfg) {
+    const uint64_t N = net->neuron_count, S = net->synapse_count;
+    const bool has_codes = net->code_offset_ptr != nullptr && net->code_offsets != nullptr;
+    uint64_t pre_total = 0, max_delta = 1, max_code = 0;
+    std::vector<uint8_t> present(1u << 20, 0);
+    uint64_t D = 0;
+    for (uint64_t s = 0; s < S; ++s) {
+        const uint64_t k = has_codes ? net->code_offset_ptr[s + 1] - net->code_offset_ptr[s] : 0;
+        pre_total += k == 0 ? 1 : k;
+        for (uint64_t j = 0; j < (k == 0 ? 1 : k); ++j) {
+            const uint64_t c = k ? net->code_offsets[net->code_offset_ptr[s] + j] : 0;
+            const uint64_t d = std::max<uint64_t>(1, static_cast<uint64_t>(net->delay_ticks[s]) + c);
+            max_code = std::max(max_code, c);
+            if (d < present.size() && !present[d]) {
+                present[d] = 1;
+                ++D;
+            }
+            max_delta = std::max(max_delta, d);
+        }
+    }
+    uint64_t W = 2;
+    while (W <= max_delta) W <<= 1;
+    const uint64_t run_budget = cfg.pattern_run_capacity ? cfg.pattern_run_capacity : 4096;
+    uint64_t neuron_bytes = 0, refs_max = 1;
+    for (uint64_t n = 0; n < N; ++n) {
+        const uint64_t window = net->pattern_window_ticks[n], refs = std::max<uint64_t>(1, net->max_reference_patterns[n]);
+        refs_max = std::max(refs_max, refs);
+        const uint64_t ring = std::min<uint64_t>(refs * (window + 1), std::max<uint64_t>(window + 1, run_budget));
+        neuron_bytes += 64 + 64 + 32 + 8 * (window + 1) + sizeof(RefMeta) * refs + 8 * ring + 8 + 4 * (D + 1) + 24;
+    }
+    uint64_t slot_cap = cfg.slot_event_capacity;
+    if (slot_cap == 0) slot_cap = std::min<uint64_t>(1ull << 27, std::max<uint64_t>(1ull << 16, pre_total / 8));
+    const uint64_t fire_cap = std::min<uint64_t>(slot_cap, std::max<uint64_t>(65536, 4ull * N));
+    const uint64_t lcode = refs_max > 1 ? 2ull * S * refs_max * kMaxExpected : 0;
+    const uint64_t persistent = 64 * S + 8 * S + 8 * pre_total + neuron_bytes + lcode +
+                                W * slot_cap * 8 + slot_cap * (8 + 8 + 16 + 32 + 4 + 1) +
+                                fire_cap * 4 + (fire_cap / 8 + 1) * 12 * std::max<uint64_t>(D, 1) +
+                                16 * cfg.raster_capacity + (16u << 20);
+    const uint64_t transient = S * (23 + 8 + 12 + 8) + 4 * (has_codes ? net->code_offset_ptr[S] : 0) +
+                               N * (16 + 8 + 4 * D) + (4u << 20);
+    (void)max_code;
+    return persistent + transient;
+}
+
+struct ServerJob {
+    snncuda_network net{};
+    snncuda_config cfg{};
+    std::vector<uint32_t> inj_n;
+    std::vector<uint64_t> inj_t;
+    std::vector<float> inj_w;
+    uint64_t ticks{0};
+    uint64_t bytes{0};
+    snncuda_sim* sim{nullptr};
+    snncuda_job_result res{};
+};
+
+// Jobs are created (host packing, uploads) by a worker thread, so that the
+// caller's thread keeps the running jobs' streams fed meanwhile.
+struct snncuda_server {
+    snncuda_server_config cfg{};
+    std::vector<std::unique_ptr<ServerJob>> jobs;
+    std::deque<uint64_t> queue;     // submitted, not admitted
+    std::vector<uint64_t> running;  // created, advanced by step()
+    uint64_t used{0};               // admission estimate of admitted jobs
+    uint32_t creating{0};           // admitted, not yet created
+    int device{0};
+    std::chrono::steady_clock::time_point t0{std::chrono::steady_clock::now()};
+    // worker
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<uint64_t> to_create;
+    std::vector<uint64_t> created;  // with the worker's status in the job
+    bool stop{false};
+    std::thread worker;
+
+    double now() const {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    void work() {
+        cudaSetDevice(device);
+        for (;;) {
+            uint64_t id;
+            {
+                std::unique_lock<std::mutex> lock(mu);
+                cv.wait(lock, [&] { return stop || !to_create.empty(); });
+                if (stop) return;
+                id = to_create.front();
+                to_create.pop_front();
+            }
+            ServerJob& j = *jobs_at(id);
+            j.sim = new (std::nothrow) snncuda_sim();
+            int rc = j.sim ? SNNCUDA_OK : SNNCUDA_ERR_OUT_OF_MEMORY;
+            if (rc == SNNCUDA_OK) rc = guarded([&] { create_impl(&j.net, j.cfg, j.sim); });
+            if (rc == SNNCUDA_OK)
+                rc = snncuda_sim_inject(j.sim, j.inj_n.size(), j.inj_n.data(), j.inj_t.data(), j.inj_w.data());
+            if (rc == SNNCUDA_OK) sort_pending(j.sim);  // host work off the stepping thread
+            j.res.error = rc;
+            std::lock_guard<std::mutex> lock(mu);
+            created.push_back(id);
+        }
+    }
+    ServerJob* jobs_at(uint64_t id) {
+        std::lock_guard<std::mutex> lock(mu);
+        return jobs[id].get();
+    }
+    ~snncuda_server() {
+        {
+            std::lock_guard<std::mutex> lock(mu);
+            stop = true;
+        }
+        cv.notify_all();
+        if (worker.joinable()) worker.join();
+        for (auto& j : jobs)
+            if (j->sim) delete j->sim;
+    }
+};
+
+static void server_finish(snncuda_server* sv, ServerJob& j, int state, int error) {
+    j.res.state = state;
+    j.res.error = error;
+    j.res.finished_s = sv->now();
+    delete j.sim;
+    j.sim = nullptr;
+    sv->used -= j.bytes;
+}
+
+int snncuda_server_create(const snncuda_server_config* config, snncuda_server** out) {
+    if (out == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
+    snncuda_server* sv = new (std::nothrow) snncuda_server();
+    if (sv == nullptr) return set_error(SNNCUDA_ERR_OUT_OF_MEMORY, "host allocation failed");
+    if (config) sv->cfg = *config;
+    if (sv->cfg.memory_budget_bytes == 0) sv->cfg.memory_budget_bytes = 120ull << 30;
+    if (sv->cfg.max_running == 0) sv->cfg.max_running = 64;
+    if (sv->cfg.slice_ticks == 0) sv->cfg.slice_ticks = 64;
+    const int rc = guarded([&] {
+        check(cudaGetDevice(&sv->device), "cudaGetDevice");
+        sv->worker = std::thread([sv] { sv->work(); });
+    });
+    if (rc != SNNCUDA_OK) {
+        delete sv;
+        return rc;
+    }
+    *out = sv;
+    return SNNCUDA_OK;
+}
+
+int snncuda_server_destroy(snncuda_server* server) {
+    delete server;
+    return SNNCUDA_OK;
+}
+
+int snncuda_server_submit(snncuda_server* sv, const snncuda_network* network, const snncuda_config* config,
+                          uint64_t inject_count, const uint32_t* neurons, const uint64_t* ticks, const float* weights,
+                          uint64_t run_ticks, uint64_t* job_id) {
+    if (sv == nullptr || network == nullptr || job_id == nullptr)
+        return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
+    if (inject_count > 0 && (!neurons || !ticks || !weights)) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null array");
+    return guarded([&] {
+        std::unique_ptr<ServerJob> j(new ServerJob());
+        j->net = *network;
+        snncuda_config_default(&j->cfg);
+        if (config) j->cfg = *config;
+        j->cfg.cuda_stream = nullptr;  // every job on a stream of its own
+        j->inj_n.assign(neurons, neurons + inject_count);
+        j->inj_t.assign(ticks, ticks + inject_count);
+        j->inj_w.assign(weights, weights + inject_count);
+        j->ticks = run_ticks;
+        j->bytes = estimate_bytes_impl(network, j->cfg);
+        j->res.state = 0;
+        j->res.device_bytes = j->bytes;
+        j->res.submitted_s = sv->now();
+        std::lock_guard<std::mutex> lock(sv->mu);
+        *job_id = sv->jobs.size();
+        sv->queue.push_back(sv->jobs.size());
+        sv->jobs.push_back(std::move(j));
+    });
+}
+
+int snncuda_server_step(snncuda_server* sv, uint32_t* active) {
+    if (sv == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null server");
+    const uint64_t slice = sv->cfg.slice_ticks;
+    // advance or retire the running jobs
+    for (size_t i = 0; i < sv->running.size();) {
+        ServerJob& j = *sv->jobs_at(sv->running[i]);
+        bool ready = false, finished = false;
+        int rc = guarded([&] {
+            ready = run_complete(j.sim, false);
+            if (!ready) return;
+            if (j.sim->next_tick >= j.ticks) {
+                finished = true;
+                return;
+            }
+            run_enqueue(j.sim, std::min<uint64_t>(j.sim->next_tick + slice, j.ticks) - 1);
+        });
+        if (rc == SNNCUDA_OK && finished) {
+            rc = snncuda_sim_counters(j.sim, &j.res.counters);
+            if (rc == SNNCUDA_OK && sv->cfg.digests)
+                rc = snncuda_sim_state_digest(j.sim, &j.res.neuron_digest, &j.res.synapse_digest);
+        }
+        if (rc != SNNCUDA_OK || finished) {
+            server_finish(sv, j, rc == SNNCUDA_OK ? 2 : 3, rc);
+            sv->running.erase(sv->running.begin() + static_cast<std::ptrdiff_t>(i));
+            continue;
+        }
+        ++i;
+    }
+    // jobs the worker has created start running
+    std::vector<uint64_t> ready;
+    {
+        std::lock_guard<std::mutex> lock(sv->mu);
+        ready.swap(sv->created);
+    }
+    for (uint64_t id : ready) {
+        ServerJob& j = *sv->jobs_at(id);
+        sv->creating -= 1;
+        int rc = j.res.error;
+        if (rc == SNNCUDA_OK && j.ticks > 0)
+            rc = guarded([&] { run_enqueue(j.sim, std::min<uint64_t>(slice, j.ticks) - 1); });
+        if (rc != SNNCUDA_OK) {
+            server_finish(sv, j, 3, rc);
+            continue;
+        }
+        j.res.state = 1;
+        sv->running.push_back(id);
+    }
+    // admit queued jobs in submission order while they fit; the worker
+    // creates them
+    while (!sv->queue.empty() && sv->running.size() + sv->creating < sv->cfg.max_running) {
+        const uint64_t id = sv->queue.front();
+        ServerJob& j = *sv->jobs_at(id);
+        if (sv->used + j.bytes > sv->cfg.memory_budget_bytes && (!sv->running.empty() || sv->creating > 0)) break;
+        sv->queue.pop_front();
+        j.res.admitted_s = sv->now();
+        sv->used += j.bytes;
+        sv->creating += 1;
+        {
+            std::lock_guard<std::mutex> lock(sv->mu);
+            sv->to_create.push_back(id);
+        }
+        sv->cv.notify_one();
+    }
+    if (active) *active = static_cast<uint32_t>(sv->queue.size() + sv->running.size() + sv->creating);
+    return SNNCUDA_OK;
+}
+
+int snncuda_server_job(snncuda_server* sv, uint64_t job_id, snncuda_job_result* out) {
+    if (sv == nullptr || out == nullptr || job_id >= sv->jobs.size())
+        return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "bad server or job");
+    *out = sv->jobs_at(job_id)->res;
+    return SNNCUDA_OK;
+}
+
+int snncuda_sim_estimate_bytes(const snncuda_network* network, const snncuda_config* config, uint64_t* bytes) {
+    if (network == nullptr || bytes == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
+    snncuda_config def;
+    snncuda_config_default(&def);
+    return guarded([&] { *bytes = estimate_bytes_impl(network, config ? *config : def); });
 }
 
 }  // extern "C"

@@ -349,6 +349,60 @@ class Batch:
         return ticks, neurons
 
 
+class Server:
+    """Serving: jobs admitted in submission order under a device-memory
+    budget and advanced `slice_ticks` at a time, each on its own stream.
+    The caller drives it with step(); a job's network arrays must stay alive
+    until the job is admitted (the Server keeps them until it has finished)."""
+
+    def __init__(self, memory_budget_bytes: int = 0, max_running: int = 0, slice_ticks: int = 0,
+                 digests: bool = False, lib: Optional[ctypes.CDLL] = None):
+        self.lib = lib or backend()
+        cfg = _abi.ServerConfig(memory_budget_bytes, max_running, slice_ticks, 1 if digests else 0)
+        handle = c_void_p()
+        _check(self.lib, self.lib.snncuda_server_create(ctypes.byref(cfg), ctypes.byref(handle)))
+        self.handle = handle
+        self._keep = {}
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.snncuda_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, connectome: Connectome, config: Optional[_abi.Config], drive, ticks: int) -> int:
+        connectome.validate()
+        net, keep = _network_struct(connectome)
+        cfg = config if config is not None else default_config(self.lib)
+        n, t, w = _inject_arrays(*drive)
+        job = c_uint64()
+        _check(self.lib, self.lib.snncuda_server_submit(
+            self.handle, ctypes.byref(net), ctypes.byref(cfg), n.size, _abi.ptr(n, c_uint32), _abi.ptr(t, c_uint64),
+            _abi.ptr(w, c_float), int(ticks), ctypes.byref(job)))
+        self._keep[int(job.value)] = (net, keep)
+        return int(job.value)
+
+    def step(self) -> int:
+        active = c_uint32()
+        _check(self.lib, self.lib.snncuda_server_step(self.handle, ctypes.byref(active)))
+        return int(active.value)
+
+    def job(self, job_id: int) -> Dict[str, object]:
+        r = _abi.JobResult()
+        _check(self.lib, self.lib.snncuda_server_job(self.handle, int(job_id), ctypes.byref(r)))
+        if r.state >= 2:
+            self._keep.pop(int(job_id), None)  # finished: its arrays are no longer read
+        return {"state": r.state, "error": r.error,
+                "counters": {name: int(getattr(r.counters, name)) for name, _ in _abi.Counters._fields_},
+                "digest": (int(r.neuron_digest), int(r.synapse_digest)), "device_bytes": int(r.device_bytes),
+                "submitted_s": r.submitted_s, "admitted_s": r.admitted_s, "finished_s": r.finished_s}
+
+
 # ---------------------------------------------------------------------------
 # Reference-shaped interface
 # ---------------------------------------------------------------------------
