@@ -524,8 +524,59 @@ __device__ __forceinline__ void store_pattern(uint16_t* pat, uint32_t stride, un
 // held in two 64-bit words.  `inline_pattern`: the target keeps one reference
 // pattern and codes have at most 4 offsets, so the single learned code
 // pattern is stored in ring_hi instead of the pattern pool.
+// Sum of the squares / of the products of four 16-bit lanes (offsets below
+// 2^16: every product fits 32 bits).
+__device__ __forceinline__ unsigned long long lanes_dot(unsigned long long a, unsigned long long b) {
+    const uint32_t a0 = static_cast<uint32_t>(a), a1 = static_cast<uint32_t>(a >> 32);
+    const uint32_t b0 = static_cast<uint32_t>(b), b1 = static_cast<uint32_t>(b >> 32);
+    return static_cast<unsigned long long>((a0 & 0xFFFFu) * (b0 & 0xFFFFu)) + ((a0 >> 16) * (b0 >> 16)) +
+           static_cast<unsigned long long>((a1 & 0xFFFFu) * (b1 & 0xFFFFu)) + ((a1 >> 16) * (b1 >> 16));
+}
+
+// code_update for inline_code_pattern (one reference pattern, at most 4
+// offsets): the window is the four 16-bit lanes of ring_lo, the learned
+// pattern those of ring_hi; lanes at or above `expected` are always zero, so
+// the sums run over all four lanes.
+__device__ __forceinline__ void code_update_inline(SynB& b, uint32_t window, float sim, uint32_t t) {
+    b.flags &= 0xF0u;  // last_code_match = false
+    if (b.code_len == 0 || t - b.code_ws > window) {
+        b.code_ws = t;
+        b.code_len = 0;
+    }
+    const uint32_t o = t - b.code_ws;
+    const uint32_t expected = b.flags >> 4;
+    if (b.code_len < expected) {
+        const int sh = 16 * b.code_len;
+        b.ring_lo = (b.ring_lo & ~(0xFFFFull << sh)) | (static_cast<unsigned long long>(o) << sh);
+        b.code_len += 1;
+        if (b.code_len < expected) return;
+    } else {
+        const int sh = 16 * (expected - 1);
+        b.ring_lo = ((b.ring_lo >> 16) & ~(0xFFFFull << sh)) | (static_cast<unsigned long long>(o) << sh);
+    }
+    bool match = 0.0f >= sim;
+    if (!match && b.learned_count > 0)
+        match = cos_ge(lanes_dot(b.ring_hi, b.ring_lo), lanes_dot(b.ring_hi, b.ring_hi),
+                       lanes_dot(b.ring_lo, b.ring_lo), sim);
+    if (match) {
+        b.code_matches += 1;
+        b.flags |= 1u;
+        return;
+    }
+    b.ring_hi = b.ring_lo;
+    b.learned_count = 1;
+}
+
 __device__ void code_update(SynB& b, const NeuronParam& p, uint32_t t, uint16_t* lc, uint32_t stride, int enabled,
                             bool inline_pattern) {
+    if (inline_pattern) {
+        if (enabled) {
+            code_update_inline(b, p.window, p.similarity, t);
+        } else {
+            b.flags &= 0xF0u;
+        }
+        return;
+    }
     b.flags &= 0xF0u;  // last_code_match = false
     if (!enabled) return;
     if (b.code_len == 0 || t - b.code_ws > p.window) {
@@ -819,8 +870,33 @@ struct SortedDue {
 // indices, and the events of each synapse are found with one match; the
 // synapse's earliest event's lane then processes all of them in due order.
 // Longer groups are placed by rank into grp_sorted and scanned.
+// A synapse with a single event in its target's group this tick: the unit
+// of work k_events queues so that all 32 lanes of a warp carry one.
+struct EvItem {
+    uint32_t tm, pos, due, n;
+};
+
+// Pre-spike work of a queued event (one lane).
+__device__ __forceinline__ void synapse_item(const Engine& e, const EvItem& it, uint32_t t, int stdp, int temporal) {
+    const NeuronParam p = e.nparam[it.n];
+    const bool inl = inline_code_pattern(p.max_refs, e.code_stride);
+    uint16_t* lc =
+        inl ? nullptr : e.lcode + p.lcode_base + static_cast<size_t>(it.tm - p.in_begin) * p.max_refs * e.code_stride;
+    SynAB r = e.syn[it.tm];
+    e.ev_a0[it.pos] = r.a;
+    pre_event(r, p, t, lc, e, stdp, temporal, inl);
+    EvIn in;
+    in.weight = r.a.weight;
+    in.bits = ev_bits(r.a);
+    in.tm = it.tm;
+    in.due = it.due;
+    e.evin[it.pos] = in;
+    e.syn[it.tm] = r;
+}
+
 __device__ __forceinline__ void events_of_target(const Engine& e, uint32_t n, uint32_t beg, uint32_t len, uint32_t t,
-                                                 int stdp, int temporal, uint32_t* wdue, uint32_t* wrank) {
+                                                 int stdp, int temporal, uint32_t* wdue, uint32_t* wrank,
+                                                 EvItem* queue, uint32_t& qn) {
     const uint32_t lane = threadIdx.x & 31;
     if (len <= 32) {
         const bool valid = lane < len;
@@ -843,8 +919,19 @@ __device__ __forceinline__ void events_of_target(const Engine& e, uint32_t n, ui
             in.due = key;
             e.evin[beg + rank] = in;
         }
-        bool leader = syn;
-        if (syn && same != (1u << lane)) {
+        const bool single = syn && same == (1u << lane);
+        const uint32_t qmask = __ballot_sync(0xffffffffu, single);
+        if (single) {  // the common case: queued, processed 32 at a time
+            EvItem it;
+            it.tm = tm;
+            it.pos = beg + rank;
+            it.due = key;
+            it.n = n;
+            queue[qn + __popc(qmask & ((1u << lane) - 1u))] = it;
+        }
+        qn += __popc(qmask);
+        bool leader = syn && !single;
+        if (leader) {
             for (uint32_t m = same; m; m &= m - 1) leader = leader && wrank[__ffs(m) - 1] >= rank;
         }
         if (leader) {
@@ -914,23 +1001,37 @@ __device__ __forceinline__ void events_of_target(const Engine& e, uint32_t n, ui
     __syncwarp();
 }
 
-// One warp per touched target (events_of_target): the synapses of a target
-// proceed in parallel across lanes, each a random 64-byte record.
+// One warp per touched target (events_of_target).  Synapses with a single
+// event this tick go to a per-warp queue in shared memory and are processed
+// 32 at a time, one per lane, whatever targets they belong to; repeats and
+// long groups are processed in place.
 __global__ void __launch_bounds__(kThreads, SNNGB_EVENTS_MIN_BLOCKS) k_events(Engine e) {
     __shared__ uint32_t s_due[kThreads], s_rank[kThreads];
+    __shared__ EvItem s_queue[kThreads / 32][64];
     const uint32_t t = e.ts->tick;
     const uint32_t n_touched = e.ts->n_touched;
     const uint32_t n_due = e.ts->n_due;
     const int stdp = e.ts->stdp_enabled;
     const int temporal = e.ts->temporal_enabled;
+    const uint32_t lane = threadIdx.x & 31;
     const uint32_t wbase = threadIdx.x & ~31u;
+    EvItem* queue = s_queue[threadIdx.x >> 5];
+    uint32_t qn = 0;  // warp-uniform
     const uint32_t warps = gridDim.x * (blockDim.x / 32);
     for (uint32_t k = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); k < n_touched; k += warps) {
         const uint32_t n = e.touched[k];
         const uint32_t beg = e.tbeg[k];
         const uint32_t end = k + 1 < n_touched ? e.tbeg[k + 1] : n_due;
-        events_of_target(e, n, beg, end - beg, t, stdp, temporal, s_due + wbase, s_rank + wbase);
+        events_of_target(e, n, beg, end - beg, t, stdp, temporal, s_due + wbase, s_rank + wbase, queue, qn);
+        if (qn >= 32) {
+            __syncwarp();
+            synapse_item(e, queue[qn - 32 + lane], t, stdp, temporal);
+            qn -= 32;
+            __syncwarp();
+        }
     }
+    __syncwarp();
+    if (lane < qn) synapse_item(e, queue[lane], t, stdp, temporal);
 }
 
 // The synapse's state before event i of the walk, after the target's fires so
