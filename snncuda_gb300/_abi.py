@@ -135,7 +135,7 @@ class SynapseState(Structure):
     ]
 
 
-KERNEL_COUNT = 10
+KERNEL_COUNT = 11
 
 
 class Profile(Structure):

@@ -102,7 +102,8 @@ struct alignas(64) NeuronRec {
     uint32_t spike_count;
     uint32_t last_fired1;  // last_fired_tick + 1, 0 = none
     uint32_t last_active;
-    uint32_t flags;        // bits 0-7: 4 x 2-bit tau code; bit 8: temporal last_match
+    uint32_t flags;        // 4 x 2-bit tau code
+    // temporal pattern fields (written by k_temporal only)
     uint32_t match_count;
     uint32_t ws;           // temporal window_start_tick
     uint32_t len;          // spike_offsets.size()
@@ -115,7 +116,7 @@ struct alignas(32) NeuronTp {
     uint32_t ref_count;
     uint32_t ring_head;     // next free run slot of the learned-pattern run ring
     uint32_t ring_used;
-    uint32_t pad;
+    uint32_t last_match;    // temporal_pattern.last_match
 };
 
 struct alignas(64) NeuronParam {
@@ -257,8 +258,11 @@ constexpr uint32_t kMaxClasses = 256;    // distinct delivery delays
 // Host-side launchers (kernels.cu).
 // `marks` (optional) holds 2 * kKernelCount events recorded around every
 // kernel (before, after) for profiling graphs.
-constexpr int kKernelCount = 10;
-void launch_tick(const Engine& e, cudaStream_t stream, cudaEvent_t* marks = nullptr);
+constexpr int kKernelCount = 11;
+// One tick on `stream`; k_temporal runs on `side` (forked after the grouping
+// scan with `fork`, joined back with `join` before the tick is finished).
+void launch_tick(const Engine& e, cudaStream_t stream, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join,
+                 cudaEvent_t* marks = nullptr);
 const char* kernel_name(int index);
 void launch_inject(const Engine& e, const unsigned long long* ev, const uint32_t* slot_of_group,
                    const uint32_t* group_off, uint32_t groups, cudaStream_t stream);

@@ -17,9 +17,8 @@
 //                  each event's input for the neuron walk
 //  6. k_process    one thread per touched target: the neuron's physics over
 //                  its events in due order (:175-229), redoing the STDP of
-//                  events that follow a fire of the target; the temporal
-//                  pattern once per tick (:294-316); fires into a due-position
-//                  bitmap
+//                  events that follow a fire of the target; fires into a
+//                  due-position bitmap
 //  7. k_post       post-spike STDP over the in-rows of targets that fired
 //                  (:138-173) + fire tile counts
 //  8. k_fire_list  fires in due order (= reference fire order), raster
@@ -27,6 +26,8 @@
 //                  destinations and finishes the tick
 // 10. k_expand     copy each fire's pre-expanded (synapse, offset) events into
 //                  their delivery slots, order-preserving
+// 11. k_temporal   the neuron temporal pattern of every touched target, once
+//                  per tick, on a second stream beside 5-6 (graph fork/join)
 //
 // Every wait is a kernel boundary or a "last block" hand-off (an atomic
 // counter, no spinning), so no kernel here can hang.
@@ -43,6 +44,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr uint32_t kStageEvents = 4096;  // event inputs k_process stages per block (64 KB)
+constexpr int kFireCountThreads = 1024;  // k_fire_count's last block scans up to 32 delay classes at once
 
 // Minimum resident blocks per SM requested for k_process and k_events
 // (register budget).
@@ -225,7 +227,7 @@ __device__ __forceinline__ uint32_t wrap_add(uint32_t a, uint32_t b, uint32_t m)
 struct NState {
     float cur[4];
     uint32_t upd[4];
-    uint32_t flags;  // tau codes (2 bits each) | last_match << 8
+    uint32_t flags;  // tau codes (2 bits each); in k_temporal: last_match << 8
     float membrane;
     uint32_t spikes, last_fired1, last_active, match_count, ws, len;
     unsigned long long cn;
@@ -401,8 +403,8 @@ __device__ void temporal_tick(NState& s, const NeuronParam& p, uint32_t t, const
 }
 
 // SynapseDendriteProcessor.cpp:175-229.  Returns whether the neuron fired.
-__device__ bool process_input(NState& s, const NeuronParam& p, uint32_t comp, uint32_t rec, float w,
-                              uint32_t t, const Engine& e) {
+__device__ bool process_input(NState& s, float threshold, uint32_t comp, uint32_t rec, float w, uint32_t t,
+                              const Engine& e) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         if (t <= s.upd[k] || s.cur[k] == 0.0f) {
@@ -424,7 +426,7 @@ __device__ bool process_input(NState& s, const NeuronParam& p, uint32_t comp, ui
     }
     s.last_active = t;  // the temporal-pattern update of this event is done by temporal_tick
     s.membrane = __fadd_rn(__fadd_rn(__fadd_rn(s.cur[0], s.cur[1]), s.cur[2]), s.cur[3]);
-    if (s.membrane >= p.threshold) {
+    if (s.membrane >= threshold) {
         s.membrane = 0.0f;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -1068,84 +1070,58 @@ struct Staged {
     uint32_t lo, cnt;
 };
 
-template <bool kOne, typename Ready>
+template <typename Ready>
 __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, uint32_t beg, uint32_t len, uint32_t t,
-                                               int stdp, int temporal, Staged st, Ready ready) {
-    const NeuronParam p = e.nparam[n];
-    const NeuronRec r = e.nrec[n];
-    const NeuronTp q = e.ntp[n];
+                                               int stdp, Staged st, Ready ready) {
+    // the physics fields only: the temporal ones belong to k_temporal, which
+    // may be running at the same time
     NState s;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        s.cur[c] = r.cur[c];
-        s.upd[c] = r.upd[c];
+    NeuronRec* rec = e.nrec + n;
+    const float threshold = e.nparam[n].threshold;
+    {
+        const float4 c = reinterpret_cast<const float4*>(rec->cur)[0];
+        const uint4 u = reinterpret_cast<const uint4*>(rec->upd)[0];
+        const uint4 m = *reinterpret_cast<const uint4*>(&rec->membrane);
+        s.cur[0] = c.x;
+        s.cur[1] = c.y;
+        s.cur[2] = c.z;
+        s.cur[3] = c.w;
+        s.upd[0] = u.x;
+        s.upd[1] = u.y;
+        s.upd[2] = u.z;
+        s.upd[3] = u.w;
+        s.membrane = __uint_as_float(m.x);
+        s.spikes = m.y;
+        s.last_fired1 = m.z;
+        s.last_active = m.w;
+        s.flags = rec->flags;
     }
-    s.flags = r.flags;
-    s.membrane = r.membrane;
-    s.spikes = r.spike_count;
-    s.last_fired1 = r.last_fired1;
-    s.last_active = r.last_active;
-    s.match_count = r.match_count;
-    s.ws = r.ws;
-    s.len = r.len;
-    s.cn = q.cn;
-    s.nruns = q.nruns;
-    s.ref_head = q.ref_head;
-    s.ref_count = q.ref_count;
-    s.ring_head = q.ring_head;
-    s.ring_used = q.ring_used;
-    s.last_run = s.nruns > 0 ? e.cand[p.cand_base + s.nruns - 1] : 0ull;
-    if (kOne && s.ref_count > 0) s.one = e.refmeta[p.meta_base];
-    s.snap_pending = false;
 
     uint32_t fires = 0, first_fire = 0;
     if (!ready()) st.cnt = 0;
     for (uint32_t i = 0; i < len; ++i) {
         const uint32_t o = beg + i - st.lo;
-        const EvIn x = o < st.cnt ? st.s[o] : e.evin[beg + i];
+        EvIn x;
+        if (o < st.cnt) {
+            x = st.s[o];
+        } else {
+            x = e.evin[beg + i];
+        }
         float w = x.weight;
         if (fires > 0 && !(x.bits & kEvExternal)) w = replay_pre_stdp(e, beg, i, first_fire, x, t, fires, stdp);
-        if (process_input(s, p, x.bits & 3u, (x.bits >> 2) & 3u, w, t, e)) {
+        if (process_input(s, threshold, x.bits & 3u, (x.bits >> 2) & 3u, w, t, e)) {
             if (fires == 0) first_fire = i;
             fires += 1;
             atomicOr(&e.fire_bits[x.due >> 5], 1u << (x.due & 31));
             e.fire_at[x.due] = n;
         }
     }
-    temporal_tick<kOne>(s, p, t, e, temporal, len);
-    if (s.nruns > 0) e.cand[p.cand_base + s.nruns - 1] = s.last_run;
-    if (kOne && s.ref_count > 0) e.refmeta[p.meta_base] = s.one;
-    if (kOne && s.snap_pending) {
-        // runs 0 .. snap_nruns-2 are final in cand; the last one was saved
-        unsigned long long* ring = e.ring + p.ring_base;
-        const unsigned long long* cand = e.cand + p.cand_base;
-        for (uint32_t j = 0; j + 1 < s.snap_nruns; ++j) ring[wrap_add(s.one.start, j, p.ring_cap)] = cand[j];
-        ring[wrap_add(s.one.start, s.snap_nruns - 1, p.ring_cap)] = s.snap_last;
-    }
-    NeuronRec w;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        w.cur[c] = s.cur[c];
-        w.upd[c] = s.upd[c];
-    }
-    w.flags = s.flags;
-    w.membrane = s.membrane;
-    w.spike_count = s.spikes;
-    w.last_fired1 = s.last_fired1;
-    w.last_active = s.last_active;
-    w.match_count = s.match_count;
-    w.ws = s.ws;
-    w.len = s.len;
-    NeuronTp wq;
-    wq.cn = s.cn;
-    wq.nruns = s.nruns;
-    wq.ref_head = s.ref_head;
-    wq.ref_count = s.ref_count;
-    wq.ring_head = s.ring_head;
-    wq.ring_used = s.ring_used;
-    wq.pad = 0;
-    e.nrec[n] = w;
-    e.ntp[n] = wq;
+
+    reinterpret_cast<float4*>(rec->cur)[0] = make_float4(s.cur[0], s.cur[1], s.cur[2], s.cur[3]);
+    reinterpret_cast<uint4*>(rec->upd)[0] = make_uint4(s.upd[0], s.upd[1], s.upd[2], s.upd[3]);
+    *reinterpret_cast<uint4*>(&rec->membrane) =
+        make_uint4(__float_as_uint(s.membrane), s.spikes, s.last_fired1, s.last_active);
+    rec->flags = s.flags;
     if (fires > 0) {
         const uint32_t j = atomicAdd(&e.ts->n_fired_targets, 1u);
         e.fired_tgt[j] = n;
@@ -1153,10 +1129,11 @@ __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, uint
     }
 }
 
-// One thread per touched target.  Exact because every state an event reads
-// or writes belongs to its target (the target's neuron state and the
-// target's incoming synapses); post-spike STDP of a fire is applied lazily
-// to synapses touched later in the tick and in bulk by k_post for the rest.
+// One thread per touched target: the neuron's physics over its events in
+// due order.  Exact because every state an event reads or writes belongs to
+// its target (the target's neuron state and the target's incoming synapses);
+// post-spike STDP of a fire is applied lazily to synapses touched later in the
+// tick and in bulk by k_post for the rest.
 // A block's targets are consecutive touched targets, so their event inputs
 // are one contiguous range: one thread copies it into shared memory with a
 // bulk copy while every thread loads its neuron's records.
@@ -1168,7 +1145,6 @@ __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(
     const uint32_t n_touched = e.ts->n_touched;
     const uint32_t n_due = e.ts->n_due;
     const int stdp = e.ts->stdp_enabled;
-    const int temporal = e.ts->temporal_enabled;
     if (threadIdx.x == 0) mbar_init(&s_bar, 1);
     __syncthreads();
     uint32_t parity = 0;
@@ -1199,11 +1175,7 @@ __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(
             const uint32_t n = e.touched[k];
             const uint32_t beg = e.tbeg[k];
             const uint32_t end = k + 1 < n_touched ? e.tbeg[k + 1] : n_due;
-            if (e.nparam[n].max_refs == 1) {
-                process_target<true>(e, n, beg, end - beg, t, stdp, temporal, st, ready);
-            } else {
-                process_target<false>(e, n, beg, end - beg, t, stdp, temporal, st, ready);
-            }
+            process_target(e, n, beg, end - beg, t, stdp, st, ready);
         }
         ready();
         const bool failed = __syncthreads_or(!ok);
@@ -1217,6 +1189,69 @@ __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(
             parity ^= 1u;
         }
         if (failed) staging = false;
+    }
+}
+
+// The temporal pattern update of every touched target (SynapseDendriteProcessor
+// .cpp:294-316), once per tick for all its k events (temporal_tick).  It reads
+// and writes only the neuron's temporal fields, which nothing else in the tick
+// touches, so it runs beside k_scatter / k_events / k_process.
+template <bool kOne>
+__device__ __forceinline__ void temporal_target(const Engine& e, uint32_t n, uint32_t k, uint32_t t, int temporal) {
+    const NeuronParam p = e.nparam[n];
+    NeuronRec* rec = e.nrec + n;
+    const NeuronTp q = e.ntp[n];
+    NState s;
+    s.match_count = rec->match_count;
+    s.ws = rec->ws;
+    s.len = rec->len;
+    s.flags = q.last_match << 8;
+    s.cn = q.cn;
+    s.nruns = q.nruns;
+    s.ref_head = q.ref_head;
+    s.ref_count = q.ref_count;
+    s.ring_head = q.ring_head;
+    s.ring_used = q.ring_used;
+    s.last_run = s.nruns > 0 ? e.cand[p.cand_base + s.nruns - 1] : 0ull;
+    if (kOne && s.ref_count > 0) s.one = e.refmeta[p.meta_base];
+    s.snap_pending = false;
+    temporal_tick<kOne>(s, p, t, e, temporal, k);
+    if (s.nruns > 0) e.cand[p.cand_base + s.nruns - 1] = s.last_run;
+    if (kOne && s.ref_count > 0) e.refmeta[p.meta_base] = s.one;
+    if (kOne && s.snap_pending) {
+        // runs 0 .. snap_nruns-2 are final in cand; the last one was saved
+        unsigned long long* ring = e.ring + p.ring_base;
+        const unsigned long long* cand = e.cand + p.cand_base;
+        for (uint32_t j = 0; j + 1 < s.snap_nruns; ++j) ring[wrap_add(s.one.start, j, p.ring_cap)] = cand[j];
+        ring[wrap_add(s.one.start, s.snap_nruns - 1, p.ring_cap)] = s.snap_last;
+    }
+    rec->match_count = s.match_count;
+    rec->ws = s.ws;
+    rec->len = s.len;
+    NeuronTp wq;
+    wq.cn = s.cn;
+    wq.nruns = s.nruns;
+    wq.ref_head = s.ref_head;
+    wq.ref_count = s.ref_count;
+    wq.ring_head = s.ring_head;
+    wq.ring_used = s.ring_used;
+    wq.last_match = (s.flags >> 8) & 1u;
+    e.ntp[n] = wq;
+}
+
+__global__ void __launch_bounds__(kThreads) k_temporal(Engine e) {
+    const uint32_t t = e.ts->tick;
+    const uint32_t n_touched = e.ts->n_touched;
+    const uint32_t n_due = e.ts->n_due;
+    const int temporal = e.ts->temporal_enabled;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n_touched; k += gridDim.x * blockDim.x) {
+        const uint32_t n = e.touched[k];
+        const uint32_t len = (k + 1 < n_touched ? e.tbeg[k + 1] : n_due) - e.tbeg[k];
+        if (e.nparam[n].max_refs == 1) {
+            temporal_target<true>(e, n, len, t, temporal);
+        } else {
+            temporal_target<false>(e, n, len, t, temporal);
+        }
     }
 }
 
@@ -1299,30 +1334,31 @@ __global__ void k_fire_list(Engine e) {
     }
 }
 
-// Events per (expansion block of kExpandFires fires, delay class), one
-// thread per fire.  The last block turns the counts into wheel positions
+// Events per (expansion block of kExpandFires fires, delay class), one warp
+// per fire and one lane per class.  The last block turns the counts into wheel positions
 // (exclusive scan over blocks per class, appended behind each delivery slot's
 // current contents) and finishes the tick.
-__global__ void k_fire_count(Engine e) {
+__global__ void __launch_bounds__(kFireCountThreads) k_fire_count(Engine e) {
     const uint32_t t = e.ts->tick;
     const uint32_t nfires = e.ts->n_fires;
     const uint32_t nf = nfires < e.fire_cap ? nfires : e.fire_cap;
     const uint32_t D = e.D;
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < nf; r += gridDim.x * blockDim.x) {
+    // one warp per fire, one lane per delay class
+    const uint32_t lane0 = threadIdx.x & 31;
+    const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nf; r += nwarps) {
         const uint32_t* row = e.pre_off + static_cast<size_t>(e.fire_list[r]) * (D + 1);
         uint32_t* xs = e.xsum + static_cast<size_t>(r / kExpandFires) * D;
-        uint32_t prev = row[0];
-        for (uint32_t d = 0; d < D; ++d) {
-            const uint32_t next = row[d + 1];
-            if (next != prev) atomicAdd(xs + d, next - prev);
-            prev = next;
+        for (uint32_t d = lane0; d < D; d += 32) {
+            const uint32_t c = row[d + 1] - row[d];
+            if (c) atomicAdd(xs + d, c);
         }
     }
     if (!last_block(&e.ts->done_fire_list)) return;
     if (nfires > e.fire_cap && threadIdx.x == 0) raise_status(e, kStatusFireOverflow);
     const uint32_t blocks = (nf + kExpandFires - 1) / kExpandFires;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (uint32_t d = warp; d < D; d += kThreads / 32) {
+    for (uint32_t d = warp; d < D; d += blockDim.x / 32) {
         const uint32_t slot = (t + e.cls_delta[d]) & e.wmask;
         const uint32_t start = e.slot_count[slot];
         uint32_t carry = 0;
@@ -1368,38 +1404,33 @@ __global__ void k_fire_count(Engine e) {
 }
 
 // Spike-code offset expansion (NetworkPropagator.cpp:104-130): one block per
-// fire copies the fire's pre-expanded events, class by class, to their
-// delivery slots.  Destinations were fixed by k_fire_count, so the wheel ends
-// up in exactly the reference's scheduling order.
+// fire, one warp per delay class.  A fire's events of one class are
+// contiguous in its pre-expanded list and go to one contiguous range of their
+// delivery slot: the range k_fire_count reserved for the fire's expansion
+// block, behind the block's earlier fires.  So the wheel ends up in exactly
+// the reference's scheduling order.
 __global__ void __launch_bounds__(kThreads) k_expand(Engine e) {
-    __shared__ uint32_t s_row[kMaxClasses + 1];
-    __shared__ unsigned long long s_dst[kMaxClasses];
+    __shared__ uint32_t s_rows[kExpandFires][kMaxClasses + 1];
     const uint32_t nf = e.ts->expand_fires;
     const uint32_t D = e.D;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (uint32_t r = blockIdx.x; r < nf; r += gridDim.x) {
-        const uint32_t n = e.fire_list[r];
-        const uint32_t* row = e.pre_off + static_cast<size_t>(n) * (D + 1);
-        for (uint32_t d = threadIdx.x; d <= D; d += blockDim.x) s_row[d] = row[d];
-        // destination = expansion-block base + the block's earlier fires
         const uint32_t first = r - r % kExpandFires;
-        for (uint32_t d = threadIdx.x; d < D; d += blockDim.x) {
-            unsigned long long dst = __ldcg(e.xdst + static_cast<size_t>(r / kExpandFires) * D + d);
-            for (uint32_t q = first; q < r; ++q) {
-                const uint32_t* rq = e.pre_off + static_cast<size_t>(e.fire_list[q]) * (D + 1);
-                dst += rq[d + 1] - rq[d];
-            }
-            s_dst[d] = dst;
+        const uint32_t m = r - first + 1;  // fires first .. r of the expansion block
+        for (uint32_t i = threadIdx.x; i < m * (D + 1); i += blockDim.x) {
+            const uint32_t q = i / (D + 1), d = i - q * (D + 1);
+            s_rows[q][d] = e.pre_off[static_cast<size_t>(e.fire_list[first + q]) * (D + 1) + d];
         }
         __syncthreads();
-        const unsigned long long* src = e.pre_ev + e.pre_base[n];
-        const uint32_t total = s_row[D];
-        for (uint32_t j = threadIdx.x; j < total; j += blockDim.x) {
-            uint32_t lo = 0, hi = D;  // class of event j: last d with s_row[d] <= j
-            while (hi - lo > 1) {
-                const uint32_t mid = (lo + hi) >> 1;
-                if (s_row[mid] <= j) lo = mid; else hi = mid;
-            }
-            if (e.xdst_ok[lo]) e.wheel[s_dst[lo] + (j - s_row[lo])] = src[j];
+        const unsigned long long* src = e.pre_ev + e.pre_base[e.fire_list[r]];
+        const uint32_t* row = s_rows[m - 1];
+        for (uint32_t d = warp; d < D; d += kThreads / 32) {
+            const uint32_t beg = row[d], len = row[d + 1] - beg;
+            if (len == 0 || !e.xdst_ok[d]) continue;
+            uint32_t before = 0;  // this class's events of the block's earlier fires
+            for (uint32_t q = 0; q + 1 < m; ++q) before += s_rows[q][d + 1] - s_rows[q][d];
+            unsigned long long* dst = e.wheel + __ldcg(e.xdst + static_cast<size_t>(r / kExpandFires) * D + d) + before;
+            for (uint32_t i = lane; i < len; i += 32) dst[i] = src[beg + i];
         }
         __syncthreads();
     }
@@ -1460,7 +1491,8 @@ void launch_range_counts(const Engine& e, uint32_t n_begin, uint32_t n_end, unsi
     k_range_counts<<<e.grid_wide, kThreads, 0, stream>>>(e, n_begin, n_end, tm_begin, tm_end, out);
 }
 
-void launch_tick(const Engine& e, cudaStream_t stream, cudaEvent_t* marks) {
+void launch_tick(const Engine& e, cudaStream_t stream, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join,
+                 cudaEvent_t* marks) {
     const uint32_t tiles = (e.N + kScanTile - 1) / kScanTile;
     const uint32_t wide = e.grid_wide;
     const uint32_t scan_grid = tiles == 0 ? 1 : (tiles < wide ? tiles : wide);
@@ -1473,18 +1505,28 @@ void launch_tick(const Engine& e, cudaStream_t stream, cudaEvent_t* marks) {
     mark(false); k_scan_tile<<<scan_grid, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_scan_out<<<scan_grid, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_scatter<<<wide, kThreads, 0, stream>>>(e); mark(true);
+    // the temporal update forks off here and runs beside k_events / k_process
+    // (it needs only the touched list and the group sizes; started before
+    // k_scatter it slowed that kernel's atomics more than it gained)
+    cudaEventRecord(fork, stream);
+    cudaStreamWaitEvent(side, fork, 0);
+    if (marks) cudaEventRecordWithFlags(marks[2 * 10], side, cudaEventRecordExternal);
+    k_temporal<<<e.grid_process, kThreads, 0, side>>>(e);
+    if (marks) cudaEventRecordWithFlags(marks[2 * 10 + 1], side, cudaEventRecordExternal);
+    cudaEventRecord(join, side);
     mark(false); k_events<<<e.grid_wide * 4, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_process<<<e.grid_process, kThreads, kStageEvents * sizeof(EvIn), stream>>>(e); mark(true);
-    mark(false); k_post<<<wide, kThreads, 0, stream>>>(e); mark(true);
+    mark(false); k_post<<<wide * 4, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_fire_list<<<e.grid_fire, kThreads, 0, stream>>>(e); mark(true);
-    mark(false); k_fire_count<<<e.grid_wide, kThreads, 0, stream>>>(e); mark(true);
-    mark(false); k_expand<<<wide, kThreads, 0, stream>>>(e); mark(true);
+    cudaStreamWaitEvent(stream, join, 0);  // k_fire_count finishes the tick
+    mark(false); k_fire_count<<<e.grid_wide / 4 + 1, kFireCountThreads, 0, stream>>>(e); mark(true);
+    mark(false); k_expand<<<e.grid_wide * 4, kThreads, 0, stream>>>(e); mark(true);
 }
 
 const char* kernel_name(int index) {
     static const char* names[kKernelCount] = {"k_hist",    "k_scan_tile", "k_scan_out",   "k_scatter",
                                               "k_events",  "k_process",   "k_post",       "k_fire_list",
-                                              "k_fire_count", "k_expand"};
+                                              "k_fire_count", "k_expand", "k_temporal"};
     return index >= 0 && index < kKernelCount ? names[index] : "";
 }
 

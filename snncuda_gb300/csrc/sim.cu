@@ -162,6 +162,9 @@ struct snncuda_sim {
     cudaEvent_t marks[2 * kKernelCount]{};
     static constexpr int kTicksPerGraph = 16;
 
+    // second stream of the tick graphs (k_temporal) and its fork/join events
+    cudaStream_t side{nullptr};
+    cudaEvent_t fork_ev{nullptr}, join_ev{nullptr};
     // asynchronous runs (run_enqueue / run_complete)
     TickState* ts_pinned{nullptr};  // tick state copied back at the end of a run
     cudaEvent_t run_done{nullptr};
@@ -170,6 +173,8 @@ struct snncuda_sim {
 
     ~snncuda_sim() {
         if (run_done) cudaEventDestroy(run_done);
+        if (fork_ev) cudaEventDestroy(fork_ev);
+        if (join_ev) cudaEventDestroy(join_ev);
         if (ts_pinned) cudaFreeHost(ts_pinned);
         if (graph_many) cudaGraphExecDestroy(graph_many);
         if (graph_one) cudaGraphExecDestroy(graph_one);
@@ -187,6 +192,7 @@ struct snncuda_sim {
         if (inj_off) cudaFreeAsync(inj_off, stream);
         if (host_ev) cudaFreeHost(host_ev);
         if (host_idx) cudaFreeHost(host_idx);
+        if (side) cudaStreamDestroy(side);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
 
@@ -218,7 +224,7 @@ struct snncuda_sim {
         if (profiled && marks[0] == nullptr)
             for (cudaEvent_t& ev : marks) check(cudaEventCreate(&ev), "event");
         check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-        for (int i = 0; i < ticks; ++i) launch_tick(e, stream, profiled ? marks : nullptr);
+        for (int i = 0; i < ticks; ++i) launch_tick(e, stream, side, fork_ev, join_ev, profiled ? marks : nullptr);
         check(cudaStreamEndCapture(stream, &g), "end capture");
         cudaGraphExec_t exec = nullptr;
         const cudaError_t err = cudaGraphInstantiate(&exec, g, 0);
@@ -315,6 +321,9 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
         check(cudaStreamCreateWithFlags(&sim->stream, cudaStreamNonBlocking), "stream");
         sim->own_stream = true;
     }
+    check(cudaStreamCreateWithFlags(&sim->side, cudaStreamNonBlocking), "stream");
+    check(cudaEventCreateWithFlags(&sim->fork_ev, cudaEventDisableTiming), "event");
+    check(cudaEventCreateWithFlags(&sim->join_ev, cudaEventDisableTiming), "event");
     sim->N = N;
     sim->S = S;
     sim->config = cfg;
@@ -901,7 +910,7 @@ static void read_neurons_range(snncuda_sim* sim, uint32_t n0, uint32_t n1, const
         if (o->offset_count) o->offset_count[i] = r[i].len;
         if (o->learned_count) o->learned_count[i] = q[i].ref_count;
         if (o->match_count) o->match_count[i] = r[i].match_count;
-        if (o->last_match) o->last_match[i] = (r[i].flags >> 8) & 1u;
+        if (o->last_match) o->last_match[i] = q[i].last_match;
     }
 }
 
@@ -1018,7 +1027,7 @@ static void digest_range(snncuda_sim* sim, const HostState& h, uint32_t n0, uint
                 d.word(v.size());
                 for (uint32_t x : v) d.word(x);
             }
-            d.word((r.flags >> 8) & 1u);
+            d.word(h.ntp[n].last_match);
             d.word(r.match_count);
         }
         *neuron_digest = d.h;
