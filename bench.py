@@ -53,7 +53,7 @@ KERNELS_PER_TICK = 11   # launch_tick in snncuda_gb300/csrc/kernels.cu
 # DRAM bytes (read + write) per launch of a kernel on the default stdp_100k
 # workload, from one ncu capture of this code (profiles/); reported as
 # roofline.traffic for the dominant kernel.
-MEASURED_TRAFFIC = {("stdp_100k", "k_events"): 159.0e6 + 96.6e6, ("stdp_100k", "k_process"): 55.3e6 + 0.1e6}
+MEASURED_TRAFFIC = {("stdp_100k", "k_events"): 159.0e6 + 96.6e6}
 
 # Algorithmic bytes of the two per-event kernels (device layout in
 # snncuda_gb300/csrc/engine.h), per synaptic event, per external event and
@@ -62,12 +62,15 @@ MEASURED_TRAFFIC = {("stdp_100k", "k_events"): 159.0e6 + 96.6e6, ("stdp_100k", "
 #              the record (64), the event's input (16) and the STDP snapshot
 #              (32); external events: entry + input; per target its
 #              parameters (64) and segment bounds (12)
-#   k_process  reads each event's input (16); per target its parameters (64),
-#              dynamic and temporal records read + write (128 + 64) and one
-#              run append (8)
+#   k_process  reads each event's input (16); per target its threshold (4)
+#              and the physics fields of its record, read + write (2 x 52)
+#   k_temporal per target: parameters (64), temporal record read + write
+#              (2 x 32), the temporal fields of the neuron record (2 x 12) and
+#              one run of the window (2 x 8)
 BYTES_MODEL = {
     "k_events": (8 + 64 + 64 + 16 + 32, 8 + 16, 64 + 12),
-    "k_process": (16, 16, 64 + 128 + 64 + 8),
+    "k_process": (16, 16, 4 + 2 * 52),
+    "k_temporal": (0, 0, 64 + 2 * 32 + 2 * 12 + 2 * 8),
 }
 
 
@@ -425,6 +428,8 @@ def main():
                     help="batched form: this many networks in one handle vs one handle per network")
     ap.add_argument("--batch-ticks", type=int, default=500)
     ap.add_argument("--batch-neurons", type=str, default="1000,20000", help="log-uniform range of N")
+    ap.add_argument("--rmw-floor", action="store_true",
+                    help="time random 64-byte record read-modify-writes (the per-event access floor)")
     ap.add_argument("--serve", action="store_true", help="serving: Poisson arrivals under a memory budget")
     ap.add_argument("--serve-rate", type=float, default=4.0, help="job arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=15.0, help="arrival window")
@@ -436,6 +441,13 @@ def main():
     args = ap.parse_args()
     if args.serve:
         print(json.dumps(run_serving(args)), flush=True)
+        return
+    if args.rmw_floor:
+        import __graft_entry__
+        __graft_entry__.build()
+        out = subprocess.run([str(ROOT / "snncuda_gb300" / "_lib" / "rmw_floor")], check=True,
+                             stdout=subprocess.PIPE, text=True).stdout
+        print(out.strip(), flush=True)
         return
     if args.batched:
         print(json.dumps(run_batched(args)), flush=True)
