@@ -135,7 +135,7 @@ class SynapseState(Structure):
     ]
 
 
-KERNEL_COUNT = 11
+KERNEL_COUNT = 12
 
 
 class Profile(Structure):

@@ -162,7 +162,8 @@ struct TickState {
     uint32_t n_due;           // events due this tick
     uint32_t n_touched;       // targets with at least one due event
     uint32_t n_fires;         // fires this tick
-    uint32_t n_fired_targets; // distinct targets that fired this tick
+    uint32_t n_fired_targets; // distinct targets that fired this tick (reset by k_hist)
+    uint32_t post_tick;       // tick of the pending post-spike STDP (set by k_hist; read by k_post)
     uint32_t expand_fires;    // fires whose events k_expand copies
     uint32_t far_first_tick;  // delivery tick of far_idx[0] for the current run
     uint32_t far_ticks;       // entries of far_idx minus one (0 = none)
@@ -258,11 +259,15 @@ constexpr uint32_t kMaxClasses = 256;    // distinct delivery delays
 // Host-side launchers (kernels.cu).
 // `marks` (optional) holds 2 * kKernelCount events recorded around every
 // kernel (before, after) for profiling graphs.
-constexpr int kKernelCount = 11;
-// One tick on `stream`; k_temporal runs on `side` (forked after the grouping
-// scan with `fork`, joined back with `join` before the tick is finished).
-void launch_tick(const Engine& e, cudaStream_t stream, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join,
-                 cudaEvent_t* marks = nullptr);
+constexpr int kKernelCount = 12;
+// The streams of a tick: k_temporal and k_post run on `side`, forked from
+// `main` with ev[0] / ev[2] and joined back with ev[1] / ev[3].
+struct TickStreams {
+    cudaStream_t main;
+    cudaStream_t side;
+    cudaEvent_t ev[4];
+};
+void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks = nullptr);
 const char* kernel_name(int index);
 void launch_inject(const Engine& e, const unsigned long long* ev, const uint32_t* slot_of_group,
                    const uint32_t* group_off, uint32_t groups, cudaStream_t stream);

@@ -684,7 +684,11 @@ __global__ void k_hist(Engine e) {
     }
     ext = __reduce_add_sync(0xffffffffu, ext);
     if ((threadIdx.x & 31) == 0 && ext) atomicAdd(&e.ts->external, static_cast<unsigned long long>(ext));
-    if (blockIdx.x == 0 && threadIdx.x == 0) e.ts->n_due = n;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        e.ts->n_due = n;
+        e.ts->post_tick = t;        // the previous tick's k_post has finished
+        e.ts->n_fired_targets = 0;
+    }
 }
 
 // Phase 1 of the per-target scan: tile sums of counts and of touched targets;
@@ -1268,10 +1272,11 @@ __global__ void k_init_syn(SynAB* syn, const SynA* a, unsigned long long S) {
 
 // Post-spike STDP over the incoming rows of every target that fired
 // (NetworkPropagator.cpp:95-102), one block per fired target, coalesced over
-// the target-major row; then popcounts of the fire bitmap tiles, whose last
-// block turns into exclusive tile bases.
+// the target-major row.  Runs on the side stream beside k_fire_tiles ..
+// k_expand (none of which touches synapse records), so it reads the tick
+// from post_tick, not from the tick counter k_fire_count advances.
 __global__ void k_post(Engine e) {
-    const uint32_t t = e.ts->tick;
+    const uint32_t t = e.ts->post_tick;
     const uint32_t nf = e.ts->n_fired_targets;
     const int stdp = e.ts->stdp_enabled;
     for (uint32_t j = blockIdx.x; j < nf; j += gridDim.x) {
@@ -1287,7 +1292,11 @@ __global__ void k_post(Engine e) {
             if (post_catch_up(a, t, fires, e, stdp)) e.syn[tm].a = a;
         }
     }
-    // fire bitmap tile popcounts (one thread per bitmap word)
+}
+
+// Popcounts of the fire bitmap tiles; the last block turns them into
+// exclusive tile bases and the tick's fire count.
+__global__ void k_fire_tiles(Engine e) {
     const uint32_t words = (e.ts->n_due + 31) / 32;
     const uint32_t tiles = (words + kThreads - 1) / kThreads;
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
@@ -1398,7 +1407,6 @@ __global__ void __launch_bounds__(kFireCountThreads) k_fire_count(Engine e) {
         ts->expand_fires = nf;
         e.slot_count[t & e.wmask] = 0;
         ts->n_touched = 0;
-        ts->n_fired_targets = 0;
         ts->tick = t + 1;
     }
 }
@@ -1491,15 +1499,18 @@ void launch_range_counts(const Engine& e, uint32_t n_begin, uint32_t n_end, unsi
     k_range_counts<<<e.grid_wide, kThreads, 0, stream>>>(e, n_begin, n_end, tm_begin, tm_end, out);
 }
 
-void launch_tick(const Engine& e, cudaStream_t stream, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join,
-                 cudaEvent_t* marks) {
+void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     const uint32_t tiles = (e.N + kScanTile - 1) / kScanTile;
     const uint32_t wide = e.grid_wide;
     const uint32_t scan_grid = tiles == 0 ? 1 : (tiles < wide ? tiles : wide);
+    cudaStream_t stream = s.main;
     int k = 0;
     auto mark = [&](bool after) {
         if (marks) cudaEventRecordWithFlags(marks[2 * k + (after ? 1 : 0)], stream, cudaEventRecordExternal);
         if (after) ++k;
+    };
+    auto side_mark = [&](int index, bool after) {
+        if (marks) cudaEventRecordWithFlags(marks[2 * index + (after ? 1 : 0)], s.side, cudaEventRecordExternal);
     };
     mark(false); k_hist<<<wide, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_scan_tile<<<scan_grid, kThreads, 0, stream>>>(e); mark(true);
@@ -1508,25 +1519,34 @@ void launch_tick(const Engine& e, cudaStream_t stream, cudaStream_t side, cudaEv
     // the temporal update forks off here and runs beside k_events / k_process
     // (it needs only the touched list and the group sizes; started before
     // k_scatter it slowed that kernel's atomics more than it gained)
-    cudaEventRecord(fork, stream);
-    cudaStreamWaitEvent(side, fork, 0);
-    if (marks) cudaEventRecordWithFlags(marks[2 * 10], side, cudaEventRecordExternal);
-    k_temporal<<<e.grid_process, kThreads, 0, side>>>(e);
-    if (marks) cudaEventRecordWithFlags(marks[2 * 10 + 1], side, cudaEventRecordExternal);
-    cudaEventRecord(join, side);
+    cudaEventRecord(s.ev[0], stream);
+    cudaStreamWaitEvent(s.side, s.ev[0], 0);
+    side_mark(10, false);
+    k_temporal<<<e.grid_process, kThreads, 0, s.side>>>(e);
+    side_mark(10, true);
+    cudaEventRecord(s.ev[1], s.side);
     mark(false); k_events<<<e.grid_wide * 4, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_process<<<e.grid_process, kThreads, kStageEvents * sizeof(EvIn), stream>>>(e); mark(true);
-    mark(false); k_post<<<wide * 4, kThreads, 0, stream>>>(e); mark(true);
+    // post-spike STDP of the fired targets runs beside the fire ordering and
+    // the expansion (synapse records are not touched by those)
+    cudaEventRecord(s.ev[2], stream);
+    cudaStreamWaitEvent(s.side, s.ev[2], 0);
+    side_mark(11, false);
+    k_post<<<wide * 4, kThreads, 0, s.side>>>(e);
+    side_mark(11, true);
+    cudaEventRecord(s.ev[3], s.side);
+    mark(false); k_fire_tiles<<<wide, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_fire_list<<<e.grid_fire, kThreads, 0, stream>>>(e); mark(true);
-    cudaStreamWaitEvent(stream, join, 0);  // k_fire_count finishes the tick
+    cudaStreamWaitEvent(stream, s.ev[1], 0);  // k_temporal reads the tick counter k_fire_count advances
     mark(false); k_fire_count<<<e.grid_wide / 4 + 1, kFireCountThreads, 0, stream>>>(e); mark(true);
     mark(false); k_expand<<<e.grid_wide * 4, kThreads, 0, stream>>>(e); mark(true);
+    cudaStreamWaitEvent(stream, s.ev[3], 0);  // the next tick's k_events reads the synapse records
 }
 
 const char* kernel_name(int index) {
     static const char* names[kKernelCount] = {"k_hist",    "k_scan_tile", "k_scan_out",   "k_scatter",
-                                              "k_events",  "k_process",   "k_post",       "k_fire_list",
-                                              "k_fire_count", "k_expand", "k_temporal"};
+                                              "k_events",  "k_process",   "k_fire_tiles", "k_fire_list",
+                                              "k_fire_count", "k_expand", "k_temporal",  "k_post"};
     return index >= 0 && index < kKernelCount ? names[index] : "";
 }
 

@@ -164,7 +164,7 @@ struct snncuda_sim {
 
     // second stream of the tick graphs (k_temporal) and its fork/join events
     cudaStream_t side{nullptr};
-    cudaEvent_t fork_ev{nullptr}, join_ev{nullptr};
+    cudaEvent_t tick_ev[4]{};
     // asynchronous runs (run_enqueue / run_complete)
     TickState* ts_pinned{nullptr};  // tick state copied back at the end of a run
     cudaEvent_t run_done{nullptr};
@@ -173,8 +173,8 @@ struct snncuda_sim {
 
     ~snncuda_sim() {
         if (run_done) cudaEventDestroy(run_done);
-        if (fork_ev) cudaEventDestroy(fork_ev);
-        if (join_ev) cudaEventDestroy(join_ev);
+        for (cudaEvent_t ev : tick_ev)
+            if (ev) cudaEventDestroy(ev);
         if (ts_pinned) cudaFreeHost(ts_pinned);
         if (graph_many) cudaGraphExecDestroy(graph_many);
         if (graph_one) cudaGraphExecDestroy(graph_one);
@@ -224,7 +224,8 @@ struct snncuda_sim {
         if (profiled && marks[0] == nullptr)
             for (cudaEvent_t& ev : marks) check(cudaEventCreate(&ev), "event");
         check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-        for (int i = 0; i < ticks; ++i) launch_tick(e, stream, side, fork_ev, join_ev, profiled ? marks : nullptr);
+        const TickStreams ts{stream, side, {tick_ev[0], tick_ev[1], tick_ev[2], tick_ev[3]}};
+        for (int i = 0; i < ticks; ++i) launch_tick(e, ts, profiled ? marks : nullptr);
         check(cudaStreamEndCapture(stream, &g), "end capture");
         cudaGraphExec_t exec = nullptr;
         const cudaError_t err = cudaGraphInstantiate(&exec, g, 0);
@@ -322,8 +323,7 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
         sim->own_stream = true;
     }
     check(cudaStreamCreateWithFlags(&sim->side, cudaStreamNonBlocking), "stream");
-    check(cudaEventCreateWithFlags(&sim->fork_ev, cudaEventDisableTiming), "event");
-    check(cudaEventCreateWithFlags(&sim->join_ev, cudaEventDisableTiming), "event");
+    for (cudaEvent_t& ev : sim->tick_ev) check(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
     sim->N = N;
     sim->S = S;
     sim->config = cfg;
