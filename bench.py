@@ -135,6 +135,19 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def combine_ranks(ms, events, world, dist=None, device="cpu"):
+    """Replicas only: every rank runs its own copy of the workload; the job's
+    time is the slowest rank's, its work the sum over ranks."""
+    if world <= 1 or dist is None:
+        return ms, float(events)
+    import torch
+    t = torch.tensor([ms, float(events)], dtype=torch.float64, device=device)
+    mx = t.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(mx[0]), float(t[1])
+
+
 def tick_roofline(w, events, fires, ext, prof, ticks, ms):
     """Whole-tick roofline: minimal algorithmic bytes of the tick loop (a
     compact structure-of-arrays design, per-term below) over the timed ticks,
@@ -527,14 +540,7 @@ def main():
     events = c1["synaptic_events"] - c0["synaptic_events"]
     ext_events = c1["external_events"] - c0["external_events"]
     fires = c1["fired_spikes"] - c0["fired_spikes"]
-    if world > 1:
-        t = torch.tensor([ms, float(events)], dtype=torch.float64, device=dev)
-        mx = t.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        ms_max, events_all = float(mx[0]), float(t[1])
-    else:
-        ms_max, events_all = ms, float(events)
+    ms_max, events_all = combine_ranks(ms, events, world, dist if world > 1 else None, dev)
     value = events_all / (ms_max / 1e3)
 
     # ---- per-kernel profile for the roofline -------------------------------
