@@ -1512,7 +1512,7 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     auto side_mark = [&](int index, bool after) {
         if (marks) cudaEventRecordWithFlags(marks[2 * index + (after ? 1 : 0)], s.side, cudaEventRecordExternal);
     };
-    mark(false); k_hist<<<wide, kThreads, 0, stream>>>(e); mark(true);
+    mark(false); k_hist<<<wide * 4, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_scan_tile<<<scan_grid, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_scan_out<<<scan_grid, kThreads, 0, stream>>>(e); mark(true);
     mark(false); k_scatter<<<wide, kThreads, 0, stream>>>(e); mark(true);
