@@ -536,6 +536,8 @@ def main():
     if world > 1:
         dist.barrier()
     c1 = sim.counters()
+    # recognition workloads: the sums the reference's recognition metric adds up
+    recognition = sim.recognition() if w.stimulus_codes else None
     ms = ev0.elapsed_time(ev1)
     events = c1["synaptic_events"] - c0["synaptic_events"]
     ext_events = c1["external_events"] - c0["external_events"]
@@ -623,6 +625,7 @@ def main():
             "gpu_launches": args.steps * tps * KERNELS_PER_TICK,
             "tick_roofline": tick_roofline(w, events, fires, ext_events, prof, args.steps * tps, ms_max),
             "clocks": clocks, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            **({"recognition": recognition} if recognition is not None else {}),
         }
         print(json.dumps(line), flush=True)
     if world > 1:

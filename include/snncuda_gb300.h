@@ -302,6 +302,12 @@ typedef struct snncuda_profile {
     uint64_t touched_targets;   /* sum over ticks of targets with due events */
 } snncuda_profile;
 int snncuda_sim_profile(snncuda_sim* sim, uint64_t inclusive_tick, snncuda_profile* out);
+
+/* Recognition sums (engine extension): the sum over neurons of
+ * temporal_pattern.match_count and over synapses of code_match_count,
+ * reduced on the device (reading every record back would move the whole
+ * synapse state). */
+int snncuda_sim_recognition(snncuda_sim* sim, uint64_t* neuron_matches, uint64_t* synapse_code_matches);
 const char* snncuda_kernel_name(int32_t index);
 
 /* ---- building block: group a tick's due events by target ----------------

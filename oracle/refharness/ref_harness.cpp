@@ -506,6 +506,23 @@ int snncuda_sim_profile(snncuda_sim* sim, uint64_t inclusive_tick, snncuda_profi
 
 const char* snncuda_kernel_name(int32_t) { return ""; }
 
+int snncuda_sim_recognition(snncuda_sim* sim, uint64_t* neuron_matches, uint64_t* synapse_code_matches) {
+    if (sim == nullptr) return fail(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
+    uint64_t a = 0, b = 0;
+    std::vector<uint64_t> m(sim->connectome.neurons.size()), c(sim->connectome.synapses.size());
+    snncuda_neuron_state ns{};
+    ns.match_count = m.data();
+    snncuda_synapse_state ss{};
+    ss.code_match_count = c.data();
+    snncuda_sim_read_neurons(sim, &ns);
+    snncuda_sim_read_synapses(sim, &ss);
+    for (uint64_t v : m) a += v;
+    for (uint64_t v : c) b += v;
+    if (neuron_matches) *neuron_matches = a;
+    if (synapse_code_matches) *synapse_code_matches = b;
+    return SNNCUDA_OK;
+}
+
 // Stable grouping of an event buffer by target (host memory here).
 int snncuda_group_events(const uint64_t* events, uint32_t count, uint32_t neuron_count, uint64_t* grouped,
                          uint32_t* segment_start, void*) {

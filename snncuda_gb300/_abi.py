@@ -172,6 +172,7 @@ _SIGNATURES = {
                                         POINTER(c_uint32)]),
     "snncuda_sim_profile": (c_int, [c_void_p, c_uint64, POINTER(Profile)]),
     "snncuda_kernel_name": (c_char_p, [c_int32]),
+    "snncuda_sim_recognition": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64)]),
     "snncuda_batch_create": (c_int, [c_uint32, POINTER(Network), POINTER(c_int32), POINTER(Config),
                                      POINTER(c_void_p)]),
     "snncuda_batch_destroy": (c_int, [c_void_p]),

@@ -279,7 +279,9 @@ void launch_group(const Engine& e, cudaStream_t stream);
 void launch_rule_off(const Engine& e, unsigned long long tm_begin, unsigned long long tm_end, cudaStream_t stream);
 // out[0] += spike counts of neurons [n_begin, n_end); out[1] += pre-spike
 // counts of target-major synapses [tm_begin, tm_end); out[2] += wheel events
-// (all slots) whose target is in [n_begin, n_end).  out must start at zero.
+// (all slots) whose target is in [n_begin, n_end); out[3] += the neurons'
+// temporal match counts; out[4] += the synapses' code match counts.  out (5
+// entries) must start at zero.
 void launch_range_counts(const Engine& e, uint32_t n_begin, uint32_t n_end, unsigned long long tm_begin,
                          unsigned long long tm_end, unsigned long long* out, cudaStream_t stream);
 // One-time kernel attributes (dynamic shared memory of k_process); call with

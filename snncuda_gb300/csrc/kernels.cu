@@ -1472,9 +1472,15 @@ __global__ void k_range_counts(Engine e, uint32_t nb, uint32_t ne, unsigned long
                                unsigned long long* out) {
     const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
     const unsigned long long first = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
-    unsigned long long spikes = 0, pre = 0, wheel = 0;
-    for (unsigned long long n = nb + first; n < ne; n += stride) spikes += e.nrec[n].spike_count;
-    for (unsigned long long i = tb + first; i < te; i += stride) pre += e.syn[i].b.pre_count;
+    unsigned long long spikes = 0, pre = 0, wheel = 0, matches = 0, code_matches = 0;
+    for (unsigned long long n = nb + first; n < ne; n += stride) {
+        spikes += e.nrec[n].spike_count;
+        matches += e.nrec[n].match_count;
+    }
+    for (unsigned long long i = tb + first; i < te; i += stride) {
+        pre += e.syn[i].b.pre_count;
+        code_matches += e.syn[i].b.code_matches;
+    }
     for (uint32_t slot = 0; slot < e.W; ++slot) {
         const uint32_t cnt = e.slot_count[slot];
         const unsigned long long* ev = e.wheel + static_cast<size_t>(slot) * e.slot_cap;
@@ -1486,6 +1492,8 @@ __global__ void k_range_counts(Engine e, uint32_t nb, uint32_t ne, unsigned long
     if (spikes) atomicAdd(out, spikes);
     if (pre) atomicAdd(out + 1, pre);
     if (wheel) atomicAdd(out + 2, wheel);
+    if (matches) atomicAdd(out + 3, matches);
+    if (code_matches) atomicAdd(out + 4, code_matches);
 }
 
 }  // namespace

@@ -1242,6 +1242,27 @@ int snncuda_sim_read_raster(snncuda_sim* sim, uint64_t first, uint64_t count, ui
 }
 
 
+int snncuda_sim_recognition(snncuda_sim* sim, uint64_t* neuron_matches, uint64_t* synapse_code_matches) {
+    if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
+    return guarded([&] {
+        cudaStream_t st = sim->stream;
+        unsigned long long* d = nullptr;
+        check(cudaMallocAsync(&d, 5 * sizeof(unsigned long long), st), "device allocation");
+        unsigned long long c[5] = {};
+        cudaError_t err = cudaMemsetAsync(d, 0, sizeof(c), st);
+        if (err == cudaSuccess) {
+            launch_range_counts(sim->e, 0, sim->N, 0, sim->S, d, st);
+            err = cudaGetLastError();
+        }
+        if (err == cudaSuccess) err = cudaMemcpyAsync(c, d, sizeof(c), cudaMemcpyDeviceToHost, st);
+        cudaFreeAsync(d, st);
+        if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+        check(err, "recognition sums");
+        if (neuron_matches) *neuron_matches = c[3];
+        if (synapse_code_matches) *synapse_code_matches = c[4];
+    });
+}
+
 // ---------------------------------------------------------------------------
 // batched form: the networks of a batch are one disjoint union inside a
 // single simulation.  Network i owns neurons [nbase[i], nbase[i+1]) and
@@ -1259,7 +1280,7 @@ struct snncuda_batch {
     std::vector<uint32_t> nbase;                   // [count + 1]
     std::vector<uint64_t> sbase;                   // [count + 1]
     std::vector<std::vector<uint64_t>> inj_ticks;  // per network: clamped delivery tick of each injection
-    unsigned long long* d_counts{nullptr};         // [3] scratch of launch_range_counts
+    unsigned long long* d_counts{nullptr};         // [5] scratch of launch_range_counts
     ~snncuda_batch() {
         if (d_counts) cudaFree(d_counts);
         delete sim;
@@ -1330,7 +1351,7 @@ static snncuda_batch* batch_create_impl(uint32_t count, const snncuda_network* n
     for (uint32_t i = 0; i < count; ++i)
         if (stdp_enabled && !stdp_enabled[i]) launch_rule_off(b->sim->e, b->tm_begin(i), b->tm_end(i), b->sim->stream);
     check(cudaGetLastError(), "batch rule launch");
-    check(cudaMalloc(&b->d_counts, 3 * sizeof(unsigned long long)), "cudaMalloc");
+    check(cudaMalloc(&b->d_counts, 5 * sizeof(unsigned long long)), "cudaMalloc");
     check(cudaStreamSynchronize(b->sim->stream), "batch create synchronize");
     return b.release();
 }
@@ -1408,10 +1429,10 @@ int snncuda_batch_counters(snncuda_batch* b, uint32_t i, snncuda_counters* out) 
     return guarded([&] {
         snncuda_sim* sim = b->sim;
         cudaStream_t st = sim->stream;
-        check(cudaMemsetAsync(b->d_counts, 0, 3 * sizeof(unsigned long long), st), "memset");
+        check(cudaMemsetAsync(b->d_counts, 0, 5 * sizeof(unsigned long long), st), "memset");
         launch_range_counts(sim->e, b->nbase[i], b->nbase[i + 1], b->tm_begin(i), b->tm_end(i), b->d_counts, st);
         check(cudaGetLastError(), "count launch");
-        unsigned long long c[3];
+        unsigned long long c[5];
         check(cudaMemcpyAsync(c, b->d_counts, sizeof(c), cudaMemcpyDeviceToHost, st), "counts");
         const TickState ts = sim->read_ts();  // synchronizes the stream
         uint64_t external = 0;

@@ -236,6 +236,13 @@ class Simulation:
                 "synaptic_events": int(out.synaptic_events), "external_events": int(out.external_events),
                 "fires": int(out.fires), "touched_targets": int(out.touched_targets)}
 
+    def recognition(self) -> Dict[str, int]:
+        """Sum of the neurons' temporal match counts and of the synapses' code
+        match counts."""
+        a, b = c_uint64(), c_uint64()
+        _check(self.lib, self.lib.snncuda_sim_recognition(self.handle, ctypes.byref(a), ctypes.byref(b)))
+        return {"neuron_matches": int(a.value), "synapse_code_matches": int(b.value)}
+
     def digest(self) -> tuple:
         a, b = c_uint64(), c_uint64()
         _check(self.lib, self.lib.snncuda_sim_state_digest(self.handle, ctypes.byref(a), ctypes.byref(b)))

@@ -79,3 +79,24 @@ def test_slot_overflow_is_reported_and_poisons(gpu_lib):
         sim.run_until(300)
     assert err.value.status == 7
     assert sim.counters()["next_tick"] >= 0   # readers still work
+
+
+@pytest.mark.gpu
+def test_recognition_sums_match_oracle(gpu_lib, port_lib):
+    """Device-reduced recognition sums (neuron temporal matches, synapse code
+    matches) on the recognition workload's distributions."""
+    w = synthetic.RECOG_1M.scaled(neurons=3000, fanout=80, weight_scale=0.05, max_weight=0.2, seed=31, ticks=300)
+    net = synthetic.build_network(w)
+    drive = synthetic.build_drive(w, 300)
+    got = []
+    for lib in (gpu_lib, port_lib):
+        sim = Simulation(net, default_config(lib, max_weight=1.0), lib)
+        sim.inject(*drive)
+        sim.run_until(299)
+        got.append(sim.recognition())
+        n, s = sim.neurons(), sim.synapses()
+        assert got[-1]["neuron_matches"] == int(n["match_count"].sum())
+        assert got[-1]["synapse_code_matches"] == int(s["code_match_count"].sum())
+        sim.close()
+    assert got[0] == got[1]
+    assert got[0]["neuron_matches"] > 0 and got[0]["synapse_code_matches"] > 0
