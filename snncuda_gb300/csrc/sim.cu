@@ -523,8 +523,11 @@ void sort_pending(snncuda_sim* sim) {
     if (sim->pend_sorted < pend.size()) {
         auto by_tick = [](const Pending& a, const Pending& b) { return a.tick < b.tick; };
         const auto mid = pend.begin() + static_cast<std::ptrdiff_t>(sim->pend_sorted);
-        std::stable_sort(mid, pend.end(), by_tick);
-        std::inplace_merge(pend.begin() + static_cast<std::ptrdiff_t>(sim->pend_head), mid, pend.end(), by_tick);
+        // a drive injected in tick order (the common case) needs no sort, and
+        // one that starts at or after every queued event needs no merge
+        if (!std::is_sorted(mid, pend.end(), by_tick)) std::stable_sort(mid, pend.end(), by_tick);
+        if (sim->pend_sorted > sim->pend_head && by_tick(*mid, *(mid - 1)))
+            std::inplace_merge(pend.begin() + static_cast<std::ptrdiff_t>(sim->pend_head), mid, pend.end(), by_tick);
         sim->pend_sorted = pend.size();
     }
 }
