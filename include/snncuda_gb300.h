@@ -326,7 +326,8 @@ const char* snncuda_kernel_name(int32_t index);
  *                  word of each target; [neuron_count] = count
  * Runs on cuda_stream (NULL: the legacy default stream) and returns when the
  * device has finished.  Allocates and frees its scratch on every call.
- * A target >= neuron_count fails with SNNCUDA_ERR_INVALID_ARGUMENT. */
+ * A target >= neuron_count, or events overlapping grouped (no in-place
+ * grouping), fails with SNNCUDA_ERR_INVALID_ARGUMENT. */
 int snncuda_group_events(const uint64_t* events, uint32_t count, uint32_t neuron_count, uint64_t* grouped,
                          uint32_t* segment_start, void* cuda_stream);
 

@@ -682,6 +682,8 @@ int snncuda_group_events(const uint64_t* events, uint32_t count, uint32_t neuron
                          uint32_t* segment_start, void*) {
     if ((count > 0 && (events == nullptr || grouped == nullptr)) || segment_start == nullptr)
         return fail(SNNCUDA_ERR_INVALID_ARGUMENT, "null array");
+    if (count > 0 && events < grouped + count && grouped < events + count)
+        return fail(SNNCUDA_ERR_INVALID_ARGUMENT, "events and grouped overlap");
     std::vector<uint32_t> start(static_cast<size_t>(neuron_count) + 1, 0);
     for (uint32_t i = 0; i < count; ++i) {
         const uint32_t tgt = static_cast<uint32_t>(events[i]) & 0x7FFFFFFFu;

@@ -2,10 +2,11 @@
 //
 // One tick t processes wheel slot t mod W, whose buffer holds the events due
 // at t in the exact order the reference scheduler would pop them
-// (SpikeScheduler.cpp:25-47: bucket FIFO order).  Per tick:
+// (SpikeScheduler.cpp:25-47: bucket FIFO order).  Per tick, on the main
+// stream:
 //
-//  1. k_hist       count due events per target (and move far-future injects
-//                  that become reachable into the wheel)
+//  1. k_hist       count due events per target (and move far-future
+//                  injections that become reachable into the wheel)
 //  2. k_scan_tile  exclusive scan of the per-target counts (+ last block
 //                  scans the tile sums)
 //  3. k_scan_out   segment starts and the ascending list of touched targets
@@ -19,18 +20,28 @@
 //                  its events in due order (:175-229), redoing the STDP of
 //                  events that follow a fire of the target; fires into a
 //                  due-position bitmap
-//  7. k_post       post-spike STDP over the in-rows of targets that fired
-//                  (:138-173) + fire tile counts
+//  7. k_fire_tiles fire counts per tile of the bitmap
 //  8. k_fire_list  fires in due order (= reference fire order), raster
 //  9. k_fire_count events per (fire block, delay class); the last block scans
 //                  destinations and finishes the tick
 // 10. k_expand     copy each fire's pre-expanded (synapse, offset) events into
 //                  their delivery slots, order-preserving
-// 11. k_temporal   the neuron temporal pattern of every touched target, once
-//                  per tick, on a second stream beside 5-6 (graph fork/join)
 //
-// Every wait is a kernel boundary or a "last block" hand-off (an atomic
-// counter, no spinning), so no kernel here can hang.
+// and on a second stream (graph fork/join):
+//
+// 11. k_temporal   the neuron temporal pattern of every touched target, once
+//                  per tick, beside 5-6
+// 12. k_post       post-spike STDP over the in-rows of targets that fired
+//                  (:138-173), beside 7-10
+//
+// Main-stream kernels that directly follow another are launched as
+// programmatic dependents (tick_enter), so each is scheduled while the one
+// before it drains.
+//
+// Every wait is a kernel boundary (a programmatic dependent's grid
+// dependency wait included), a "last block" hand-off (an atomic counter, no
+// spinning) or the time-bounded mbarrier wait of k_process's staging copy,
+// so no kernel here can hang.
 // Float arithmetic uses explicitly rounded intrinsics so nothing is
 // contracted into an FMA: each operation rounds exactly as the reference's
 // separately evaluated float expressions.
@@ -59,6 +70,17 @@ __device__ __forceinline__ float rec_gain(uint32_t r) { return r == 1 ? 0.55f : 
 __device__ __forceinline__ float rec_sign(uint32_t r) { return r >= 2 ? -1.0f : 1.0f; }
 
 __device__ __forceinline__ void raise_status(const Engine& e, uint32_t bit) { atomicOr(&e.ts->status, bit); }
+
+// First statement of every main-stream tick kernel.  A kernel launched as a
+// programmatic dependent of the previous kernel on its stream is scheduled
+// while that kernel still runs and waits here until it has completed and its
+// writes are visible (for any other launch the wait returns at once); then it
+// lets its own dependent be scheduled.  The wait is the hardware's grid
+// dependency, not a spin on memory.
+__device__ __forceinline__ void tick_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
 
 // ---------------------------------------------------------------------------
 // bulk copies into shared memory (TMA, cp.async.bulk) with an mbarrier
@@ -648,6 +670,7 @@ __device__ void code_update(SynB& b, const NeuronParam& p, uint32_t t, uint16_t*
 // whose delivery tick t + W - 1 just became addressable into the (empty)
 // slot of that tick.
 __global__ void k_hist(Engine e) {
+    tick_enter();
     const uint32_t t = e.ts->tick;
     if (blockIdx.x == 0) {
         const uint32_t ft = e.ts->far_ticks;
@@ -694,6 +717,7 @@ __global__ void k_hist(Engine e) {
 // Phase 1 of the per-target scan: tile sums of counts and of touched targets;
 // the last block turns them into exclusive tile bases.
 __global__ void k_scan_tile(Engine e) {
+    tick_enter();
     constexpr int kItems = kScanTile / kThreads;
     const uint32_t tiles = (e.N + kScanTile - 1) / kScanTile;
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
@@ -722,6 +746,7 @@ __global__ void k_scan_tile(Engine e) {
 
 // Phase 2: per-target segment starts and the ascending touched list.
 __global__ void k_scan_out(Engine e) {
+    tick_enter();
     constexpr int kItems = kScanTile / kThreads;
     const uint32_t tiles = (e.N + kScanTile - 1) / kScanTile;
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
@@ -755,6 +780,7 @@ __global__ void k_scan_out(Engine e) {
 // Group due events by target: each event takes a position inside its
 // target's segment (counts return to zero for the next tick).
 __global__ void k_scatter(Engine e) {
+    tick_enter();
     const uint32_t t = e.ts->tick;
     const uint32_t slot = t & e.wmask;
     const uint32_t n = e.ts->n_due;
@@ -1012,6 +1038,7 @@ __device__ __forceinline__ void events_of_target(const Engine& e, uint32_t n, ui
 // 32 at a time, one per lane, whatever targets they belong to; repeats and
 // long groups are processed in place.
 __global__ void __launch_bounds__(kThreads, SNNGB_EVENTS_MIN_BLOCKS) k_events(Engine e) {
+    tick_enter();
     __shared__ uint32_t s_due[kThreads], s_rank[kThreads];
     __shared__ EvItem s_queue[kThreads / 32][64];
     const uint32_t t = e.ts->tick;
@@ -1142,6 +1169,7 @@ __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, uint
 // are one contiguous range: one thread copies it into shared memory with a
 // bulk copy while every thread loads its neuron's records.
 __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(Engine e) {
+    tick_enter();
     extern __shared__ __align__(128) EvIn s_ev[];  // kStageEvents entries
     __shared__ __align__(8) unsigned long long s_bar;
     __shared__ uint32_t s_lo, s_cnt;
@@ -1297,6 +1325,7 @@ __global__ void k_post(Engine e) {
 // Popcounts of the fire bitmap tiles; the last block turns them into
 // exclusive tile bases and the tick's fire count.
 __global__ void k_fire_tiles(Engine e) {
+    tick_enter();
     const uint32_t words = (e.ts->n_due + 31) / 32;
     const uint32_t tiles = (words + kThreads - 1) / kThreads;
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
@@ -1317,6 +1346,7 @@ __global__ void k_fire_tiles(Engine e) {
 // 80-93); the fire list and the raster are written here and the bitmap is
 // cleared.
 __global__ void k_fire_list(Engine e) {
+    tick_enter();
     const uint32_t t = e.ts->tick;
     const uint32_t words = (e.ts->n_due + 31) / 32;
     const uint32_t tiles = (words + kThreads - 1) / kThreads;
@@ -1348,6 +1378,7 @@ __global__ void k_fire_list(Engine e) {
 // (exclusive scan over blocks per class, appended behind each delivery slot's
 // current contents) and finishes the tick.
 __global__ void __launch_bounds__(kFireCountThreads) k_fire_count(Engine e) {
+    tick_enter();
     const uint32_t t = e.ts->tick;
     const uint32_t nfires = e.ts->n_fires;
     const uint32_t nf = nfires < e.fire_cap ? nfires : e.fire_cap;
@@ -1418,6 +1449,7 @@ __global__ void __launch_bounds__(kFireCountThreads) k_fire_count(Engine e) {
 // block, behind the block's earlier fires.  So the wheel ends up in exactly
 // the reference's scheduling order.
 __global__ void __launch_bounds__(kThreads) k_expand(Engine e) {
+    tick_enter();
     __shared__ uint32_t s_rows[kExpandFires][kMaxClasses + 1];
     const uint32_t nf = e.ts->expand_fires;
     const uint32_t D = e.D;
@@ -1507,11 +1539,33 @@ void launch_range_counts(const Engine& e, uint32_t n_begin, uint32_t n_end, unsi
     k_range_counts<<<e.grid_wide, kThreads, 0, stream>>>(e, n_begin, n_end, tm_begin, tm_end, out);
 }
 
+// Launch of a main-stream tick kernel.  `dependent` makes it a programmatic
+// dependent of the kernel before it on the stream (see tick_enter): its
+// blocks are scheduled while that kernel drains instead of after it.
+static void launch_main(void (*kernel)(Engine), uint32_t grid, uint32_t block, size_t smem, cudaStream_t stream,
+                        bool dependent, const Engine& e) {
+    cudaLaunchAttribute attr{};
+    attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr.val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cfg.attrs = &attr;
+    cfg.numAttrs = dependent ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kernel, e);
+}
+
 void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     const uint32_t tiles = (e.N + kScanTile - 1) / kScanTile;
     const uint32_t wide = e.grid_wide;
     const uint32_t scan_grid = tiles == 0 ? 1 : (tiles < wide ? tiles : wide);
     cudaStream_t stream = s.main;
+    // Kernels that follow another kernel directly on the main stream are
+    // programmatic dependents; the per-kernel profile (event marks between
+    // the kernels) launches them plainly so each kernel is timed alone.
+    const bool dep = marks == nullptr;
     int k = 0;
     auto mark = [&](bool after) {
         if (marks) cudaEventRecordWithFlags(marks[2 * k + (after ? 1 : 0)], stream, cudaEventRecordExternal);
@@ -1520,10 +1574,11 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     auto side_mark = [&](int index, bool after) {
         if (marks) cudaEventRecordWithFlags(marks[2 * index + (after ? 1 : 0)], s.side, cudaEventRecordExternal);
     };
-    mark(false); k_hist<<<wide * 4, kThreads, 0, stream>>>(e); mark(true);
-    mark(false); k_scan_tile<<<scan_grid, kThreads, 0, stream>>>(e); mark(true);
-    mark(false); k_scan_out<<<scan_grid, kThreads, 0, stream>>>(e); mark(true);
-    mark(false); k_scatter<<<wide, kThreads, 0, stream>>>(e); mark(true);
+    // k_hist follows a wait on the side stream: a full dependency
+    mark(false); launch_main(k_hist, wide * 4, kThreads, 0, stream, false, e); mark(true);
+    mark(false); launch_main(k_scan_tile, scan_grid, kThreads, 0, stream, dep, e); mark(true);
+    mark(false); launch_main(k_scan_out, scan_grid, kThreads, 0, stream, dep, e); mark(true);
+    mark(false); launch_main(k_scatter, wide, kThreads, 0, stream, dep, e); mark(true);
     // the temporal update forks off here and runs beside k_events / k_process
     // (it needs only the touched list and the group sizes; started before
     // k_scatter it slowed that kernel's atomics more than it gained)
@@ -1533,8 +1588,8 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     k_temporal<<<e.grid_process, kThreads, 0, s.side>>>(e);
     side_mark(10, true);
     cudaEventRecord(s.ev[1], s.side);
-    mark(false); k_events<<<e.grid_wide * 4, kThreads, 0, stream>>>(e); mark(true);
-    mark(false); k_process<<<e.grid_process, kThreads, kStageEvents * sizeof(EvIn), stream>>>(e); mark(true);
+    mark(false); launch_main(k_events, e.grid_wide * 4, kThreads, 0, stream, dep, e); mark(true);
+    mark(false); launch_main(k_process, e.grid_process, kThreads, kStageEvents * sizeof(EvIn), stream, dep, e); mark(true);
     // post-spike STDP of the fired targets runs beside the fire ordering and
     // the expansion (synapse records are not touched by those)
     cudaEventRecord(s.ev[2], stream);
@@ -1543,11 +1598,11 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     k_post<<<wide * 4, kThreads, 0, s.side>>>(e);
     side_mark(11, true);
     cudaEventRecord(s.ev[3], s.side);
-    mark(false); k_fire_tiles<<<wide, kThreads, 0, stream>>>(e); mark(true);
-    mark(false); k_fire_list<<<e.grid_fire, kThreads, 0, stream>>>(e); mark(true);
+    mark(false); launch_main(k_fire_tiles, wide, kThreads, 0, stream, dep, e); mark(true);
+    mark(false); launch_main(k_fire_list, e.grid_fire, kThreads, 0, stream, dep, e); mark(true);
     cudaStreamWaitEvent(stream, s.ev[1], 0);  // k_temporal reads the tick counter k_fire_count advances
-    mark(false); k_fire_count<<<e.grid_wide / 4 + 1, kFireCountThreads, 0, stream>>>(e); mark(true);
-    mark(false); k_expand<<<e.grid_wide * 4, kThreads, 0, stream>>>(e); mark(true);
+    mark(false); launch_main(k_fire_count, e.grid_wide / 4 + 1, kFireCountThreads, 0, stream, false, e); mark(true);
+    mark(false); launch_main(k_expand, e.grid_wide * 4, kThreads, 0, stream, dep, e); mark(true);
     cudaStreamWaitEvent(stream, s.ev[3], 0);  // the next tick's k_events reads the synapse records
 }
 

@@ -1145,6 +1145,8 @@ int snncuda_group_events(const uint64_t* events, uint32_t count, uint32_t neuron
                          uint32_t* segment_start, void* cuda_stream) {
     if ((count > 0 && (events == nullptr || grouped == nullptr)) || segment_start == nullptr)
         return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null array");
+    if (count > 0 && events < grouped + count && grouped < events + count)
+        return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "events and grouped overlap");
     if (count >= (1u << 31) || neuron_count >= (1u << 31))
         return set_error(SNNCUDA_ERR_UNSUPPORTED, "at most 2^31-1 events and neurons");
     cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
@@ -1210,6 +1212,8 @@ int snncuda_group_events_static(const uint64_t* events, uint32_t count, uint32_t
                                 uint64_t* grouped, uint32_t* segment_start, void* cuda_stream) {
     if ((count > 0 && (events == nullptr || grouped == nullptr)) || segment_start == nullptr)
         return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null array");
+    if (count > 0 && events < grouped + count && grouped < events + count)
+        return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "events and grouped overlap");
     if (count > kStaticEvents || neuron_count > kStaticNeurons)
         return set_error(SNNCUDA_ERR_CAPACITY,
                          "snncuda_group_events_static handles at most 2^20 events and 2^18 neurons; "

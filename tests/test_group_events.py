@@ -50,6 +50,17 @@ def test_oracle_rejects_bad_target(port_lib):
     assert run_host(port_lib, ev, 5)[0] == 1
 
 
+def test_oracle_rejects_overlapping_output(port_lib):
+    """No in-place grouping: events and grouped must not overlap (the same
+    contract on the GPU)."""
+    ev = np.arange(8, dtype=np.uint64) % np.uint64(3)
+    start = np.zeros(4, np.uint32)
+    for shift in (0, 8, 56):
+        rc = port_lib.snncuda_group_events(ev.ctypes.data, ev.size, 3, ev.ctypes.data + shift, start.ctypes.data,
+                                           None)
+        assert rc == 1, shift
+
+
 def run_device(lib, events, neurons, fn="snncuda_group_events"):
     import torch
     d_ev = torch.from_numpy(events.view(np.int64)).cuda()
@@ -78,3 +89,15 @@ def test_gpu_grouping(gpu_lib, count, neurons):
 def test_gpu_grouping_rejects_bad_target(gpu_lib):
     ev = np.array([3, 9], np.uint64)
     assert run_device(gpu_lib, ev, 5)[0] == 1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fn", ["snncuda_group_events", "snncuda_group_events_static"])
+def test_gpu_grouping_rejects_overlapping_output(gpu_lib, fn):
+    import torch
+    d_ev = torch.zeros(16, dtype=torch.int64, device="cuda")
+    d_s = torch.zeros(4, dtype=torch.int32, device="cuda")
+    for shift in (0, 8, 120):
+        rc = getattr(gpu_lib, fn)(d_ev.data_ptr(), 16, 3, d_ev.data_ptr() + shift, d_s.data_ptr(),
+                                  torch.cuda.current_stream().cuda_stream)
+        assert rc == 1, shift
