@@ -54,7 +54,9 @@ namespace snngb {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr uint32_t kStageEvents = 4096;  // event inputs k_process stages per block (64 KB)
+constexpr uint32_t kStageEvents = 3584;  // event inputs k_process stages per block (56 KB)
+constexpr uint32_t kLtpShared = 2560;    // longest LTP table k_process copies to shared memory (10 KB)
+constexpr size_t kProcessSmem = kStageEvents * sizeof(EvIn) + kLtpShared * sizeof(float);
 constexpr int kFireCountThreads = 1024;  // k_fire_count's last block scans up to 32 delay classes at once
 
 // Minimum resident blocks per SM requested for k_process and k_events
@@ -424,9 +426,12 @@ __device__ void temporal_tick(NState& s, const NeuronParam& p, uint32_t t, const
     }
 }
 
-// SynapseDendriteProcessor.cpp:175-229.  Returns whether the neuron fired.
-__device__ bool process_input(NState& s, float threshold, uint32_t comp, uint32_t rec, float w, uint32_t t,
-                              const Engine& e) {
+// The decay step of SynapseDendriteProcessor.cpp:175-229: every compartment
+// is brought forward to tick t.  All events of a target in one tick share t,
+// so after the first event every compartment is already at t and the step
+// does nothing; it is therefore applied once per target and tick, before the
+// first event (a fire's reset also leaves every compartment at t).
+__device__ __forceinline__ void decay_to(NState& s, uint32_t t, const Engine& e) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         if (t <= s.upd[k] || s.cur[k] == 0.0f) {
@@ -437,12 +442,18 @@ __device__ bool process_input(NState& s, float threshold, uint32_t comp, uint32_
             s.upd[k] = t;
         }
     }
+}
+
+// The rest of SynapseDendriteProcessor.cpp:175-229 for one event at tick t,
+// every compartment already at t (decay_to).  Returns whether the neuron
+// fired.
+__device__ __forceinline__ bool process_input(NState& s, float threshold, uint32_t comp, uint32_t rec, float w,
+                                              uint32_t t) {
     const float applied = __fmul_rn(__fmul_rn(w, rec_gain(rec)), rec_sign(rec));
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         if (static_cast<uint32_t>(k) == comp) {
-            s.cur[k] = __fadd_rn(s.cur[k], applied);
-            s.upd[k] = t;
+            s.cur[k] = __fadd_rn(s.cur[k], applied);  // its update tick is already t
             s.flags = (s.flags & ~(3u << (2 * k))) | (rec << (2 * k));
         }
     }
@@ -465,14 +476,15 @@ __device__ bool process_input(NState& s, float threshold, uint32_t comp, uint32_
 }
 
 // StdpRule::weight_delta + apply (STDP.cpp:20-40) and the update bookkeeping
-// of SynapseDendriteProcessor.cpp:108-122 / :158-172.
-__device__ void stdp_apply(SynA& a, uint32_t pre, uint32_t post, const Engine& e, int stdp) {
+// of SynapseDendriteProcessor.cpp:108-122 / :158-172.  `ltp` is the LTP delta
+// table (e.tab.ltp, or k_process's copy of it in shared memory).
+__device__ void stdp_apply(SynA& a, uint32_t pre, uint32_t post, const Engine& e, int stdp, const float* ltp) {
     const float before = a.weight;
     float delta = 0.0f;
     if (stdp && !((a.meta >> kMetaRuleOffBit) & 1u)) {
         if (post > pre) {
             const uint32_t dt = post - pre;
-            delta = e.tab.ltp[dt < e.tab.stdp_len ? dt : e.tab.stdp_len - 1];
+            delta = ltp[dt < e.tab.stdp_len ? dt : e.tab.stdp_len - 1];
         } else if (post < pre) {
             const uint32_t dt = pre - post;
             delta = e.tab.ltd[dt < e.tab.stdp_len ? dt : e.tab.stdp_len - 1];
@@ -487,13 +499,14 @@ __device__ void stdp_apply(SynA& a, uint32_t pre, uint32_t post, const Engine& e
 
 // apply_post_spike_plasticity for every target fire at tick t not yet
 // applied to this synapse (fires = target fires so far this tick).
-__device__ __forceinline__ bool post_catch_up(SynA& a, uint32_t t, uint32_t fires, const Engine& e, int stdp) {
+__device__ __forceinline__ bool post_catch_up(SynA& a, uint32_t t, uint32_t fires, const Engine& e, int stdp,
+                                              const float* ltp) {
     const uint32_t applied = a.last_post1 == t + 1 ? a.post_cnt : 0u;
     if (fires <= applied) return false;
     const bool plastic = (a.meta >> kMetaPlasticBit) & 1u;
     for (uint32_t k = applied; k < fires; ++k) {
         a.last_post1 = t + 1;
-        if (plastic && a.last_pre1 != 0) stdp_apply(a, a.last_pre1 - 1, t, e, stdp);
+        if (plastic && a.last_pre1 != 0) stdp_apply(a, a.last_pre1 - 1, t, e, stdp, ltp);
     }
     a.post_cnt = fires;
     return true;
@@ -850,13 +863,14 @@ __global__ void __launch_bounds__(kThreads) k_segsort(Engine e) {
 // against the last post spike, last_pre, the pre-spike count, and the
 // spike-code pattern (:318-365).  None of it depends on the target's neuron
 // state; only the STDP part depends on whether the target fired earlier in the
-// tick, which k_process handles by redoing it (replay_pre_stdp).
+// tick, which k_process handles by redoing it (walk_fired_targets).
 __device__ __forceinline__ void pre_event(SynAB& r, const NeuronParam& p, uint32_t t, uint16_t* lc,
                                           const Engine& e, int stdp, int temporal, bool inl) {
     SynA& a = r.a;
     const uint32_t delay = a.meta & kMetaDelayMask;
     const uint32_t pre_tick = t >= delay ? t - delay : t;
-    if (((a.meta >> kMetaPlasticBit) & 1u) && a.last_post1 != 0) stdp_apply(a, pre_tick, a.last_post1 - 1, e, stdp);
+    if (((a.meta >> kMetaPlasticBit) & 1u) && a.last_post1 != 0)
+        stdp_apply(a, pre_tick, a.last_post1 - 1, e, stdp, e.tab.ltp);
     a.last_pre1 = pre_tick + 1;
     r.b.pre_count += 1;
     code_update(r.b, p, t, lc, e.code_stride, temporal, inl);
@@ -1067,48 +1081,72 @@ __global__ void __launch_bounds__(kThreads, SNNGB_EVENTS_MIN_BLOCKS) k_events(En
     if (lane < qn) synapse_item(e, queue[lane], t, stdp, temporal);
 }
 
-// The synapse's state before event i of the walk, after the target's fires so
-// far: k_events' snapshot, unless an earlier event of the same synapse came
-// after the first fire (the walk has rewritten the record then).  Applies the
-// owed post-spike STDP and the event's pre-spike STDP, stores the record and
-// returns the weight.  Only events that follow a fire of their target get here.
-__device__ __noinline__ float replay_pre_stdp(const Engine& e, uint32_t beg, uint32_t i, uint32_t first_fire,
-                                              const EvIn& x, uint32_t t, uint32_t fires, int stdp) {
-    bool rewritten = false;
-    if (x.bits & kEvRepeat) {
-        for (uint32_t q = first_fire + 1; q < i && !rewritten; ++q) {
-            const EvIn y = e.evin[beg + q];
-            rewritten = !(y.bits & kEvExternal) && y.tm == x.tm;
-        }
-    }
-    SynA a = rewritten ? e.syn[x.tm].a : e.ev_a0[beg + i];
-    post_catch_up(a, t, fires, e, stdp);
-    const uint32_t delay = a.meta & kMetaDelayMask;
-    const uint32_t pre_tick = t >= delay ? t - delay : t;
-    if (((a.meta >> kMetaPlasticBit) & 1u) && a.last_post1 != 0) stdp_apply(a, pre_tick, a.last_post1 - 1, e, stdp);
-    a.last_pre1 = pre_tick + 1;
-    e.syn[x.tm].a = a;
-    return a.weight;
-}
-
-// The reference's sequential per-event loop (NetworkPropagator.cpp:80-131)
-// restricted to one target: its events' inputs in due order (from k_events),
-// the neuron's physics, and the temporal pattern once for the tick.
 // The block's event inputs: entries [lo, lo + cnt) of evin staged in shared
 // memory once `ready()` returns true; the rest read from global memory.
 struct Staged {
     const EvIn* s;
     uint32_t lo, cnt;
+    __device__ __forceinline__ EvIn at(const Engine& e, uint32_t g) const {
+        const uint32_t o = g - lo;
+        return o < cnt ? s[o] : e.evin[g];
+    }
 };
 
-template <typename Ready>
-__device__ __forceinline__ void process_target(const Engine& e, uint32_t n, uint32_t beg, uint32_t len, uint32_t t,
-                                               int stdp, Staged st, Ready ready) {
-    // the physics fields only: the temporal ones belong to k_temporal, which
-    // may be running at the same time
+// Applies to a synapse record the post-spike STDP owed for the target's fires
+// so far and the event's pre-spike STDP (the record is the synapse's state
+// before the event) and returns the weight the event delivers.  Both STDP
+// steps have post >= pre, so they read only the LTP table.
+__device__ __forceinline__ float redo_pre_stdp(const Engine& e, SynA& a, uint32_t t, uint32_t fires, int stdp,
+                                               const float* ltp) {
+    post_catch_up(a, t, fires, e, stdp, ltp);
+    const uint32_t delay = a.meta & kMetaDelayMask;
+    const uint32_t pre_tick = t >= delay ? t - delay : t;
+    if (((a.meta >> kMetaPlasticBit) & 1u) && a.last_post1 != 0)
+        stdp_apply(a, pre_tick, a.last_post1 - 1, e, stdp, ltp);
+    a.last_pre1 = pre_tick + 1;
+    return a.weight;
+}
+
+__device__ __forceinline__ SynA shfl_syn(const SynA& a, uint32_t src) {
+    SynA r;
+    r.weight = __shfl_sync(0xffffffffu, a.weight, src);
+    r.last_pre1 = __shfl_sync(0xffffffffu, a.last_pre1, src);
+    r.last_post1 = __shfl_sync(0xffffffffu, a.last_post1, src);
+    r.meta = __shfl_sync(0xffffffffu, a.meta, src);
+    r.clamp_hi = __shfl_sync(0xffffffffu, a.clamp_hi, src);
+    r.updates = __shfl_sync(0xffffffffu, a.updates, src);
+    r.last_delta = __shfl_sync(0xffffffffu, a.last_delta, src);
+    r.post_cnt = __shfl_sync(0xffffffffu, a.post_cnt, src);
+    return r;
+}
+
+// One target's walk (the reference's sequential per-event loop,
+// NetworkPropagator.cpp:80-131, restricted to that target): its neuron state
+// and how far the walk has got.
+struct Walk {
     NState s;
-    NeuronRec* rec = e.nrec + n;
-    const float threshold = e.nparam[n].threshold;
+    float threshold;
+    uint32_t n, beg, len;
+    uint32_t i;           // next event
+    uint32_t fires;       // target fires so far this tick
+    uint32_t first_fire;  // event of the first fire
+};
+
+__device__ __forceinline__ void record_fire(const Engine& e, const Walk& w, uint32_t due) {
+    atomicOr(&e.fire_bits[due >> 5], 1u << (due & 31));
+    e.fire_at[due] = w.n;
+}
+
+// Phase 1 of a target's walk: load the neuron (the physics fields only: the
+// temporal ones belong to k_temporal, which may be running at the same time)
+// and process its events in due order up to and including its first fire.
+// Every event before the first fire uses the weight k_events computed.
+// Returns whether the target fired.
+template <typename Ready>
+__device__ __forceinline__ bool walk_to_first_fire(const Engine& e, Walk& w, uint32_t t, Staged& st, Ready ready) {
+    NState& s = w.s;
+    const NeuronRec* rec = e.nrec + w.n;
+    w.threshold = e.nparam[w.n].threshold;
     {
         const float4 c = reinterpret_cast<const float4*>(rec->cur)[0];
         const uint4 u = reinterpret_cast<const uint4*>(rec->upd)[0];
@@ -1127,36 +1165,127 @@ __device__ __forceinline__ void process_target(const Engine& e, uint32_t n, uint
         s.last_active = m.w;
         s.flags = rec->flags;
     }
-
-    uint32_t fires = 0, first_fire = 0;
+    w.fires = 0;
+    w.first_fire = 0;
+    if (w.len > 0) decay_to(s, t, e);
     if (!ready()) st.cnt = 0;
-    for (uint32_t i = 0; i < len; ++i) {
-        const uint32_t o = beg + i - st.lo;
-        EvIn x;
-        if (o < st.cnt) {
-            x = st.s[o];
-        } else {
-            x = e.evin[beg + i];
-        }
-        float w = x.weight;
-        if (fires > 0 && !(x.bits & kEvExternal)) w = replay_pre_stdp(e, beg, i, first_fire, x, t, fires, stdp);
-        if (process_input(s, threshold, x.bits & 3u, (x.bits >> 2) & 3u, w, t, e)) {
-            if (fires == 0) first_fire = i;
-            fires += 1;
-            atomicOr(&e.fire_bits[x.due >> 5], 1u << (x.due & 31));
-            e.fire_at[x.due] = n;
+    for (uint32_t i = 0; i < w.len; ++i) {
+        const EvIn x = st.at(e, w.beg + i);
+        if (process_input(s, w.threshold, x.bits & 3u, (x.bits >> 2) & 3u, x.weight, t)) {
+            record_fire(e, w, x.due);
+            w.fires = 1;
+            w.first_fire = i;
+            w.i = i + 1;
+            return true;
         }
     }
+    w.i = w.len;
+    return false;
+}
 
+// Phase 2, one warp: the rest of the walks of its lanes' fired targets, one
+// target at a time.  Every synaptic event after a fire redoes its STDP with
+// the target's fire count so far, starting from the synapse's state before
+// the event: k_events' snapshot, or, when the same synapse already had an
+// event after the first fire, the record that event left.  The warp redoes up
+// to 32 events at once (an event whose predecessor is in the same chunk waits
+// a round and takes its record by shuffle); the target's own lane then runs
+// the neuron physics over them in order.  If the target fires again inside the
+// chunk, the events after that fire are redone with the new count; only the
+// records of events before it are stored (the last event of each synapse
+// stores).  The result is the sequential order's.
+__device__ __forceinline__ void walk_fired_targets(const Engine& e, Walk& w, bool fired, uint32_t t, int stdp,
+                                                   Staged st, const float* ltp, float* s_wt) {
+    const uint32_t lane = threadIdx.x & 31;
+    unsigned pend = __ballot_sync(0xffffffffu, fired);
+    while (pend) {
+        const uint32_t L = __ffs(pend) - 1;
+        pend &= pend - 1;
+        const uint32_t beg = __shfl_sync(0xffffffffu, w.beg, L);
+        const uint32_t len = __shfl_sync(0xffffffffu, w.len, L);
+        const uint32_t after = __shfl_sync(0xffffffffu, w.first_fire, L) + 1;  // first event after the first fire
+        uint32_t pos = __shfl_sync(0xffffffffu, w.i, L);
+        uint32_t fires = __shfl_sync(0xffffffffu, w.fires, L);
+        while (pos < len) {
+            const uint32_t m = len - pos < 32 ? len - pos : 32;
+            const uint32_t j = pos + lane;
+            EvIn x{};
+            if (lane < m) x = st.at(e, beg + j);
+            const bool syn = lane < m && !(x.bits & kEvExternal);
+            // the synapse's latest earlier event after the first fire
+            uint32_t pred = 0xFFFFFFFFu;
+            if (syn && (x.bits & kEvRepeat)) {
+                for (uint32_t q = j; q-- > after;) {
+                    const EvIn y = st.at(e, beg + q);
+                    if (!(y.bits & kEvExternal) && y.tm == x.tm) {
+                        pred = q;
+                        break;
+                    }
+                }
+            }
+            const bool wait = pred != 0xFFFFFFFFu && pred >= pos;  // predecessor in this chunk
+            SynA a{};
+            float wt = x.weight;
+            bool done = !syn;
+            if (syn && !wait) {
+                a = pred != 0xFFFFFFFFu ? e.syn[x.tm].a : e.ev_a0[beg + j];
+                wt = redo_pre_stdp(e, a, t, fires, stdp, ltp);
+                done = true;
+            }
+            while (!__all_sync(0xffffffffu, done)) {
+                const uint32_t src = wait ? pred - pos : lane;
+                const SynA pa = shfl_syn(a, src);
+                const bool pdone = __shfl_sync(0xffffffffu, done, src);
+                if (!done && pdone) {
+                    a = pa;
+                    wt = redo_pre_stdp(e, a, t, fires, stdp, ltp);
+                    done = true;
+                }
+            }
+            if (lane < m) s_wt[lane] = wt;
+            __syncwarp();
+            uint32_t next = pos + m;
+            if (lane == L) {
+                for (uint32_t c = 0; c < m; ++c) {
+                    const EvIn y = st.at(e, beg + pos + c);
+                    if (process_input(w.s, w.threshold, y.bits & 3u, (y.bits >> 2) & 3u, s_wt[c], t)) {
+                        record_fire(e, w, y.due);
+                        w.fires += 1;
+                        if (c + 1 < m) {
+                            next = pos + c + 1;
+                            break;
+                        }
+                    }
+                }
+                w.i = next;
+            }
+            next = __shfl_sync(0xffffffffu, next, L);
+            // store the records of the events before `next`, the last one of
+            // each synapse
+            const bool store = syn && j < next;
+            const unsigned long long key = store ? x.tm : (1ull << 32) | lane;
+            const unsigned same = __match_any_sync(0xffffffffu, key);
+            if (store && lane == 31u - __clz(same)) e.syn[x.tm].a = a;
+            pos = next;
+            fires = __shfl_sync(0xffffffffu, w.fires, L);
+            __syncwarp();
+        }
+    }
+}
+
+// Stores a finished walk's neuron state and lists the target if it fired.
+__device__ __forceinline__ void finish_walk(const Engine& e, const Walk& w) {
+    const NState& s = w.s;
+    NeuronRec* rec = e.nrec + w.n;
     reinterpret_cast<float4*>(rec->cur)[0] = make_float4(s.cur[0], s.cur[1], s.cur[2], s.cur[3]);
     reinterpret_cast<uint4*>(rec->upd)[0] = make_uint4(s.upd[0], s.upd[1], s.upd[2], s.upd[3]);
     *reinterpret_cast<uint4*>(&rec->membrane) =
         make_uint4(__float_as_uint(s.membrane), s.spikes, s.last_fired1, s.last_active);
     rec->flags = s.flags;
-    if (fires > 0) {
+    if (w.fires > 0) {
         const uint32_t j = atomicAdd(&e.ts->n_fired_targets, 1u);
-        e.fired_tgt[j] = n;
-        e.fired_cnt[j] = fires;
+        e.fired_tgt[j] = w.n;
+        e.fired_cnt[j] = w.fires;
     }
 }
 
@@ -1173,12 +1302,18 @@ __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(
     extern __shared__ __align__(128) EvIn s_ev[];  // kStageEvents entries
     __shared__ __align__(8) unsigned long long s_bar;
     __shared__ uint32_t s_lo, s_cnt;
+    __shared__ float s_wt[kThreads / 32][32];  // per warp: weights of the events redone after a fire
     const uint32_t t = e.ts->tick;
     const uint32_t n_touched = e.ts->n_touched;
     const uint32_t n_due = e.ts->n_due;
     const int stdp = e.ts->stdp_enabled;
     if (threadIdx.x == 0) mbar_init(&s_bar, 1);
     __syncthreads();
+    // the LTP table goes to shared memory (when it fits) during the first
+    // round's copy: the STDP redone after a fire then makes no dependent
+    // global load besides the snapshot
+    const bool ltp_shared = stdp && e.tab.stdp_len <= kLtpShared;
+    const float* ltp = ltp_shared ? reinterpret_cast<const float*>(s_ev + kStageEvents) : e.tab.ltp;
     uint32_t parity = 0;
     bool staging = true;  // false after a copy outlived its wait: shared memory is no longer used
     for (uint32_t k0 = blockIdx.x * blockDim.x; k0 < n_touched; k0 += gridDim.x * blockDim.x) {
@@ -1190,6 +1325,10 @@ __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(
             s_lo = lo;
             s_cnt = cnt;
             if (cnt > 0) bulk_load(s_ev, e.evin + lo, cnt * static_cast<uint32_t>(sizeof(EvIn)), &s_bar);
+        }
+        if (ltp_shared && k0 == blockIdx.x * blockDim.x) {
+            float* s_ltp = reinterpret_cast<float*>(s_ev + kStageEvents);
+            for (uint32_t i = threadIdx.x; i < e.tab.stdp_len; i += blockDim.x) s_ltp[i] = e.tab.ltp[i];
         }
         __syncthreads();
         const Staged st{s_ev, s_lo, s_cnt};
@@ -1203,13 +1342,19 @@ __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(
             return ok;
         };
         const uint32_t k = k0 + threadIdx.x;
+        Walk w;
+        w.n = w.beg = w.len = w.i = w.fires = w.first_fire = 0;
+        bool fired = false;
+        Staged mine = st;
         if (k < n_touched) {
-            const uint32_t n = e.touched[k];
-            const uint32_t beg = e.tbeg[k];
-            const uint32_t end = k + 1 < n_touched ? e.tbeg[k + 1] : n_due;
-            process_target(e, n, beg, end - beg, t, stdp, st, ready);
+            w.n = e.touched[k];
+            w.beg = e.tbeg[k];
+            w.len = (k + 1 < n_touched ? e.tbeg[k + 1] : n_due) - w.beg;
+            fired = walk_to_first_fire(e, w, t, mine, ready);
         }
-        ready();
+        if (!ready()) mine.cnt = 0;
+        walk_fired_targets(e, w, fired, t, stdp, mine, ltp, s_wt[threadIdx.x >> 5]);
+        if (k < n_touched) finish_walk(e, w);
         const bool failed = __syncthreads_or(!ok);
         if (st.cnt > 0) {
             if (failed) {
@@ -1317,7 +1462,7 @@ __global__ void k_post(Engine e) {
         const unsigned long long b = e.in_ptr[n], en = e.in_ptr[n + 1];
         for (unsigned long long tm = b + threadIdx.x; tm < en; tm += blockDim.x) {
             SynA a = e.syn[tm].a;
-            if (post_catch_up(a, t, fires, e, stdp)) e.syn[tm].a = a;
+            if (post_catch_up(a, t, fires, e, stdp, e.tab.ltp)) e.syn[tm].a = a;
         }
     }
 }
@@ -1589,7 +1734,7 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     side_mark(10, true);
     cudaEventRecord(s.ev[1], s.side);
     mark(false); launch_main(k_events, e.grid_wide * 4, kThreads, 0, stream, dep, e); mark(true);
-    mark(false); launch_main(k_process, e.grid_process, kThreads, kStageEvents * sizeof(EvIn), stream, dep, e); mark(true);
+    mark(false); launch_main(k_process, e.grid_process, kThreads, kProcessSmem, stream, dep, e); mark(true);
     // post-spike STDP of the fired targets runs beside the fire ordering and
     // the expansion (synapse records are not touched by those)
     cudaEventRecord(s.ev[2], stream);
@@ -1625,7 +1770,7 @@ void launch_group(const Engine& e, cudaStream_t stream) {
 
 void configure_kernels() {
     cudaFuncSetAttribute(k_process, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         static_cast<int>(kStageEvents * sizeof(EvIn)));
+                         static_cast<int>(kProcessSmem));
 }
 
 void launch_init_syn(const Engine& e, const SynA* a, cudaStream_t stream) {
