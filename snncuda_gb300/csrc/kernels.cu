@@ -1596,26 +1596,42 @@ __global__ void __launch_bounds__(kFireCountThreads) k_fire_count(Engine e) {
 __global__ void __launch_bounds__(kThreads) k_expand(Engine e) {
     tick_enter();
     __shared__ uint32_t s_rows[kExpandFires][kMaxClasses + 1];
+    __shared__ unsigned long long s_dst[kMaxClasses];
+    __shared__ unsigned long long s_base;
     const uint32_t nf = e.ts->expand_fires;
     const uint32_t D = e.D;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (uint32_t r = blockIdx.x; r < nf; r += gridDim.x) {
         const uint32_t first = r - r % kExpandFires;
         const uint32_t m = r - first + 1;  // fires first .. r of the expansion block
+        // everything the copies depend on, fetched together: the class rows of
+        // the block's fires, the block's destinations, the fire's event list
         for (uint32_t i = threadIdx.x; i < m * (D + 1); i += blockDim.x) {
             const uint32_t q = i / (D + 1), d = i - q * (D + 1);
             s_rows[q][d] = e.pre_off[static_cast<size_t>(e.fire_list[first + q]) * (D + 1) + d];
         }
+        for (uint32_t d = threadIdx.x; d < D; d += blockDim.x)
+            s_dst[d] = e.xdst_ok[d] ? __ldcg(e.xdst + static_cast<size_t>(r / kExpandFires) * D + d) : ~0ull;
+        if (threadIdx.x == 0) s_base = e.pre_base[e.fire_list[r]];
         __syncthreads();
-        const unsigned long long* src = e.pre_ev + e.pre_base[e.fire_list[r]];
+        const unsigned long long* src = e.pre_ev + s_base;
         const uint32_t* row = s_rows[m - 1];
         for (uint32_t d = warp; d < D; d += kThreads / 32) {
             const uint32_t beg = row[d], len = row[d + 1] - beg;
-            if (len == 0 || !e.xdst_ok[d]) continue;
+            if (len == 0 || s_dst[d] == ~0ull) continue;
             uint32_t before = 0;  // this class's events of the block's earlier fires
             for (uint32_t q = 0; q + 1 < m; ++q) before += s_rows[q][d + 1] - s_rows[q][d];
-            unsigned long long* dst = e.wheel + __ldcg(e.xdst + static_cast<size_t>(r / kExpandFires) * D + d) + before;
-            for (uint32_t i = lane; i < len; i += 32) dst[i] = src[beg + i];
+            unsigned long long* dst = e.wheel + s_dst[d] + before;
+            const unsigned long long* sp = src + beg;
+            uint32_t i = lane;
+            for (; i + 96 < len; i += 128) {  // four loads in flight per lane
+                const unsigned long long a0 = sp[i], a1 = sp[i + 32], a2 = sp[i + 64], a3 = sp[i + 96];
+                dst[i] = a0;
+                dst[i + 32] = a1;
+                dst[i + 64] = a2;
+                dst[i + 96] = a3;
+            }
+            for (; i < len; i += 32) dst[i] = sp[i];
         }
         __syncthreads();
     }
