@@ -49,7 +49,7 @@ if "--serve" in sys.argv:
 METRIC = "synaptic_events_per_s"
 UNIT = "events/s"
 ORACLE = ROOT / "oracle" / "_build" / "liboracle_port.so"
-KERNELS_PER_TICK = 12   # launch_tick in snncuda_gb300/csrc/kernels.cu
+KERNELS_PER_TICK = 11   # launch_tick in snncuda_gb300/csrc/kernels.cu
 # DRAM bytes (read + write) per launch of a kernel on the default stdp_100k
 # workload, from one ncu capture of this code (profiles/); reported as
 # roofline.traffic for the dominant kernel.

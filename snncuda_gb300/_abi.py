@@ -135,7 +135,7 @@ class SynapseState(Structure):
     ]
 
 
-KERNEL_COUNT = 12
+KERNEL_COUNT = 11
 
 
 class Profile(Structure):

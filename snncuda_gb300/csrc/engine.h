@@ -170,7 +170,6 @@ struct TickState {
     int32_t stdp_enabled;     // StdpRule::enabled (runtime toggle)
     int32_t temporal_enabled; // SynapseDendriteConfig::temporal_learning_enabled
     uint32_t done_scan;       // "last block" counters
-    uint32_t done_fire_tile;
     uint32_t done_fire_list;
 };
 
@@ -230,7 +229,7 @@ struct Engine {
     SynA* ev_a0;                           // [slot_cap] each synaptic event's SynA before the event
     uint32_t* fire_bits;                   // [slot_cap/32] bitmap of due positions that fired
     uint32_t* fire_at;                     // [slot_cap] firing neuron at a due position
-    uint32_t* fire_tile;                   // bitmap tile bases
+    uint32_t* fire_tile;                   // fires per bitmap tile of kThreads words (zero between ticks)
     uint32_t* fire_list;                   // [fire_cap] firing neurons in reference order
     uint32_t* fired_tgt;                   // [N] targets that fired this tick
     uint32_t* fired_cnt;                   // [N] their fire counts
@@ -259,7 +258,7 @@ constexpr uint32_t kMaxClasses = 256;    // distinct delivery delays
 // Host-side launchers (kernels.cu).
 // `marks` (optional) holds 2 * kKernelCount events recorded around every
 // kernel (before, after) for profiling graphs.
-constexpr int kKernelCount = 12;
+constexpr int kKernelCount = 11;
 // The streams of a tick: k_temporal and k_post run on `side`, forked from
 // `main` with ev[0] / ev[2] and joined back with ev[1] / ev[3].
 struct TickStreams {

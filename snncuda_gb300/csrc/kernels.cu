@@ -20,19 +20,18 @@
 //                  its events in due order (:175-229), redoing the STDP of
 //                  events that follow a fire of the target; fires into a
 //                  due-position bitmap
-//  7. k_fire_tiles fire counts per tile of the bitmap
-//  8. k_fire_list  fires in due order (= reference fire order), raster
-//  9. k_fire_count events per (fire block, delay class); the last block scans
+//  7. k_fire_list  fires in due order (= reference fire order), raster
+//  8. k_fire_count events per (fire block, delay class); the last block scans
 //                  destinations and finishes the tick
-// 10. k_expand     copy each fire's pre-expanded (synapse, offset) events into
+//  9. k_expand     copy each fire's pre-expanded (synapse, offset) events into
 //                  their delivery slots, order-preserving
 //
 // and on a second stream (graph fork/join):
 //
-// 11. k_temporal   the neuron temporal pattern of every touched target, once
+// 10. k_temporal   the neuron temporal pattern of every touched target, once
 //                  per tick, beside 5-6
-// 12. k_post       post-spike STDP over the in-rows of targets that fired
-//                  (:138-173), beside 7-10
+// 11. k_post       post-spike STDP over the in-rows of targets that fired
+//                  (:138-173), beside 7-9
 //
 // Main-stream kernels that directly follow another are launched as
 // programmatic dependents (tick_enter), so each is scheduled while the one
@@ -1132,9 +1131,12 @@ struct Walk {
     uint32_t first_fire;  // event of the first fire
 };
 
+// A fire at due position `due`: its bit in the fire bitmap, the neuron, and
+// one more fire in the bitmap tile (kThreads words) for k_fire_list.
 __device__ __forceinline__ void record_fire(const Engine& e, const Walk& w, uint32_t due) {
     atomicOr(&e.fire_bits[due >> 5], 1u << (due & 31));
     e.fire_at[due] = w.n;
+    atomicAdd(&e.fire_tile[(due >> 5) / kThreads], 1u);
 }
 
 // Phase 1 of a target's walk: load the neuron (the physics fields only: the
@@ -1445,7 +1447,7 @@ __global__ void k_init_syn(SynAB* syn, const SynA* a, unsigned long long S) {
 
 // Post-spike STDP over the incoming rows of every target that fired
 // (NetworkPropagator.cpp:95-102), one block per fired target, coalesced over
-// the target-major row.  Runs on the side stream beside k_fire_tiles ..
+// the target-major row.  Runs on the side stream beside k_fire_list ..
 // k_expand (none of which touches synapse records), so it reads the tick
 // from post_tick, not from the tick counter k_fire_count advances.
 __global__ void k_post(Engine e) {
@@ -1467,39 +1469,25 @@ __global__ void k_post(Engine e) {
     }
 }
 
-// Popcounts of the fire bitmap tiles; the last block turns them into
-// exclusive tile bases and the tick's fire count.
-__global__ void k_fire_tiles(Engine e) {
-    tick_enter();
-    const uint32_t words = (e.ts->n_due + 31) / 32;
-    const uint32_t tiles = (words + kThreads - 1) / kThreads;
-    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        const uint32_t w = tile * kThreads + threadIdx.x;
-        uint32_t tot;
-        block_excl_scan(w < words ? __popc(e.fire_bits[w]) : 0u, &tot);
-        if (threadIdx.x == 0) e.fire_tile[tile] = tot;
-    }
-    if (last_block(&e.ts->done_fire_tile)) {
-        uint32_t total;
-        block_scan_inplace(e.fire_tile, tiles, &total);
-        if (threadIdx.x == 0) e.ts->n_fires = total;
-    }
-}
-
-// Fires in due order, one thread per bitmap word.  A fire's rank r is its
-// position in the reference's fire order (due order, NetworkPropagator.cpp:
-// 80-93); the fire list and the raster are written here and the bitmap is
-// cleared.
+// Fires in due order, one thread per bitmap word (a tile is kThreads words).
+// k_process counted every tile's fires, so a block finds the first rank of
+// its tile by adding the counts of the tiles before it.  A fire's rank r is
+// its position in the reference's fire order (due order,
+// NetworkPropagator.cpp:80-93); the fire list and the raster are written here
+// and the bitmap is cleared.
 __global__ void k_fire_list(Engine e) {
     tick_enter();
     const uint32_t t = e.ts->tick;
     const uint32_t words = (e.ts->n_due + 31) / 32;
     const uint32_t tiles = (words + kThreads - 1) / kThreads;
     const unsigned long long raster0 = e.ts->raster_count;
+    uint32_t part = 0, base = 0;
+    for (uint32_t i = threadIdx.x; i < blockIdx.x && i < tiles; i += blockDim.x) part += __ldcg(e.fire_tile + i);
+    block_excl_scan(part, &base);
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const uint32_t w = tile * kThreads + threadIdx.x;
         uint32_t bits = w < words ? e.fire_bits[w] : 0u;
-        uint32_t r = __ldcg(e.fire_tile + tile) + block_excl_scan(__popc(bits), nullptr);
+        uint32_t r = base + block_excl_scan(__popc(bits), nullptr);
         if (bits) e.fire_bits[w] = 0;
         while (bits) {
             const uint32_t bit = __ffs(bits) - 1;
@@ -1515,6 +1503,13 @@ __global__ void k_fire_list(Engine e) {
             }
             r += 1;
         }
+        // the base of this block's next tile
+        part = 0;
+        for (uint32_t i = tile + threadIdx.x; i < tile + gridDim.x && i < tiles; i += blockDim.x)
+            part += __ldcg(e.fire_tile + i);
+        uint32_t step;
+        block_excl_scan(part, &step);
+        base += step;
     }
 }
 
@@ -1525,7 +1520,17 @@ __global__ void k_fire_list(Engine e) {
 __global__ void __launch_bounds__(kFireCountThreads) k_fire_count(Engine e) {
     tick_enter();
     const uint32_t t = e.ts->tick;
-    const uint32_t nfires = e.ts->n_fires;
+    // the tick's fire count: the sum of k_process's per-tile counts
+    const uint32_t tiles = ((e.ts->n_due + 31) / 32 + kThreads - 1) / kThreads;
+    __shared__ uint32_t s_nf;
+    if (threadIdx.x == 0) s_nf = 0;
+    __syncthreads();
+    uint32_t part = 0;
+    for (uint32_t i = threadIdx.x; i < tiles; i += blockDim.x) part += __ldcg(e.fire_tile + i);
+    part = __reduce_add_sync(0xffffffffu, part);
+    if ((threadIdx.x & 31) == 0 && part) atomicAdd(&s_nf, part);
+    __syncthreads();
+    const uint32_t nfires = s_nf;
     const uint32_t nf = nfires < e.fire_cap ? nfires : e.fire_cap;
     const uint32_t D = e.D;
     // one warp per fire, one lane per delay class
@@ -1540,6 +1545,7 @@ __global__ void __launch_bounds__(kFireCountThreads) k_fire_count(Engine e) {
         }
     }
     if (!last_block(&e.ts->done_fire_list)) return;
+    for (uint32_t i = threadIdx.x; i < tiles; i += blockDim.x) e.fire_tile[i] = 0;  // zero for the next tick
     if (nfires > e.fire_cap && threadIdx.x == 0) raise_status(e, kStatusFireOverflow);
     const uint32_t blocks = (nf + kExpandFires - 1) / kExpandFires;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1570,6 +1576,7 @@ __global__ void __launch_bounds__(kFireCountThreads) k_fire_count(Engine e) {
     }
     if (threadIdx.x == 0) {
         TickState* ts = e.ts;
+        ts->n_fires = nfires;
         const uint32_t due = ts->n_due;
         const unsigned long long raster0 = ts->raster_count;
         ts->delivered += due;
@@ -1745,9 +1752,9 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     // k_scatter it slowed that kernel's atomics more than it gained)
     cudaEventRecord(s.ev[0], stream);
     cudaStreamWaitEvent(s.side, s.ev[0], 0);
-    side_mark(10, false);
+    side_mark(9, false);
     k_temporal<<<e.grid_process, kThreads, 0, s.side>>>(e);
-    side_mark(10, true);
+    side_mark(9, true);
     cudaEventRecord(s.ev[1], s.side);
     mark(false); launch_main(k_events, e.grid_wide * 4, kThreads, 0, stream, dep, e); mark(true);
     mark(false); launch_main(k_process, e.grid_process, kThreads, kProcessSmem, stream, dep, e); mark(true);
@@ -1755,11 +1762,10 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     // the expansion (synapse records are not touched by those)
     cudaEventRecord(s.ev[2], stream);
     cudaStreamWaitEvent(s.side, s.ev[2], 0);
-    side_mark(11, false);
+    side_mark(10, false);
     k_post<<<wide * 4, kThreads, 0, s.side>>>(e);
-    side_mark(11, true);
+    side_mark(10, true);
     cudaEventRecord(s.ev[3], s.side);
-    mark(false); launch_main(k_fire_tiles, wide, kThreads, 0, stream, dep, e); mark(true);
     mark(false); launch_main(k_fire_list, e.grid_fire, kThreads, 0, stream, dep, e); mark(true);
     cudaStreamWaitEvent(stream, s.ev[1], 0);  // k_temporal reads the tick counter k_fire_count advances
     mark(false); launch_main(k_fire_count, e.grid_wide / 4 + 1, kFireCountThreads, 0, stream, false, e); mark(true);
@@ -1768,9 +1774,9 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
 }
 
 const char* kernel_name(int index) {
-    static const char* names[kKernelCount] = {"k_hist",    "k_scan_tile", "k_scan_out",   "k_scatter",
-                                              "k_events",  "k_process",   "k_fire_tiles", "k_fire_list",
-                                              "k_fire_count", "k_expand", "k_temporal",  "k_post"};
+    static const char* names[kKernelCount] = {"k_hist",      "k_scan_tile",  "k_scan_out", "k_scatter",
+                                              "k_events",    "k_process",    "k_fire_list", "k_fire_count",
+                                              "k_expand",    "k_temporal",   "k_post"};
     return index >= 0 && index < kKernelCount ? names[index] : "";
 }
 
