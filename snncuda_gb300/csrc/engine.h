@@ -248,6 +248,7 @@ struct Engine {
     // launch shapes
     uint32_t grid_wide;
     uint32_t grid_process;
+    uint32_t grid_walk;  // k_process blocks
     uint32_t grid_fire;
 };
 

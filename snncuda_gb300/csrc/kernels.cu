@@ -1318,9 +1318,14 @@ __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(
     const float* ltp = ltp_shared ? reinterpret_cast<const float*>(s_ev + kStageEvents) : e.tab.ltp;
     uint32_t parity = 0;
     bool staging = true;  // false after a copy outlived its wait: shared memory is no longer used
-    for (uint32_t k0 = blockIdx.x * blockDim.x; k0 < n_touched; k0 += gridDim.x * blockDim.x) {
+    // `per` consecutive touched targets per block and round: the grid has at
+    // least three blocks per SM, so one wave of equal blocks spreads over
+    // every SM (the block scheduler fills each SM to its occupancy limit)
+    const uint32_t per_even = (n_touched + gridDim.x - 1) / gridDim.x;
+    const uint32_t per = per_even < blockDim.x ? per_even : blockDim.x;
+    for (uint32_t k0 = blockIdx.x * per; k0 < n_touched; k0 += gridDim.x * per) {
         if (threadIdx.x == 0) {
-            const uint32_t k1 = k0 + blockDim.x < n_touched ? k0 + blockDim.x : n_touched;
+            const uint32_t k1 = k0 + per < n_touched ? k0 + per : n_touched;
             const uint32_t lo = e.tbeg[k0];
             const uint32_t hi = k1 < n_touched ? e.tbeg[k1] : n_due;
             const uint32_t cnt = staging ? (hi - lo < kStageEvents ? hi - lo : kStageEvents) : 0u;
@@ -1328,7 +1333,7 @@ __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(
             s_cnt = cnt;
             if (cnt > 0) bulk_load(s_ev, e.evin + lo, cnt * static_cast<uint32_t>(sizeof(EvIn)), &s_bar);
         }
-        if (ltp_shared && k0 == blockIdx.x * blockDim.x) {
+        if (ltp_shared && k0 == blockIdx.x * per) {
             float* s_ltp = reinterpret_cast<float*>(s_ev + kStageEvents);
             for (uint32_t i = threadIdx.x; i < e.tab.stdp_len; i += blockDim.x) s_ltp[i] = e.tab.ltp[i];
         }
@@ -1344,11 +1349,12 @@ __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(
             return ok;
         };
         const uint32_t k = k0 + threadIdx.x;
+        const bool mine_target = threadIdx.x < per && k < n_touched;
         Walk w;
         w.n = w.beg = w.len = w.i = w.fires = w.first_fire = 0;
         bool fired = false;
         Staged mine = st;
-        if (k < n_touched) {
+        if (mine_target) {
             w.n = e.touched[k];
             w.beg = e.tbeg[k];
             w.len = (k + 1 < n_touched ? e.tbeg[k + 1] : n_due) - w.beg;
@@ -1356,7 +1362,7 @@ __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(
         }
         if (!ready()) mine.cnt = 0;
         walk_fired_targets(e, w, fired, t, stdp, mine, ltp, s_wt[threadIdx.x >> 5]);
-        if (k < n_touched) finish_walk(e, w);
+        if (mine_target) finish_walk(e, w);
         const bool failed = __syncthreads_or(!ok);
         if (st.cnt > 0) {
             if (failed) {
@@ -1757,7 +1763,7 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     side_mark(9, true);
     cudaEventRecord(s.ev[1], s.side);
     mark(false); launch_main(k_events, e.grid_wide * 4, kThreads, 0, stream, dep, e); mark(true);
-    mark(false); launch_main(k_process, e.grid_process, kThreads, kProcessSmem, stream, dep, e); mark(true);
+    mark(false); launch_main(k_process, e.grid_walk, kThreads, kProcessSmem, stream, dep, e); mark(true);
     // post-spike STDP of the fired targets runs beside the fire ordering and
     // the expansion (synapse records are not touched by those)
     cudaEventRecord(s.ev[2], stream);

@@ -495,6 +495,11 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sim->device), "device attribute");
     e.grid_wide = static_cast<uint32_t>(std::max(1, sms * 2));
     e.grid_process = static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>((N + 255) / 256, sms * 8ull)));
+    // k_process: at least three blocks per SM (of at least 64 targets) so its
+    // one wave covers every SM; at most eight per SM
+    e.grid_walk = static_cast<uint32_t>(std::max<uint64_t>(
+        1, std::min<uint64_t>(std::max<uint64_t>((N + 255) / 256, std::min<uint64_t>(sms * 3ull, (N + 63) / 64)),
+                              sms * 8ull)));
     e.grid_fire = static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>(fire_tiles, sms * 2ull)));
     sim->ensure_far(1, 2);
     check(cudaStreamSynchronize(st), "create synchronize");
