@@ -1523,7 +1523,7 @@ __global__ void k_fire_list(Engine e) {
 // per fire and one lane per class.  The last block turns the counts into wheel positions
 // (exclusive scan over blocks per class, appended behind each delivery slot's
 // current contents) and finishes the tick.
-__global__ void __launch_bounds__(kFireCountThreads) k_fire_count(Engine e) {
+__global__ void __launch_bounds__(kFireCountThreads, 1) k_fire_count(Engine e) {
     tick_enter();
     const uint32_t t = e.ts->tick;
     // the tick's fire count: the sum of k_process's per-tile counts
@@ -1559,16 +1559,17 @@ __global__ void __launch_bounds__(kFireCountThreads) k_fire_count(Engine e) {
         const uint32_t slot = (t + e.cls_delta[d]) & e.wmask;
         const uint32_t start = e.slot_count[slot];
         uint32_t carry = 0;
+        uint32_t v = static_cast<uint32_t>(lane) < blocks ? __ldcg(e.xsum + static_cast<size_t>(lane) * D + d) : 0;
         for (uint32_t b0 = 0; b0 < blocks; b0 += 32) {
             const uint32_t b = b0 + lane;
-            const uint32_t v = b < blocks ? __ldcg(e.xsum + static_cast<size_t>(b) * D + d) : 0;
+            // the next chunk's counts are fetched before this chunk's stores
+            const uint32_t vn = b + 32 < blocks ? __ldcg(e.xsum + static_cast<size_t>(b + 32) * D + d) : 0;
             const uint32_t incl = warp_incl_scan(v);
-            if (b < blocks) {
+            if (b < blocks)
                 e.xdst[static_cast<size_t>(b) * D + d] =
                     static_cast<unsigned long long>(slot) * e.slot_cap + start + carry + incl - v;
-                e.xsum[static_cast<size_t>(b) * D + d] = 0;
-            }
             carry += __shfl_sync(0xffffffffu, incl, 31);
+            v = vn;
         }
         if (lane == 0) {
             if (static_cast<unsigned long long>(start) + carry > e.slot_cap) {
@@ -1580,6 +1581,10 @@ __global__ void __launch_bounds__(kFireCountThreads) k_fire_count(Engine e) {
             }
         }
     }
+    // the class counts back to zero for the next tick, once every warp has
+    // read its classes
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < blocks * D; i += blockDim.x) e.xsum[i] = 0;
     if (threadIdx.x == 0) {
         TickState* ts = e.ts;
         ts->n_fires = nfires;

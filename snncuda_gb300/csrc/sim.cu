@@ -500,7 +500,7 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.grid_walk = static_cast<uint32_t>(std::max<uint64_t>(
         1, std::min<uint64_t>(std::max<uint64_t>((N + 255) / 256, std::min<uint64_t>(sms * 3ull, (N + 63) / 64)),
                               sms * 8ull)));
-    e.grid_fire = static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>(fire_tiles, sms * 2ull)));
+    e.grid_fire = static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>(fire_tiles, sms * 8ull)));
     sim->ensure_far(1, 2);
     check(cudaStreamSynchronize(st), "create synchronize");
 }
