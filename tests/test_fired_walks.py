@@ -57,6 +57,17 @@ def test_oracle_fan_in_has_many_events_after_fires(port_lib, codes, threshold):
     assert events_per_target_tick >= 2 * SOURCES - 8
 
 
+@pytest.mark.parametrize("codes,threshold", [((0,), 3.0), ((0, 1), 40.0)])
+def test_oracle_fan_in_matches_reference(port_lib, ref_lib, codes, threshold):
+    """The CPU restatement against the reference runtime built from its own
+    sources on the same fan-in network (pins the many-fires-per-tick case)."""
+    got, want = run(port_lib, codes, True, threshold), run(ref_lib, codes, True, threshold)
+    for k in want[0]:
+        assert got[0][k] == want[0][k], k
+    assert np.array_equal(got[2][0], want[2][0]) and np.array_equal(got[2][1], want[2][1])
+    assert got[1] == want[1]
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("codes,stdp,threshold", [((0,), True, 3.0), ((0,), True, 40.0), ((0, 1), True, 40.0),
                                                   ((0, 1), True, 3.0), ((0,), False, 40.0)])
