@@ -9,6 +9,8 @@ import pathlib
 import pytest
 
 from scenarios import SCENARIOS, run_scenario
+from snncuda_gb300 import synthetic
+from snncuda_gb300.simulation import Simulation, default_config
 
 GOLDEN = json.loads((pathlib.Path(__file__).parent / "golden" / "scenarios.json").read_text())
 
@@ -48,3 +50,22 @@ def test_planted_mistake_is_caught(port_lib):
     sim.run_until(5)
     nd, sd = sim.digest()
     assert f"{nd:016x}" != GOLDEN["three_stage"]["probes"][-1]["neuron_digest"]
+
+
+def test_port_matches_reference_on_stdp_network(port_lib, ref_lib):
+    """At the size the GPU parity tests use against the port: 5,000 neurons,
+    fan-out 1,000 (5e6 synapses), the stdp_100k distributions, 200 ticks
+    (~1.2e7 synaptic events) -- the port equals the reference runtime."""
+    w = synthetic.STDP_100K.scaled(neurons=5_000, fanout=1000, weight_scale=0.01, max_weight=1.0, seed=21)
+    net = synthetic.build_network(w)
+    drive = synthetic.build_drive(w, 200)
+    out = []
+    for lib in (port_lib, ref_lib):
+        sim = Simulation(net, default_config(lib, max_weight=1.0), lib)
+        sim.inject(*drive)
+        sim.run_until(199)
+        out.append((sim.counters(), sim.digest()))
+        sim.close()
+    assert out[0][0]["synaptic_events"] > 1_000_000
+    assert out[0][0] == out[1][0]
+    assert out[0][1] == out[1][1]
