@@ -554,6 +554,18 @@ class NetworkPropagator:
             int(a["code_window_start_tick"][i]), self.sim.pattern(2, i), learned,
             int(a["code_match_count"][i]), bool(a["last_code_match"][i]))
 
+    def cache_eviction_count(self) -> int:
+        """NetworkPropagator::cache_eviction_count (NetworkPropagator.h:27):
+        neuron state never leaves device memory here, so nothing is evicted
+        (the reference counts its LRU page-outs)."""
+        return 0
+
+    def resident_neuron_count(self) -> int:
+        """NetworkPropagator::resident_neuron_count (NetworkPropagator.h:28):
+        every neuron is resident in device memory (the reference counts the
+        neurons its LRU cache currently holds)."""
+        return self.sim.neuron_count
+
     def idle(self) -> bool:
         self._flush()
         return self.sim.idle()

@@ -133,6 +133,8 @@ def test_state_paging_under_tiny_resident_capacity(lib):
     p.inject(net.populations["input"][0], 0, 1.0)
     p.run_until(1)
     assert p.spike_count(1) == 1 and p.spike_count(2) == 1
+    # no paging here: every neuron stays resident in device memory
+    assert p.cache_eviction_count() == 0 and p.resident_neuron_count() == 2
 
 
 def test_late_injection_is_clamped_to_next_tick(lib):
