@@ -457,9 +457,8 @@ def main():
         return
     if args.rmw_floor:
         import __graft_entry__
-        __graft_entry__.build()
-        out = subprocess.run([str(ROOT / "snncuda_gb300" / "_lib" / "rmw_floor")], check=True,
-                             stdout=subprocess.PIPE, text=True).stdout
+        exe = __graft_entry__.build_rmw_floor()
+        out = subprocess.run([str(exe)], check=True, stdout=subprocess.PIPE, text=True).stdout
         print(out.strip(), flush=True)
         return
     if args.batched:

@@ -102,7 +102,7 @@ typedef struct snncuda_config {
     float max_weight;                  /* 2 */
     int32_t temporal_learning_enabled; /* 1 */
 
-    /* Engine options (0 = default). */
+    /* Engine options (0 = default, except stage_wait_ns). */
     uint64_t timing_wheel_slots;       /* accepted for parity with the reference
                                           constructor; must be nonzero
                                           (SpikeScheduler.cpp:10-12) */
@@ -113,6 +113,14 @@ typedef struct snncuda_config {
                                           0 disables capture */
     void* cuda_stream;                 /* cudaStream_t to launch on; NULL =
                                           the handle creates its own */
+    uint64_t stage_wait_ns;            /* limit of the tick's bounded wait for
+                                          a bulk copy into shared memory
+                                          (default 100 ms).  When it runs out
+                                          the tick reads its inputs from
+                                          global memory (results unchanged)
+                                          and the run returns
+                                          SNNCUDA_ERR_TIMEOUT, poisoning the
+                                          handle; 0 gives up without waiting */
 } snncuda_config;
 
 /* Fills the reference defaults. */
@@ -263,9 +271,9 @@ typedef struct snncuda_server_config {
 } snncuda_server_config;
 int snncuda_server_create(const snncuda_server_config* config, snncuda_server** out);
 int snncuda_server_destroy(snncuda_server* server);
-/* Queues a job that runs ticks 0 .. ticks-1.  The network's arrays are read
- * when the job is admitted and must stay valid until then; the injections
- * are copied.  *job_id numbers jobs from 0 in submission order. */
+/* Queues a job that runs ticks 0 .. ticks-1.  The network's arrays and the
+ * injections are copied here: the caller may free them when the call
+ * returns.  *job_id numbers jobs from 0 in submission order. */
 int snncuda_server_submit(snncuda_server* server, const snncuda_network* network, const snncuda_config* config,
                           uint64_t inject_count, const uint32_t* neurons, const uint64_t* ticks,
                           const float* weights, uint64_t run_ticks, uint64_t* job_id);
@@ -345,7 +353,9 @@ int snncuda_group_events(const uint64_t* events, uint32_t count, uint32_t neuron
  * and neuron_count <= SNNCUDA_GROUP_STATIC_MAX_NEURONS, otherwise
  * SNNCUDA_ERR_CAPACITY.  The first call on a device looks up the array's
  * device address (cudaGetSymbolAddress) with that device current; make that
- * first call before any stream capture.  Every call shares the one array:
+ * first call before any stream capture (later calls made outside a capture
+ * look the address up again, so it stays valid across a cudaDeviceReset).
+ * Every call shares the one array:
  * calls that overlap on the GPU (other streams or host threads) race and must
  * be serialized by the caller. */
 #define SNNCUDA_GROUP_STATIC_MAX_EVENTS (1u << 20)

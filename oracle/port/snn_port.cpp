@@ -379,6 +379,7 @@ void snncuda_config_default(snncuda_config* c) {
     c->max_weight = 2.0F;
     c->temporal_learning_enabled = 1;
     c->timing_wheel_slots = 4096;
+    c->stage_wait_ns = 100000000ULL;  // engine option; no device waits here
 }
 
 int snncuda_sim_create(const snncuda_network* net, const snncuda_config* cfg, snncuda_sim** out) {

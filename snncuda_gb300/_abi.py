@@ -63,6 +63,7 @@ class Config(Structure):
         ("pattern_run_capacity", c_uint64),
         ("raster_capacity", c_uint64),
         ("cuda_stream", c_void_p),
+        ("stage_wait_ns", c_uint64),
     ]
 
 

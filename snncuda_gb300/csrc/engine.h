@@ -194,6 +194,7 @@ struct Engine {
     uint32_t fire_cap;
     uint32_t fire_tiles_cap;
     float min_weight;
+    unsigned long long stage_wait_ns;  // limit of k_process's wait for its staged event inputs
 
     // network
     const unsigned long long* in_ptr;      // [N+1] target-major row pointers

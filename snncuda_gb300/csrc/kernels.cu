@@ -114,9 +114,11 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return v;
 }
 
-// Waits for phase `parity` of the barrier to complete, for at most about
-// 100 ms; returns false if it did not.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity) {
+// Waits for phase `parity` of the barrier to complete, for at most
+// `limit_ns` nanoseconds (and at most 2^24 polls); returns false if it did
+// not.  A limit of 0 gives up without polling.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity, unsigned long long limit_ns) {
+    if (limit_ns == 0) return false;
     const uint32_t a = smem_addr(bar);
     const unsigned long long t0 = global_ns();
     for (uint32_t it = 0; it < (1u << 24); ++it) {
@@ -127,10 +129,15 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t pari
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
-        if ((it & 255u) == 255u && global_ns() - t0 > 100000000ull) break;
+        if ((it & 255u) == 255u && global_ns() - t0 > limit_ns) break;
     }
     return false;
 }
+
+// Limit of the wait that drains a bulk copy still in flight before its
+// shared-memory buffer is reused or the block exits (1 s: a copy of at most
+// 64 KB completes in microseconds).
+constexpr unsigned long long kDrainWaitNs = 1000000000ull;
 
 // ---------------------------------------------------------------------------
 // block-level helpers
@@ -807,11 +814,87 @@ __global__ void k_scatter(Engine e) {
     }
 }
 
+// Sort key of a grouped entry: its due index (unique within one due list).
+__device__ __forceinline__ uint32_t grp_key(unsigned long long v) { return static_cast<uint32_t>(v) & ~kExternalBit; }
+
+// Ascending bitonic sort of one entry per lane by key (lanes without an
+// entry carry key 0xFFFFFFFF and sort last).
+__device__ __forceinline__ void warp_bitonic(unsigned long long& v, uint32_t& key) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            const uint32_t ok = __shfl_xor_sync(0xffffffffu, key, stride);
+            const unsigned long long ov = __shfl_xor_sync(0xffffffffu, v, stride);
+            const bool up = ((lane & size) == 0);
+            const bool lower = (lane & stride) == 0;
+            const bool take_min = (lower == up);
+            if (take_min ? (ok < key) : (ok > key)) {
+                key = ok;
+                v = ov;
+            }
+        }
+    }
+}
+
+// One warp sorts entries [0, len) of `a` by key into `b` (a is scratch and
+// is overwritten).  Runs of 32 are sorted in registers, then runs are merged
+// pairwise, doubling their width: an entry's place in the merged run is its
+// index in its own run plus the number of keys below it in the other run
+// (a binary search; keys are unique).  O(len log^2 len) work per warp, so a
+// segment of 2^20 entries takes milliseconds, not the len^2 of a rank count.
+__device__ void warp_merge_sort(unsigned long long* a, unsigned long long* b, uint32_t len) {
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t c = 0; c < len; c += 32) {
+        const uint32_t n = len - c < 32 ? len - c : 32;
+        unsigned long long v = lane < n ? a[c + lane] : ~0ull;
+        uint32_t key = lane < n ? grp_key(v) : 0xFFFFFFFFu;
+        warp_bitonic(v, key);
+        if (lane < n) a[c + lane] = v;
+    }
+    __syncwarp();
+    unsigned long long* src = a;
+    unsigned long long* dst = b;
+    for (uint32_t w = 32; w < len; w <<= 1) {
+        for (uint32_t base = 0; base < len; base += 2 * w) {
+            const uint32_t la = len - base < w ? len - base : w;
+            const uint32_t lb = len - base - la < w ? len - base - la : w;
+            const unsigned long long* L = src + base;
+            const unsigned long long* R = L + la;
+            for (uint32_t j = lane; j < la + lb; j += 32) {
+                const bool left = j < la;
+                const unsigned long long v = left ? L[j] : R[j - la];
+                const uint32_t key = grp_key(v);
+                const unsigned long long* other = left ? R : L;
+                uint32_t lo = 0, hi = left ? lb : la;  // keys of `other` below key
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (grp_key(other[mid]) < key) {
+                        lo = mid + 1;
+                    } else {
+                        hi = mid;
+                    }
+                }
+                dst[base + (left ? j : j - la) + lo] = v;
+            }
+        }
+        __syncwarp();
+        unsigned long long* t = src;
+        src = dst;
+        dst = t;
+    }
+    if (src != b) {
+        for (uint32_t j = lane; j < len; j += 32) b[j] = src[j];
+        __syncwarp();
+    }
+}
+
 // Restore due order inside every target's group (k_scatter leaves it in
 // arbitrary order; keys are unique due indices).  One warp per target:
 // groups of up to 32 events are bitonic-sorted in registers, longer ones are
-// placed by rank (number of smaller keys).  Output goes to grp_sorted.  Used
-// by the grouping entry point; the tick sorts inside k_events.
+// merge-sorted (warp_merge_sort).  Output goes to grp_sorted.  Used by the
+// grouping entry point; the tick sorts inside k_events.
 __global__ void __launch_bounds__(kThreads) k_segsort(Engine e) {
     const uint32_t n_touched = e.ts->n_touched;
     const uint32_t n_due = e.ts->n_due;
@@ -822,37 +905,17 @@ __global__ void __launch_bounds__(kThreads) k_segsort(Engine e) {
         const uint32_t beg = e.seg_start[n];
         const uint32_t end = k + 1 < n_touched ? e.seg_start[e.touched[k + 1]] : n_due;
         const uint32_t len = end - beg;
-        const unsigned long long* src = e.grp + beg;
+        unsigned long long* src = e.grp + beg;
         unsigned long long* dst = e.grp_sorted + beg;
         for (uint32_t j = lane; j < len; j += 32) e.evt_tgt[beg + j] = n;
         if (lane == 0) e.seg_len[n] = len;
         if (len <= 32) {
             unsigned long long v = lane < static_cast<int>(len) ? src[lane] : ~0ull;
-            uint32_t key = lane < static_cast<int>(len) ? static_cast<uint32_t>(v) & ~kExternalBit : 0xFFFFFFFFu;
-#pragma unroll
-            for (int size = 2; size <= 32; size <<= 1) {
-#pragma unroll
-                for (int stride = size >> 1; stride > 0; stride >>= 1) {
-                    const uint32_t ok = __shfl_xor_sync(0xffffffffu, key, stride);
-                    const unsigned long long ov = __shfl_xor_sync(0xffffffffu, v, stride);
-                    const bool up = ((lane & size) == 0);
-                    const bool lower = (lane & stride) == 0;
-                    const bool take_min = (lower == up);
-                    if (take_min ? (ok < key) : (ok > key)) {
-                        key = ok;
-                        v = ov;
-                    }
-                }
-            }
+            uint32_t key = lane < static_cast<int>(len) ? grp_key(v) : 0xFFFFFFFFu;
+            warp_bitonic(v, key);
             if (lane < static_cast<int>(len)) dst[lane] = v;
         } else {
-            for (uint32_t j = lane; j < len; j += 32) {
-                const unsigned long long v = src[j];
-                const uint32_t key = static_cast<uint32_t>(v) & ~kExternalBit;
-                uint32_t rank = 0;
-                for (uint32_t i = 0; i < len; ++i) rank += (static_cast<uint32_t>(src[i]) & ~kExternalBit) < key;
-                dst[rank] = v;
-            }
+            warp_merge_sort(src, dst, len);
         }
     }
 }
@@ -1010,16 +1073,8 @@ __device__ __forceinline__ void events_of_target(const Engine& e, uint32_t n, ui
         __syncwarp();
         return;
     }
-    const unsigned long long* src = e.grp + beg;
     unsigned long long* srt = e.grp_sorted + beg;
-    for (uint32_t j = lane; j < len; j += 32) {
-        const unsigned long long x = src[j];
-        const uint32_t key = static_cast<uint32_t>(x) & ~kExternalBit;
-        uint32_t rank = 0;
-        for (uint32_t i = 0; i < len; ++i) rank += (static_cast<uint32_t>(src[i]) & ~kExternalBit) < key;
-        srt[rank] = x;
-    }
-    __syncwarp();
+    warp_merge_sort(e.grp + beg, srt, len);
     const NeuronParam p = e.nparam[n];
     for (uint32_t j = lane; j < len; j += 32) {
         const unsigned long long x = srt[j];
@@ -1343,7 +1398,7 @@ __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(
         bool ok = true;
         auto ready = [&]() {
             if (!waited) {
-                ok = mbar_wait(&s_bar, parity);
+                ok = mbar_wait(&s_bar, parity, e.stage_wait_ns);
                 waited = true;
             }
             return ok;
@@ -1369,7 +1424,7 @@ __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(
                 // the block read its inputs from global memory; wait once more
                 // for the copy before the buffer is reused or the block exits
                 if (threadIdx.x == 0) raise_status(e, kStatusStageTimeout);
-                if (!__syncthreads_and(mbar_wait(&s_bar, parity))) return;
+                if (!__syncthreads_and(mbar_wait(&s_bar, parity, kDrainWaitNs))) return;
             }
             parity ^= 1u;
         }

@@ -331,6 +331,7 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.N = N;
     e.S = S;
     e.min_weight = cfg.min_weight;
+    e.stage_wait_ns = cfg.stage_wait_ns;
 
     // ---- synapse side, packed on the device: validation, target-major
     // order, synapse records, pre-expanded outgoing events ----
@@ -805,6 +806,7 @@ void snncuda_config_default(snncuda_config* c) {
     c->max_weight = 2.0F;
     c->temporal_learning_enabled = 1;
     c->timing_wheel_slots = 4096;
+    c->stage_wait_ns = 100000000ULL;
 }
 
 int snncuda_sim_create(const snncuda_network* net, const snncuda_config* config, snncuda_sim** out) {
@@ -1196,14 +1198,20 @@ constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mutex;
 unsigned char* g_scratch_addr[kMaxDevices] = {};
 
-// Device address of the static scratch on the current device (looked up once
-// per device, with that device current).
-unsigned char* static_scratch() {
+// Device address of the static scratch on the current device.  Set up on the
+// first call on a device, with that device current (cudaGetSymbolAddress may
+// load the module then, which a stream capture does not allow).  Later calls
+// made outside a stream capture look it up again (a cheap table lookup), so
+// the address follows the module if a cudaDeviceReset reloaded it; a call
+// inside a capture uses the address of the last call.
+unsigned char* static_scratch(cudaStream_t st) {
     int dev = 0;
     check(cudaGetDevice(&dev), "cudaGetDevice");
     if (dev < 0 || dev >= kMaxDevices) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "device index too large");
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (g_scratch_addr[dev] == nullptr) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (g_scratch_addr[dev] != nullptr) check(cudaStreamIsCapturing(st, &cap), "cudaStreamIsCapturing");
+    if (g_scratch_addr[dev] == nullptr || cap == cudaStreamCaptureStatusNone) {
         void* p = nullptr;
         check(cudaGetSymbolAddress(&p, g_group_scratch), "cudaGetSymbolAddress");
         g_scratch_addr[dev] = static_cast<unsigned char*>(p);
@@ -1224,8 +1232,8 @@ int snncuda_group_events_static(const uint64_t* events, uint32_t count, uint32_t
                          "snncuda_group_events_static handles at most 2^20 events and 2^18 neurons; "
                          "use snncuda_group_events");
     cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
-    return guarded([&] {
-        unsigned char* base = static_scratch();
+    const int rc = guarded([&] {
+        unsigned char* base = static_scratch(st);
         GroupScratch sc;
         sc.cnt = reinterpret_cast<uint32_t*>(base + kOffCnt);
         sc.touched = reinterpret_cast<uint32_t*>(base + kOffTouched);
@@ -1237,6 +1245,10 @@ int snncuda_group_events_static(const uint64_t* events, uint32_t count, uint32_t
         sc.ts = reinterpret_cast<TickState*>(base + kOffTs);
         group_run(events, count, neuron_count, grouped, segment_start, st, sc);
     });
+    // a failed call may have left kernels writing the shared scratch and the
+    // caller's buffers: they finish before the caller's next call can start
+    if (rc != SNNCUDA_OK) cudaStreamSynchronize(st);
+    return rc;
 }
 
 int snncuda_sim_read_raster(snncuda_sim* sim, uint64_t first, uint64_t count, uint64_t* ticks, uint32_t* neurons) {
@@ -1555,7 +1567,65 @@ static uint64_t estimate_bytes_impl(const snncuda_network* net, const snncuda_co
     return persistent + transient;
 }
 
+// A job's own copy of its network's arrays (submit copies them, so the
+// caller's buffers may go away before the worker thread creates the job).
+extern "C++" {
+struct NetworkCopy {
+    std::vector<float> threshold, similarity, weight, max_weight;
+    std::vector<uint64_t> window, refs, code_ptr;
+    std::vector<uint32_t> source, target, delay, codes;
+    std::vector<uint8_t> compartment, receptor, plastic;
+
+    template <typename T>
+    static void take(std::vector<T>& v, const T* p, uint64_t n) {
+        if (p) v.assign(p, p + n);
+    }
+    // The copy, seen as an snncuda_network (null where the caller's was).
+    snncuda_network copy_of(const snncuda_network& n) {
+        const uint32_t N = n.neuron_count;
+        const uint64_t S = n.synapse_count;
+        take(threshold, n.threshold, N);
+        take(window, n.pattern_window_ticks, N);
+        take(similarity, n.similarity_threshold, N);
+        take(refs, n.max_reference_patterns, N);
+        take(source, n.source, S);
+        take(target, n.target, S);
+        take(weight, n.weight, S);
+        take(max_weight, n.max_weight, S);
+        take(delay, n.delay_ticks, S);
+        take(compartment, n.compartment, S);
+        take(receptor, n.receptor, S);
+        take(plastic, n.plasticity_enabled, S);
+        const bool codes_given = n.code_offset_ptr != nullptr && n.code_offsets != nullptr;
+        if (codes_given) {
+            take(code_ptr, n.code_offset_ptr, S + 1);
+            take(codes, n.code_offsets, n.code_offset_ptr[S]);
+            if (codes.empty()) codes.push_back(0);  // a non-null array of no offsets
+        }
+        auto at = [](auto& v, const void* orig) { return orig ? v.data() : nullptr; };
+        snncuda_network c = n;
+        c.threshold = at(threshold, n.threshold);
+        c.pattern_window_ticks = at(window, n.pattern_window_ticks);
+        c.similarity_threshold = at(similarity, n.similarity_threshold);
+        c.max_reference_patterns = at(refs, n.max_reference_patterns);
+        c.source = at(source, n.source);
+        c.target = at(target, n.target);
+        c.weight = at(weight, n.weight);
+        c.max_weight = at(max_weight, n.max_weight);
+        c.delay_ticks = at(delay, n.delay_ticks);
+        c.compartment = at(compartment, n.compartment);
+        c.receptor = at(receptor, n.receptor);
+        c.plasticity_enabled = at(plastic, n.plasticity_enabled);
+        c.code_offset_ptr = codes_given ? code_ptr.data() : nullptr;
+        c.code_offsets = codes_given ? codes.data() : nullptr;
+        return c;
+    }
+    void release() { *this = NetworkCopy{}; }
+};
+}  // extern "C++"
+
 struct ServerJob {
+    NetworkCopy arrays;     // owned copy of the network's arrays (freed once created)
     snncuda_network net{};
     snncuda_config cfg{};
     std::vector<uint32_t> inj_n;
@@ -1607,8 +1677,9 @@ struct snncuda_server {
             if (rc == SNNCUDA_OK)
                 rc = snncuda_sim_inject(j.sim, j.inj_n.size(), j.inj_n.data(), j.inj_t.data(), j.inj_w.data());
             if (rc == SNNCUDA_OK) sort_pending(j.sim);  // host work off the stepping thread
-            j.res.error = rc;
+            j.arrays.release();                          // the device holds the network now
             std::lock_guard<std::mutex> lock(mu);
+            j.res.error = rc;
             created.push_back(id);
         }
     }
@@ -1629,9 +1700,12 @@ struct snncuda_server {
 };
 
 static void server_finish(snncuda_server* sv, ServerJob& j, int state, int error) {
-    j.res.state = state;
-    j.res.error = error;
-    j.res.finished_s = sv->now();
+    {
+        std::lock_guard<std::mutex> lock(sv->mu);
+        j.res.state = state;
+        j.res.error = error;
+        j.res.finished_s = sv->now();
+    }
     delete j.sim;
     j.sim = nullptr;
     sv->used -= j.bytes;
@@ -1670,7 +1744,7 @@ int snncuda_server_submit(snncuda_server* sv, const snncuda_network* network, co
     if (inject_count > 0 && (!neurons || !ticks || !weights)) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null array");
     return guarded([&] {
         std::unique_ptr<ServerJob> j(new ServerJob());
-        j->net = *network;
+        j->net = j->arrays.copy_of(*network);
         snncuda_config_default(&j->cfg);
         if (config) j->cfg = *config;
         j->cfg.cuda_stream = nullptr;  // every job on a stream of its own
@@ -1726,7 +1800,11 @@ int snncuda_server_step(snncuda_server* sv, uint32_t* active) {
     for (uint64_t id : ready) {
         ServerJob& j = *sv->jobs_at(id);
         sv->creating -= 1;
-        int rc = j.res.error;
+        int rc;
+        {
+            std::lock_guard<std::mutex> lock(sv->mu);
+            rc = j.res.error;
+        }
         if (rc == SNNCUDA_OK && j.ticks > 0)
             rc = guarded([&] { run_enqueue(j.sim, std::min<uint64_t>(slice, j.ticks) - 1); });
         if (rc != SNNCUDA_OK) {
@@ -1759,7 +1837,8 @@ int snncuda_server_step(snncuda_server* sv, uint32_t* active) {
 int snncuda_server_job(snncuda_server* sv, uint64_t job_id, snncuda_job_result* out) {
     if (sv == nullptr || out == nullptr || job_id >= sv->jobs.size())
         return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "bad server or job");
-    *out = sv->jobs_at(job_id)->res;
+    std::lock_guard<std::mutex> lock(sv->mu);
+    *out = sv->jobs[job_id]->res;
     return SNNCUDA_OK;
 }
 

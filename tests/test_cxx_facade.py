@@ -6,6 +6,7 @@ against the reference's own declarative::Connectome where those headers are
 present."""
 
 import json
+import os
 import pathlib
 import shutil
 import subprocess
@@ -17,7 +18,7 @@ from conftest import GPU_PATH, PORT_PATH, ROOT, _ensure_built
 from snncuda_gb300.connectome import Connectome
 from snncuda_gb300.simulation import Simulation, default_config
 
-REF_INCLUDE = pathlib.Path("/root/reference/include")
+REF_INCLUDE = pathlib.Path(os.environ.get("SNNCUDA_REFERENCE_DIR", "/root/reference")) / "include"
 
 MOCK = r"""
 #include <cstdint>

@@ -101,3 +101,21 @@ def test_gpu_grouping_rejects_overlapping_output(gpu_lib, fn):
         rc = getattr(gpu_lib, fn)(d_ev.data_ptr(), 16, 3, d_ev.data_ptr() + shift, d_s.data_ptr(),
                                   torch.cuda.current_stream().cuda_stream)
         assert rc == 1, shift
+
+
+@pytest.mark.gpu
+@pytest.mark.timeout(300)
+@pytest.mark.parametrize("fn", ["snncuda_group_events", "snncuda_group_events_static"])
+def test_gpu_grouping_one_hot_target(gpu_lib, fn):
+    """2^20 events, most of them on one neuron: the long segment is merge-
+    sorted by one warp (O(n log^2 n)), not ranked by counting (O(n^2))."""
+    rng = np.random.default_rng(17)
+    count, neurons = 1 << 20, 4096
+    ev = make_events(rng, count, neurons)
+    hot = rng.random(count) < 0.9
+    ev[hot] = (ev[hot] & ~np.uint64(0x7FFFFFFF)) | np.uint64(123)
+    rc, g, s = run_device(gpu_lib, ev, neurons, fn)
+    assert rc == 0
+    want_g, want_s = expected_grouping(ev, neurons)
+    assert np.array_equal(s, want_s)
+    assert np.array_equal(g, want_g)

@@ -2,13 +2,20 @@
 cannot allocate device memory (its scratch is a static array inside the
 library).  Through the C ABI, two calls in a row must give exactly the
 results of snncuda_group_events (integer output: bit-exact) on the same
-inputs, and sizes beyond the static limits must be refused.  This file is
+inputs, the largest case it accepts must equal the numpy restatement of the
+grouping, and sizes beyond the static limits must be refused.  This file is
 collected last so a failure here never hides the other tests."""
 
 import numpy as np
 import pytest
 
+from test_group_events import expected_grouping
+
 pytestmark = pytest.mark.gpu
+
+MAX_EVENTS = 1 << 20    # SNNCUDA_GROUP_STATIC_MAX_EVENTS
+MAX_NEURONS = 1 << 18   # SNNCUDA_GROUP_STATIC_MAX_NEURONS
+SNNCUDA_ERR_CAPACITY = 3
 
 
 def _call(lib, fn, events, neurons):
@@ -31,7 +38,7 @@ def _events(seed, count, neurons):
 
 
 def test_static_scratch_matches_allocating_entry_point(gpu_lib):
-    cases = [(1, 300_000, 100_000), (2, 1 << 20, 1 << 18), (3, 5_000, 70_000)]
+    cases = [(1, 300_000, 100_000), (2, MAX_EVENTS, MAX_NEURONS), (3, 5_000, 70_000)]
     inputs = [(_events(seed, count, neurons), neurons) for seed, count, neurons in cases]
     expected = [_call(gpu_lib, "snncuda_group_events", ev, n) for ev, n in inputs]
     # the static calls follow one another: each finds the previous call's
@@ -43,6 +50,20 @@ def test_static_scratch_matches_allocating_entry_point(gpu_lib):
         assert np.array_equal(g_a, g_b)
 
 
+def test_static_scratch_at_its_limits_equals_the_restatement(gpu_lib):
+    ev = _events(4, MAX_EVENTS, MAX_NEURONS)
+    rc, grouped, start = _call(gpu_lib, "snncuda_group_events_static", ev, MAX_NEURONS)
+    want_g, want_s = expected_grouping(ev, MAX_NEURONS)
+    assert rc == 0
+    assert np.array_equal(start, want_s)
+    assert np.array_equal(grouped, want_g)
+    # no events over the largest neuron count: every segment empty
+    rc, _, start = _call(gpu_lib, "snncuda_group_events_static", np.zeros(0, np.uint64), MAX_NEURONS)
+    assert rc == 0 and not start.any()
+
+
 def test_static_scratch_refuses_sizes_beyond_its_limits(gpu_lib):
     ev = _events(3, 16, 8)
-    assert _call(gpu_lib, "snncuda_group_events_static", ev, (1 << 18) + 1)[0] == 3
+    assert _call(gpu_lib, "snncuda_group_events_static", ev, MAX_NEURONS + 1)[0] == SNNCUDA_ERR_CAPACITY
+    ev = _events(5, MAX_EVENTS + 1, 1000)
+    assert _call(gpu_lib, "snncuda_group_events_static", ev, 1000)[0] == SNNCUDA_ERR_CAPACITY
