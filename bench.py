@@ -1,24 +1,44 @@
 """Throughput benchmark: synaptic events/s of the per-tick SNN hot path.
 
-Workload (default `stdp_100k`, the 100,000-neuron / 1e8-synapse STDP
-network with 1-4 spike-code offsets per synapse, temporal-pattern matching,
-5 Hz Poisson drive, 10,000 ticks): one *step* is `--ticks-per-step` ticks
-(default 400) of the network; W warm-up steps then K timed steps cover the
-workload's 10,000 ticks.
+Headline workload (default `recog_1m`): 1,000,000 neurons, fan-out 1,000
+(1e9 synapses, 64 GB of synapse state), lognormal weights, 1-4 spike-code
+offsets per synapse, pair STDP, temporal-pattern matching, a 16-code
+stimulus presented every 64 ticks to half the neurons over a 5 Hz Poisson
+background, 2,000 ticks.  One *step* is `--ticks-per-step` ticks (80 by
+default, so 5 warm-up and 20 timed steps cover the workload's 2,000 ticks).
+`stdp_100k` (1e5 neurons, 1e8 synapses, 10,000 ticks) is measured beside it
+and reported under the key "stdp_100k".
 
 GPU arm (default)
-  value   synaptic events/s with the whole drive injected before the timed
-          region (inputs resident in HBM); CUDA events on the simulation's
-          stream bracket the K timed steps.
-  e2e     the same metric through the public API with host buffers: each step
-          injects that step's drive from pinned host memory, runs, and reads
-          back the step's fire raster and counters.
-  roofline  the dominant kernel from a per-kernel profile of 200 extra ticks
-          (graph event nodes around every kernel), algorithmic bytes per launch
-          / average launch time, against the measured HBM copy bandwidth.
-  cpu_baseline  the CPU oracle port on a bounded prefix of the same workload.
-Reference arm (--impl reference): the CPU oracle port (the reference's own
-runtime cannot be built on the GPU host) on a bounded prefix of the workload.
+  value     synaptic events/s with the whole drive injected before the timed
+            region (inputs resident in HBM); CUDA events on the simulation's
+            stream bracket the K timed steps.
+  e2e       the same metric through the public API with host buffers: each
+            step injects that step's drive from pinned host memory, runs, and
+            reads back the step's fire raster and counters.
+  roofline  the dominant kernel, from a per-kernel profile of extra ticks
+            (graph event nodes around every kernel): the minimal algorithmic
+            bytes of its work (MINIMAL_BYTES) per launch over its average
+            launch time, against the measured HBM copy bandwidth; the bytes
+            of this engine's own layout give `layout_frac`.
+  tick_roofline  the whole tick loop's minimal bytes over the timed ticks.
+  parity    the GPU and the CPU oracle run from the same seed over a tick
+            prefix of the full stdp_100k network and of a 100,000-neuron
+            network with the recog_1m distributions: counters, fire
+            rasters, full state digests and recognition sums compared.
+  batched   64 networks of the batched comparison (N log-uniform in
+            1k-200k, fan-out 100-1,000, seeds 1000+i, STDP rule on for even
+            i, 2,000 ticks) advanced together in one autotuned batch handle,
+            against one handle per network over the same tick window, with
+            every network's device state checksums equal to its solo run's;
+            `--batched 256` runs all 256 networks (in waves that fit).
+  cpu_baseline  the oracle's events/s over a steady-state window of that
+            100,000-neuron recognition run (single-threaded, as the
+            reference runtime is): the oracle cannot hold the 1e9-synapse
+            network in host memory in a bounded time, so the CPU sample is
+            the same per-event work on a 1e8-synapse network.
+Reference arm (--impl reference): the CPU oracle on the same steady-state
+window, with the same `same_config: false` note.
 
 Multi-GPU: replicas only (independent copies of the network, one per rank,
 no collective on the data path); value = all ranks' events / max time.
@@ -50,28 +70,41 @@ METRIC = "synaptic_events_per_s"
 UNIT = "events/s"
 ORACLE = ROOT / "oracle" / "_build" / "liboracle_port.so"
 KERNELS_PER_TICK = 11   # launch_tick in snncuda_gb300/csrc/kernels.cu
-# DRAM bytes (read + write) per launch of a kernel on the default stdp_100k
-# workload, from one ncu capture of this code (profiles/); reported as
-# roofline.traffic for the dominant kernel.
-MEASURED_TRAFFIC = {("stdp_100k", "k_events"): 159.0e6 + 96.6e6}
 
-# Algorithmic bytes of the two per-event kernels (device layout in
-# snncuda_gb300/csrc/engine.h), per synaptic event, per external event and
-# per touched target:
-#   k_events   reads the grouped entry (8) and the synapse record (64), writes
-#              the record (64), the event's input (16) and the STDP snapshot
-#              (32); external events: entry + input; per target its
-#              parameters (64) and segment bounds (12)
-#   k_process  reads each event's input (16); per target its threshold (4)
-#              and the physics fields of its record, read + write (2 x 52)
-#   k_temporal per target: parameters (64), temporal record read + write
-#              (2 x 32), the temporal fields of the neuron record (2 x 12) and
-#              one run of the window (2 x 8)
-BYTES_MODEL = {
-    "k_events": (8 + 64 + 64 + 16 + 32, 8 + 16, 64 + 12),
-    "k_process": (16, 16, 4 + 2 * 52),
-    "k_temporal": (0, 0, 64 + 2 * 32 + 2 * 12 + 2 * 8),
+# Minimal algorithmic bytes of a compact structure-of-arrays design of the
+# tick, per fire F, synaptic event E, external event X, touched target U:
+#   F * (8 + 7 * fanout)   out-row pointers, per out-synapse target index,
+#                          delay and packed offsets
+#   E * (8 + 8)            event written into its wheel slot, read at delivery
+#   E * (1 + 4 + 4 + 4 + 16)  synapse flags, weight, last_post read,
+#                          last_pre write, code-state read
+#   E * (4 + 16)           weight write (counted for every event: an upper
+#                          bound) and code-state write
+#   U * 48 + X * 8         touched neurons' state read-modify-write, externals
+#   F * fanin * 16         post-spike STDP over the fired neurons' in-rows
+# Per kernel: the synapse-side kernel k_events carries the delivery read and
+# the synapse terms (8 + 29 + 20 = 57 B per synaptic event, 8 B per
+# external); k_process the touched-neuron term.  (per synaptic event, per
+# external event, per touched target)
+MINIMAL_BYTES = {
+    "k_events": (57, 8, 0),
+    "k_process": (0, 0, 48),
 }
+# Bytes of this engine's own layout (snncuda_gb300/csrc/engine.h) per
+# synaptic event, external event and touched target:
+#   k_events   grouped entry (8), synapse record read + write (2 x 64), event
+#              input (16), STDP snapshot (32); externals: entry + input; per
+#              target its parameters (64) and segment bounds (8)
+#   k_process  event input (16); per target its threshold (4) and the
+#              physics fields of its record, read + write (2 x 52)
+LAYOUT_BYTES = {
+    "k_events": (8 + 64 + 64 + 16 + 32, 8 + 16, 64 + 8),
+    "k_process": (16, 16, 4 + 2 * 52),
+}
+# DRAM bytes (read + write) per synaptic event of a kernel, from one ncu
+# capture of this code on a 20,000-neuron case of the workload (profiles/);
+# roofline.traffic scales it to the events of one full-size launch.
+MEASURED_TRAFFIC_PER_EVENT = {}
 
 
 def load_peaks():
@@ -148,37 +181,71 @@ def combine_ranks(ms, events, world, dist=None, device="cpu"):
     return float(mx[0]), float(t[1])
 
 
+def minimal_tick_bytes(w, events, fires, ext, touched):
+    """Minimal algorithmic bytes of the tick loop (the terms above MINIMAL_BYTES)."""
+    fanout = fanin = w.fanout  # synapses per source and per target
+    return (fires * (8 + 7 * fanout) + events * (8 + 8) + events * (1 + 4 + 4 + 4 + 16) + events * (4 + 16)
+            + touched * 48 + ext * 8 + fires * fanin * 16)
+
+
 def tick_roofline(w, events, fires, ext, prof, ticks, ms):
-    """Whole-tick roofline: minimal algorithmic bytes of the tick loop (a
-    compact structure-of-arrays design, per-term below) over the timed ticks,
-    against the measured HBM bandwidth.  Touched targets per tick come from the
-    profiled ticks that follow the timed region."""
+    """Whole-tick roofline over the timed ticks (touched targets per tick from
+    the profiled ticks that follow the timed region)."""
     if prof is None or prof["ticks"] == 0 or ms <= 0:
         return None
-    fanout = fanin = w.fanout  # synapses per source and per target
     touched = prof["touched_targets"] / prof["ticks"] * ticks
-    b = (fires * (8 + 7 * fanout)        # out-row pointers + per out-synapse index, delay, packed offsets
-         + events * (8 + 8)             # event written into its wheel slot, read at delivery
-         + events * (1 + 4 + 4 + 4 + 16)  # flags, weight, last_post, last_pre, code state read
-         + events * 4 + events * 16     # weight and code-state writes
-         + touched * 48 + ext * 8       # touched neurons' state read-modify-write, external inputs
-         + fires * fanin * 16)          # post-spike STDP over the fired neurons' incoming synapses
+    b = minimal_tick_bytes(w, events, fires, ext, touched)
     peak, kind = load_peaks()
     achieved = b / (ms / 1e3) / 1e9
     return {"bytes_per_event": b / max(events, 1), "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": kind}
 
 
-def workload_from_args(args):
+def kernel_roofline(w, prof, full_size):
+    """Roofline of the dominant kernel of a per-kernel profile."""
+    km = prof["kernel_ms"]
+    top = max(km, key=km.get)
+    launches = prof["ticks"]
+    peak, peak_kind = load_peaks()
+    avg_s = km[top] / launches / 1e3
+
+    def per_launch(model):
+        if top not in model:
+            return None
+        per_syn, per_ext, per_tgt = model[top]
+        return (per_syn * prof["synaptic_events"] + per_ext * prof["external_events"] +
+                per_tgt * prof["touched_targets"]) / launches
+
+    algo, layout = per_launch(MINIMAL_BYTES), per_launch(LAYOUT_BYTES)
+    achieved = algo / avg_s / 1e9 if algo else None
+    traffic = None
+    if full_size and top in MEASURED_TRAFFIC_PER_EVENT:
+        traffic = MEASURED_TRAFFIC_PER_EVENT[top] * prof["synaptic_events"] / launches
+    return {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak if achieved else None, "traffic": traffic, "peak_source": peak_kind,
+            "avg_launch_us": avg_s * 1e6, "algorithmic_bytes_per_launch": algo,
+            "layout_bytes_per_launch": layout,
+            "layout_frac": layout / avg_s / 1e9 / peak if layout else None,
+            "kernel_share": {k: v / sum(km.values()) for k, v in km.items()}}
+
+
+def workload_from_args(args, name=None):
     from snncuda_gb300 import synthetic
-    w = synthetic.WORKLOADS[args.workload]
-    if args.weight_scale is not None:
-        w = w.scaled(weight_scale=args.weight_scale)
-    if args.neurons is not None:
-        w = w.scaled(neurons=args.neurons)
-    if args.fanout is not None:
-        w = w.scaled(fanout=args.fanout)
+    w = synthetic.WORKLOADS[name or args.workload]
+    if name is None:
+        if args.weight_scale is not None:
+            w = w.scaled(weight_scale=args.weight_scale)
+        if args.neurons is not None:
+            w = w.scaled(neurons=args.neurons)
+        if args.fanout is not None:
+            w = w.scaled(fanout=args.fanout)
     return w
+
+
+def ticks_per_step(args, w):
+    if args.ticks_per_step:
+        return args.ticks_per_step
+    return 80 if w.name == "recog_1m" else 400
 
 
 SLOT_CAPACITY = 0  # --slot-capacity
@@ -194,51 +261,245 @@ def sim_config(lib, w, **extra):
     return cfg
 
 
-def cpu_sample(w, net, drive, budget_s: float, tick_chunk: int = 5, max_ticks: int = 400):
-    """Run the CPU oracle on a prefix of the workload for about budget_s."""
+def config_block(args, w, tps):
+    return {"workload": w.name, "neurons": w.neurons, "synapses": w.synapses, "fanout": w.fanout,
+            "weight_scale": w.weight_scale, "synapse_max_weight": w.max_weight, "stdp_clip": [0.0, 1.0],
+            "stdp": w.stdp_enabled, "drive_hz": w.drive_rate_hz, "drive_weight": w.drive_weight,
+            **({"stimulus_codes": w.stimulus_codes, "stimulus_period": w.stimulus_period,
+                "stimulus_weight": w.stimulus_weight, "stimulus_fraction": w.stimulus_fraction}
+               if w.stimulus_codes else {}),
+            "ticks": w.ticks, "ticks_per_step": tps, "seed": w.seed,
+            "l2": f"inputs larger than L2 (synapse state 64 B x {w.synapses:.0e} = {64 * w.synapses / 1e9:.1f} GB)",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle legs (parity and the CPU baseline)
+# ---------------------------------------------------------------------------
+
+def cpu_sample_workload():
+    """The CPU sample's network: the recog_1m distributions at 1e5 neurons
+    (fan-out 1,000: the same ~12.5 events per target and tick)."""
+    from snncuda_gb300 import synthetic
+    return synthetic.RECOG_1M.scaled(name="recog_100k", neurons=100_000)
+
+
+def run_oracle(w, net, drive, ticks, timed_from=None, chunk=5):
+    """The CPU oracle over ticks 0 .. ticks-1; returns its final counters,
+    raster, digests and recognition sums, and the events/s of ticks
+    timed_from .. ticks-1 (single-threaded)."""
     from snncuda_gb300 import _abi
     from snncuda_gb300.simulation import Simulation
     lib = _abi.bind(str(ORACLE))
-    sim = Simulation(net, sim_config(lib, w), lib)
+    sim = Simulation(net, sim_config(lib, w, raster_capacity=1 << 26), lib)
     n, t, wt = drive
-    keep = t < max_ticks
+    keep = t < ticks
     sim.inject(n[keep], t[keep], wt[keep])
-    start = time.perf_counter()
-    tick = 0
-    while tick < max_ticks:
-        tick += tick_chunk
-        sim.run_until(tick - 1)
-        if time.perf_counter() - start >= budget_s:
-            break
-    elapsed = time.perf_counter() - start
-    c = sim.counters()
+    tick, secs, events = 0, 0.0, 0
+    while tick < ticks:
+        nxt = min(ticks, tick + chunk)
+        before = sim.counters()["synaptic_events"] if timed_from is not None and tick >= timed_from else None
+        start = time.perf_counter()
+        sim.run_until(nxt - 1)
+        if before is not None:
+            secs += time.perf_counter() - start
+            events += sim.counters()["synaptic_events"] - before
+        tick = nxt
+    out = {"counters": sim.counters(), "raster": sim.raster(), "digest": sim.digest(),
+           "recognition": sim.recognition(), "timed_events": events, "timed_seconds": secs}
     sim.close()
-    return {"value": c["synaptic_events"] / elapsed, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"ticks 0..{tick - 1} of {w.name} ({c['synaptic_events']} synaptic events, "
-                      f"{elapsed:.1f} s, single-threaded oracle port)"}
+    return out
+
+
+def run_gpu_prefix(lib, w, net, drive, ticks, stream_ptr=None):
+    from snncuda_gb300.simulation import Simulation
+    extra = {"raster_capacity": 1 << 26}
+    if stream_ptr is not None:
+        extra["cuda_stream"] = stream_ptr
+    sim = Simulation(net, sim_config(lib, w, **extra), lib)
+    n, t, wt = drive
+    keep = t < ticks
+    sim.inject(n[keep], t[keep], wt[keep])
+    sim.run_until(ticks - 1)
+    out = {"counters": sim.counters(), "raster": sim.raster(), "digest": sim.digest(),
+           "recognition": sim.recognition()}
+    sim.close()
+    return out
+
+
+def compare(gpu, cpu, w, ticks):
+    keys = ("delivered_spikes", "fired_spikes", "synaptic_events", "external_events", "pending_events")
+    counters_equal = all(gpu["counters"][k] == cpu["counters"][k] for k in keys)
+    raster_equal = (np.array_equal(gpu["raster"][0], cpu["raster"][0]) and
+                    np.array_equal(gpu["raster"][1], cpu["raster"][1]))
+    return {"workload": w.name, "neurons": w.neurons, "synapses": w.synapses, "ticks": ticks,
+            "synaptic_events": gpu["counters"]["synaptic_events"], "fires": gpu["counters"]["fired_spikes"],
+            "counters_equal": counters_equal, "raster_equal": raster_equal,
+            "digests_equal": gpu["digest"] == cpu["digest"],
+            "recognition_equal": gpu["recognition"] == cpu["recognition"],
+            "recognition": gpu["recognition"]}
+
+
+class OracleThread(threading.Thread):
+    """run_oracle in a thread (the ctypes calls release the GIL, so several
+    oracle runs proceed on separate cores)."""
+
+    def __init__(self, *args, **kwargs):
+        super().__init__(daemon=True)
+        self.args, self.kwargs, self.result, self.error = args, kwargs, None, None
+
+    def run(self):
+        try:
+            self.result = run_oracle(*self.args, **self.kwargs)
+        except Exception as ex:  # reported in the JSON line
+            self.error = repr(ex)
+
+
+PARITY_TICKS = {"stdp_100k": 60, "recog_100k": 100}
+CPU_TIMED_FROM = 40  # the CPU sample's steady-state window starts here
+
+
+def parity_legs(lib):
+    """GPU vs oracle on the full stdp_100k network (ticks 0..59) and on the
+    1e5-neuron recognition network (ticks 0..99, which include a stimulus
+    presentation); the second run's ticks 40..99 are the CPU baseline."""
+    from snncuda_gb300 import synthetic
+    cases = []
+    for w in (synthetic.STDP_100K, cpu_sample_workload()):
+        T = PARITY_TICKS[w.name]
+        net = synthetic.build_network(w)
+        drive = synthetic.build_drive(w, T)
+        th = OracleThread(w, net, drive, T, timed_from=CPU_TIMED_FROM if w.name == "recog_100k" else None)
+        th.start()
+        cases.append((w, net, drive, T, th))
+    parity, cpu = {}, None
+    for w, net, drive, T, th in cases:
+        gpu = run_gpu_prefix(lib, w, net, drive, T)
+        th.join()
+        if th.error:
+            parity[w.name] = {"error": th.error}
+            continue
+        parity[w.name] = compare(gpu, th.result, w, T)
+        if w.name == "recog_100k":
+            r = th.result
+            cpu = {"value": r["timed_events"] / r["timed_seconds"], "unit": UNIT, "cores": 1, "kind": "port",
+                   "same_config": False,
+                   "sample": f"ticks {CPU_TIMED_FROM}..{T - 1} of recog_100k (recog_1m distributions at 1e5 "
+                             f"neurons x 1,000: {r['timed_events']} synaptic events, {r['timed_seconds']:.1f} s, "
+                             "single-threaded oracle port; the oracle cannot hold the 1e9-synapse network)"}
+    return parity, cpu
 
 
 def run_reference(args, w):
+    """The CPU oracle (the reference runtime's semantics, single-threaded as
+    the reference is) on the steady-state window of the CPU sample network."""
     from snncuda_gb300 import synthetic
-    net = synthetic.build_network(w)
-    drive = synthetic.build_drive(w, w.ticks)
-    sample = cpu_sample(w, net, drive, budget_s=args.cpu_seconds)
+    ws = cpu_sample_workload()
+    T = PARITY_TICKS[ws.name]
+    r = run_oracle(ws, synthetic.build_network(ws), synthetic.build_drive(ws, T), T, timed_from=CPU_TIMED_FROM)
+    value = r["timed_events"] / r["timed_seconds"]
+    sample = {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "same_config": False,
+              "sample": f"ticks {CPU_TIMED_FROM}..{T - 1} of recog_100k (recog_1m distributions at 1e5 neurons x "
+                        f"1,000: {r['timed_events']} synaptic events, {r['timed_seconds']:.1f} s, single-threaded "
+                        "oracle port; the oracle cannot hold the 1e9-synapse network)"}
+    tps = ticks_per_step(args, w)
     return {
-        "metric": METRIC, "value": sample["value"], "unit": UNIT, "impl": "reference",
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": config_block(args, w),
+        "data": "synthetic", "config": config_block(args, w, tps),
         "cpu_baseline": sample,
-        "e2e": {"value": sample["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
 
-def config_block(args, w):
-    return {"workload": w.name, "neurons": w.neurons, "synapses": w.synapses, "fanout": w.fanout,
-            "weight_scale": w.weight_scale, "ticks": w.ticks, "ticks_per_step": args.ticks_per_step,
-            "stdp": w.stdp_enabled, "drive_hz": w.drive_rate_hz, "seed": w.seed,
-            "l2": f"inputs larger than L2 (synapse state 64 B x {w.synapses:.0e} = {64 * w.synapses / 1e9:.1f} GB)",
-            "parallelism": f"replicas x{args.gpus}"}
+# ---------------------------------------------------------------------------
+# GPU legs
+# ---------------------------------------------------------------------------
+
+def timed_leg(lib, w, net, drive_all, total_ticks, tps, warmup, steps, stream, dist=None, local=0,
+              profile_ticks=0, clocks=True):
+    """Device-resident timing: `warmup` untimed steps, then `steps` timed
+    steps (CUDA events on the simulation's stream), then an optional
+    per-kernel profile of `profile_ticks` more ticks."""
+    import torch
+    from snncuda_gb300.simulation import Simulation
+    dn, dt, dw = drive_all
+    main_mask = dt < total_ticks
+    sim = Simulation(net, sim_config(lib, w, cuda_stream=stream.cuda_stream), lib)
+    sim.inject(dn[main_mask], dt[main_mask], dw[main_mask])
+    tick = 0
+    for _ in range(warmup):
+        tick += tps
+        sim.run_until(tick - 1)
+    c0 = sim.counters()
+    sampler = ClockSampler(local) if clocks else None
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    if sampler:
+        sampler.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        tick += tps
+        sim.run_until(tick - 1)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = sampler.stop() if sampler else None
+    if dist is not None:
+        dist.barrier()
+    c1 = sim.counters()
+    recognition = sim.recognition() if w.stimulus_codes else None
+    ms = ev0.elapsed_time(ev1)
+    prof = None
+    if profile_ticks > 0:
+        extra = ~main_mask
+        sim.inject(dn[extra], dt[extra], dw[extra])
+        prof = sim.profile(total_ticks + profile_ticks - 1)
+    sim.close()
+    events = c1["synaptic_events"] - c0["synaptic_events"]
+    return {"ms": ms, "events": events, "ext": c1["external_events"] - c0["external_events"],
+            "fires": c1["fired_spikes"] - c0["fired_spikes"], "clocks": clk, "recognition": recognition,
+            "prof": prof}
+
+
+def e2e_leg(lib, w, net, drive, total_ticks, tps, warmup, steps, stream):
+    """The metric through the public API with host buffers: every step copies
+    that step's injections from pinned host memory, runs, and reads back the
+    step's fire raster and counters."""
+    import torch
+    from snncuda_gb300.simulation import Simulation
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+    pn, pt, pw = pin(drive[0]), pin(drive[1]), pin(drive[2])
+    bounds = np.searchsorted(pt, np.arange(0, total_ticks + tps, tps))
+    sim = Simulation(net, sim_config(lib, w, cuda_stream=stream.cuda_stream, raster_capacity=1 << 26), lib)
+    h2d = d2h = 0
+    raster_pos = 0
+    tick = 0
+    start = None
+    cs = None
+    for step in range(warmup + steps):
+        if step == warmup:
+            torch.cuda.synchronize()
+            h2d = d2h = 0
+            start = time.perf_counter()
+            cs = sim.counters()
+        a, b = bounds[step], bounds[step + 1]
+        sim.inject(pn[a:b], pt[a:b], pw[a:b])
+        h2d += (b - a) * 16
+        tick += tps
+        sim.run_until(tick - 1)
+        c = sim.counters()
+        new = c["raster_count"] - raster_pos
+        sim.raster(raster_pos, new)
+        d2h += new * 12 + 64
+        raster_pos = c["raster_count"]
+    elapsed = time.perf_counter() - start
+    ce = sim.counters()
+    sim.close()
+    return {"value": (ce["synaptic_events"] - cs["synaptic_events"]) / elapsed, "unit": UNIT,
+            "h2d_bytes_per_step": int(h2d / steps), "d2h_bytes_per_step": int(d2h / steps)}
 
 
 def batch_members(count, nmin, nmax, ticks):
@@ -257,25 +518,34 @@ def batch_members(count, nmin, nmax, ticks):
     return out
 
 
-def run_batched(args):
-    """Synaptic events/s of `--batched` networks advanced together in one
-    batch handle, against the same networks run one after another, one
-    handle each (the reference's one-propagator-per-network usage).  Both
-    legs time the tick loop only (networks built and drives injected before
-    the timed region) with CUDA events; the batch's per-network digests must
-    equal the solo runs'."""
+def member_waves(members, wave_synapses):
+    """Consecutive members grouped into waves of at most `wave_synapses`
+    synapses (a wave larger than one GPU's memory would not fit)."""
+    waves, cur, acc = [], [], 0
+    for m in members:
+        if cur and acc + m[0].synapses > wave_synapses:
+            waves.append(cur)
+            cur, acc = [], 0
+        cur.append(m)
+        acc += m[0].synapses
+    if cur:
+        waves.append(cur)
+    return waves
+
+
+def batched_leg(lib, count, nmin, nmax, T, stream, wave_synapses=1.2e9, probe_ticks=20):
+    """The batched form against one handle per network (the reference's one
+    propagator per network), over the same tick window.  Members are built
+    and run in waves of at most `wave_synapses` synapses.  Per wave: the
+    batch runs `warm` untimed ticks, autotunes its launch shapes and slot
+    capacity on its next ticks, then runs to tick T-1 timed (CUDA events);
+    every member then runs alone to the batch's tuned tick untimed and on to
+    T-1 timed.  Each member's device state checksums after tick T-1 must
+    equal the batch's for it (per-network parity)."""
     import torch
-    import __graft_entry__
-    __graft_entry__.build()
     from snncuda_gb300 import synthetic
-    from snncuda_gb300.simulation import Batch, Simulation, backend
-    lib = backend()
-    nmin, nmax = (int(x) for x in args.batch_neurons.split(","))
-    T = args.batch_ticks
-    members = batch_members(args.batched, nmin, nmax, T)
-    nets = [synthetic.build_network(w) for w, _ in members]
-    drives = [synthetic.build_drive(w, T) for w, _ in members]
-    stream = torch.cuda.Stream()
+    from snncuda_gb300.simulation import Batch, Simulation
+    members = batch_members(count, nmin, nmax, T)
     warm = min(50, T // 4)
 
     def cfg_for(rule):
@@ -292,37 +562,61 @@ def run_batched(args):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1)
 
-    # batched leg
-    b = Batch(nets, cfg_for(True), lib, stdp_enabled=[r for _, r in members])
-    for i, d in enumerate(drives):
-        b.inject(i, *d)
-    b.run_until(warm - 1)
-    before = [b.counters(i)["synaptic_events"] for i in range(len(nets))]
-    ms_batch = timed(lambda: b.run_until(T - 1))
-    ev_batch = sum(b.counters(i)["synaptic_events"] - before[i] for i in range(len(nets)))
-    dig_batch = b.digests()
-    b.close()
-    # sequential leg
-    ms_seq, ev_seq, dig_seq = 0.0, 0, []
-    for (w, rule), net, d in zip(members, nets, drives):
-        sim = Simulation(net, cfg_for(rule), lib)
-        sim.inject(*d)
-        sim.run_until(warm - 1)
-        c0 = sim.counters()["synaptic_events"]
-        ms_seq += timed(lambda: sim.run_until(T - 1))
-        ev_seq += sim.counters()["synaptic_events"] - c0
-        dig_seq.append(sim.digest())
-        sim.close()
+    ms_b = ms_s = 0.0
+    ev_b = ev_s = 0
+    parity, tunings, timed_ticks = [], [], []
+    for wave in member_waves(members, wave_synapses):
+        nets = [synthetic.build_network(w) for w, _ in wave]
+        drives = [synthetic.build_drive(w, T) for w, _ in wave]
+        b = Batch(nets, cfg_for(True), lib, stdp_enabled=[r for _, r in wave])
+        for i, d in enumerate(drives):
+            b.inject(i, *d)
+        b.run_until(warm - 1)
+        tuning = b.autotune(probe_ticks)
+        t0 = b.counters(0)["next_tick"]
+        before = [b.counters(i)["synaptic_events"] for i in range(len(nets))]
+        ms_b += timed(lambda: b.run_until(T - 1))
+        ev_b += sum(b.counters(i)["synaptic_events"] - before[i] for i in range(len(nets)))
+        sums = b.checksums()
+        b.close()
+        tunings.append(tuning)
+        timed_ticks.append(T - t0)
+        for k, ((w, rule), net, d) in enumerate(zip(wave, nets, drives)):
+            sim = Simulation(net, cfg_for(rule), lib)
+            sim.inject(*d)
+            sim.run_until(t0 - 1)
+            c0 = sim.counters()["synaptic_events"]
+            ms_s += timed(lambda: sim.run_until(T - 1))
+            ev_s += sim.counters()["synaptic_events"] - c0
+            parity.append(sim.checksum() == sums[k])
+            sim.close()
+        del nets, drives
     return {
-        "metric": METRIC, "value": ev_batch / (ms_batch / 1e3), "unit": UNIT, "n_gpus": 1,
-        "higher_is_better": True, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"batched x{len(nets)}", "neurons": [w.neurons for w, _ in members],
-                   "fanout": [w.fanout for w, _ in members], "ticks": T, "timed_ticks": T - warm,
-                   "stdp_rule_on_even": True, "synapses_total": int(sum(w.synapses for w, _ in members))},
-        "ms_batched": ms_batch, "sequential": {"value": ev_seq / (ms_seq / 1e3), "ms": ms_seq},
-        "speedup_vs_sequential": (ev_batch / ms_batch) / (ev_seq / ms_seq) if ev_seq else None,
-        "events": ev_batch, "parity_per_network": dig_batch == dig_seq,
+        "value": ev_b / (ms_b / 1e3), "unit": UNIT,
+        "sequential": {"value": ev_s / (ms_s / 1e3), "ms": ms_s},
+        "speedup_vs_sequential": (ev_b / ms_b) / (ev_s / ms_s) if ev_s else None,
+        "ms_batched": ms_b, "events": ev_b, "parity_per_network": all(parity),
+        "networks_equal": int(sum(parity)),
+        "config": {"networks": count, "neurons_log_uniform": [nmin, nmax], "fanout_uniform": [100, 1000],
+                   "ticks": T, "timed_ticks_per_wave": timed_ticks, "waves": len(tunings),
+                   "wave_synapses_max": wave_synapses, "stdp_rule_on_even": True, "seeds": "1000 + i",
+                   "synapses_total": int(sum(w.synapses for w, _ in members)),
+                   "weights": "stdp_100k distributions, initial and per-synapse max weight x 1000 / fan-out"},
+        "autotune": tunings,
     }
+
+
+def run_batched(args):
+    """`bench.py --batched N`: the batched form on its own (batched_leg)."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from snncuda_gb300.simulation import backend
+    lib = backend()
+    nmin, nmax = (int(x) for x in args.batch_neurons.split(","))
+    out = batched_leg(lib, args.batched, nmin, nmax, args.batch_ticks, torch.cuda.Stream(),
+                      wave_synapses=args.batch_wave_synapses)
+    return {"metric": METRIC, "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic", **out}
 
 
 def serving_jobs(args):
@@ -421,26 +715,48 @@ def run_serving(args):
     }
 
 
+def side_leg(lib, args, stream):
+    """stdp_100k beside the headline: 10 timed steps of 400 ticks after the
+    headline's warm-up count, plus its per-kernel profile."""
+    from snncuda_gb300 import synthetic
+    w1, tps1, steps1 = synthetic.STDP_100K, 400, 10
+    total1 = (args.warmup + steps1) * tps1
+    net1 = synthetic.build_network(w1)
+    d1 = synthetic.build_drive(w1, total1 + args.profile_ticks)
+    r1 = timed_leg(lib, w1, net1, d1, total1, tps1, args.warmup, steps1, stream, clocks=False,
+                   profile_ticks=args.profile_ticks)
+    ticks1 = steps1 * tps1
+    return {"value": r1["events"] / (r1["ms"] / 1e3), "unit": UNIT, "ticks_per_s": ticks1 / (r1["ms"] / 1e3),
+            "ms_per_step": r1["ms"] / steps1, "steps": steps1, "ticks_per_step": tps1,
+            "events_per_tick": r1["events"] / ticks1, "fires_per_tick": r1["fires"] / ticks1,
+            "config": config_block(args, w1, tps1),
+            "tick_roofline": tick_roofline(w1, r1["events"], r1["fires"], r1["ext"], r1["prof"], ticks1, r1["ms"]),
+            "roofline": kernel_roofline(w1, r1["prof"], True) if r1["prof"] else None}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
-    ap.add_argument("--workload", default="stdp_100k")
-    ap.add_argument("--ticks-per-step", type=int, default=400)
+    ap.add_argument("--workload", default="recog_1m")
+    ap.add_argument("--ticks-per-step", type=int, default=0, help="0: 80 for recog_1m, 400 otherwise")
     ap.add_argument("--weight-scale", type=float, default=None)
     ap.add_argument("--neurons", type=int, default=None, help="smaller case of the workload (profiling)")
     ap.add_argument("--fanout", type=int, default=None)
-    ap.add_argument("--profile-ticks", type=int, default=200)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--profile-ticks", type=int, default=100)
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the parity legs and the CPU baseline")
+    ap.add_argument("--no-side", action="store_true", help="skip the stdp_100k leg beside the headline")
     ap.add_argument("--slot-capacity", type=int, default=0, help="events one wheel slot holds (0 = default)")
     ap.add_argument("--batched", type=int, default=0,
                     help="batched form: this many networks in one handle vs one handle per network")
-    ap.add_argument("--batch-ticks", type=int, default=500)
-    ap.add_argument("--batch-neurons", type=str, default="1000,20000", help="log-uniform range of N")
+    ap.add_argument("--batch-ticks", type=int, default=2000)
+    ap.add_argument("--batch-neurons", type=str, default="1000,200000", help="log-uniform range of N")
+    ap.add_argument("--batch-wave-synapses", type=float, default=1.2e9, help="synapses per wave of the batch")
+    ap.add_argument("--batch-networks", type=int, default=64,
+                    help="networks of the batched leg of the default run (0 skips it)")
     ap.add_argument("--rmw-floor", action="store_true",
                     help="time random 64-byte record read-modify-writes (the per-event access floor)")
     ap.add_argument("--serve", action="store_true", help="serving: Poisson arrivals under a memory budget")
@@ -473,7 +789,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     w = workload_from_args(args)
-    total_ticks = (args.warmup + args.steps) * args.ticks_per_step
+    tps = ticks_per_step(args, w)
+    total_ticks = (args.warmup + args.steps) * tps
     if total_ticks > w.ticks:
         w = w.scaled(ticks=total_ticks)
 
@@ -499,132 +816,60 @@ def main():
     if world > 1:
         dist.barrier()
     from snncuda_gb300 import synthetic
-    from snncuda_gb300.simulation import Simulation, backend
+    from snncuda_gb300.simulation import backend
 
     lib = backend()
-    net = synthetic.build_network(w)
-    profile_end = total_ticks + args.profile_ticks
-    drive_all = synthetic.build_drive(w, profile_end)
-    dn, dt, dw = drive_all
-    main_mask = dt < total_ticks
-    drive = (dn[main_mask], dt[main_mask], dw[main_mask])
     stream = torch.cuda.Stream(device=dev)
+    full_size = args.neurons is None and args.fanout is None
+    dist_or_none = dist if world > 1 else None
 
-    # ---- device-resident timing --------------------------------------------
-    sim = Simulation(net, sim_config(lib, w, cuda_stream=stream.cuda_stream), lib)
-    sim.inject(*drive)
-    tps = args.ticks_per_step
-    tick = 0
-    for _ in range(args.warmup):
-        tick += tps
-        sim.run_until(tick - 1)
-    c0 = sim.counters()
-    sampler = ClockSampler(local)
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    sampler.start()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    for _ in range(args.steps):
-        tick += tps
-        sim.run_until(tick - 1)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    clocks = sampler.stop()
-    if world > 1:
-        dist.barrier()
-    c1 = sim.counters()
-    # recognition workloads: the sums the reference's recognition metric adds up
-    recognition = sim.recognition() if w.stimulus_codes else None
-    ms = ev0.elapsed_time(ev1)
-    events = c1["synaptic_events"] - c0["synaptic_events"]
-    ext_events = c1["external_events"] - c0["external_events"]
-    fires = c1["fired_spikes"] - c0["fired_spikes"]
-    ms_max, events_all = combine_ranks(ms, events, world, dist if world > 1 else None, dev)
+    # ---- headline workload: device-resident timing and per-kernel profile --
+    net = synthetic.build_network(w)
+    drive_all = synthetic.build_drive(w, total_ticks + args.profile_ticks)
+    main_mask = drive_all[1] < total_ticks
+    drive = tuple(a[main_mask] for a in drive_all)
+    r = timed_leg(lib, w, net, drive_all, total_ticks, tps, args.warmup, args.steps, stream, dist_or_none, local,
+                  profile_ticks=args.profile_ticks)
+    ms_max, events_all = combine_ranks(r["ms"], r["events"], world, dist_or_none, dev)
     value = events_all / (ms_max / 1e3)
-
-    # ---- per-kernel profile for the roofline -------------------------------
-    roofline = None
-    prof = None
-    if args.profile_ticks > 0:
-        extra = ~main_mask
-        sim.inject(dn[extra], dt[extra], dw[extra])
-        prof = sim.profile(profile_end - 1)
-        km = prof["kernel_ms"]
-        top = max(km, key=km.get)
-        launches = prof["ticks"]
-        peak, peak_kind = load_peaks()
-        if top in BYTES_MODEL:
-            per_syn, per_ext, per_tgt = BYTES_MODEL[top]
-            algo = (per_syn * prof["synaptic_events"] + per_ext * prof["external_events"] +
-                    per_tgt * prof["touched_targets"]) / launches
-        else:
-            algo = None
-        avg_ms = km[top] / launches
-        achieved = algo / (avg_ms / 1e3) / 1e9 if algo else None
-        roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                    "frac": (achieved / peak) if achieved else None,
-                    "traffic": MEASURED_TRAFFIC.get((w.name, top)) if args.neurons is None and args.fanout is None
-                    else None,
-                    "peak_source": peak_kind, "avg_launch_us": avg_ms * 1e3,
-                    "algorithmic_bytes_per_launch": algo,
-                    "kernel_share": {k: v / sum(km.values()) for k, v in km.items()}}
-    sim.close()
-    del sim
+    prof = r["prof"]
+    roofline = kernel_roofline(w, prof, full_size) if prof else None
 
     # ---- end to end through the public API ---------------------------------
     e2e = None
     if not args.no_e2e:
-        pin = lambda a, dt_: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
-        pn, pt, pw = pin(drive[0], np.uint32), pin(drive[1], np.uint64), pin(drive[2], np.float32)
-        bounds = np.searchsorted(pt, np.arange(0, total_ticks + tps, tps))
-        sim2 = Simulation(net, sim_config(lib, w, cuda_stream=stream.cuda_stream,
-                                          raster_capacity=1 << 26), lib)
-        h2d = d2h = 0
-        raster_pos = 0
-        tick = 0
-        start = None
-        for step in range(args.warmup + args.steps):
-            if step == args.warmup:
-                torch.cuda.synchronize()
-                h2d = d2h = 0
-                start = time.perf_counter()
-                cs = sim2.counters()
-            a, b = bounds[step], bounds[step + 1]
-            sim2.inject(pn[a:b], pt[a:b], pw[a:b])
-            h2d += (b - a) * 16
-            tick += tps
-            sim2.run_until(tick - 1)
-            c = sim2.counters()
-            new = c["raster_count"] - raster_pos
-            sim2.raster(raster_pos, new)
-            d2h += new * 8 + 64
-            raster_pos = c["raster_count"]
-        elapsed = time.perf_counter() - start
-        ce = sim2.counters()
-        sim2.close()
-        e2e_events = ce["synaptic_events"] - cs["synaptic_events"]
-        e2e = {"value": e2e_events / elapsed, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
-               "d2h_bytes_per_step": int(d2h / args.steps)}
+        e2e = e2e_leg(lib, w, net, drive, total_ticks, tps, args.warmup, args.steps, stream)
+    del net, drive, drive_all
 
-    cpu = None
+    # ---- stdp_100k beside the headline, the batched form, parity and the
+    # CPU baseline ------------------------------------------------------------
+    side = batched = parity = cpu = None
+    if rank == 0 and not args.no_side and w.name != "stdp_100k":
+        side = side_leg(lib, args, stream)
+    if rank == 0 and args.batch_networks > 0 and full_size:
+        nmin, nmax = (int(x) for x in args.batch_neurons.split(","))
+        batched = batched_leg(lib, args.batch_networks, nmin, nmax, args.batch_ticks, stream,
+                              wave_synapses=args.batch_wave_synapses)
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_sample(w, net, drive_all, budget_s=args.cpu_seconds)
+        parity, cpu = parity_legs(lib)
 
     if rank == 0:
+        steps_ticks = args.steps * tps
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config_block(args, w),
-            "ticks_per_s": args.steps * tps / (ms_max / 1e3),
-            "fires_per_tick": fires / (args.steps * tps),
-            "events_per_tick": events / (args.steps * tps),
-            "gpu_launches": args.steps * tps * KERNELS_PER_TICK,
-            "tick_roofline": tick_roofline(w, events, fires, ext_events, prof, args.steps * tps, ms_max),
-            "clocks": clocks, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-            **({"recognition": recognition} if recognition is not None else {}),
+            "config": config_block(args, w, tps),
+            "ticks_per_s": steps_ticks / (ms_max / 1e3),
+            "fires_per_tick": r["fires"] / steps_ticks,
+            "events_per_tick": r["events"] / steps_ticks,
+            "gpu_launches": steps_ticks * KERNELS_PER_TICK,
+            "tick_roofline": tick_roofline(w, r["events"], r["fires"], r["ext"], prof, steps_ticks, ms_max),
+            "clocks": r["clocks"], "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            **({"recognition": r["recognition"]} if r["recognition"] is not None else {}),
+            "parity": parity,
+            **({"stdp_100k": side} if side is not None else {}),
+            **({"batched": batched} if batched is not None else {}),
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -218,10 +218,68 @@ int snncuda_sim_read_pattern(snncuda_sim* sim, int32_t kind, uint64_t index, uin
  * digest_synapses); equal digests mean bit-identical state. */
 int snncuda_sim_state_digest(snncuda_sim* sim, uint64_t* neuron_digest, uint64_t* synapse_digest);
 
+/* Engine extension: order-independent 64-bit checksums of the neuron records
+ * and of the synapse records (target-major, Connectome order inside each
+ * target), computed on the device without copying the state back.  Equal
+ * checksums of two runs of the same network mean equal state up to hash
+ * collisions; they are comparable between a batch member
+ * (snncuda_batch_state_checksums) and its solo run, not between
+ * implementations (use snncuda_sim_state_digest for that).  CPU
+ * implementations return SNNCUDA_ERR_UNSUPPORTED. */
+int snncuda_sim_state_checksum(snncuda_sim* sim, uint64_t* neuron_sum, uint64_t* synapse_sum);
+
 /* Fire records in processing order: (tick, neuron).  Requires
  * config.raster_capacity > 0. */
 int snncuda_sim_read_raster(snncuda_sim* sim, uint64_t first, uint64_t count, uint64_t* ticks,
                             uint32_t* neurons);
+
+/* ---- autotuning (engine extension) ----------------------------------------
+ * No counterpart in the reference, whose CUDA backend launches fixed shapes
+ * (CudaBackend.cu).  snncuda_sim_autotune runs the simulation's next ticks
+ * in timed probes of probe_ticks ticks (each probe first runs up to one
+ * captured graph of ticks untimed) and keeps, per knob, the fastest of a few
+ * candidates: blocks of the synapse-event kernel (events per warp), of the
+ * per-target walk, of the grouping and of the temporal update, and the ticks
+ * per captured graph; then it shrinks the wheel-slot capacity to twice the
+ * largest per-tick due list seen plus 2^16 events when that saves a quarter
+ * or more of it.  The probed ticks are ordinary ticks of the simulation and
+ * launch shapes never change results.  Threads per block stay 256: the
+ * kernels' shared-memory layouts are built for it, and blocks per SM (the
+ * knobs above) are the occupancy lever. */
+typedef struct snncuda_tuning {
+    uint32_t grid_events, grid_walk, grid_bucket, grid_temporal;  /* blocks */
+    uint32_t ticks_per_graph;
+    uint32_t block_threads;
+    uint64_t slot_event_capacity;   /* after tuning */
+    uint64_t max_slot_events;       /* largest due list seen so far */
+    double ms_per_tick_before;      /* first probe */
+    double ms_per_tick_after;       /* last probe, with the chosen shapes */
+    uint32_t probes;
+    uint64_t probe_ticks;
+} snncuda_tuning;
+int snncuda_sim_autotune(snncuda_sim* sim, uint64_t probe_ticks, snncuda_tuning* out);
+/* Sets the wheel-slot capacity (rounded up to a multiple of 32); fails with
+ * SNNCUDA_ERR_INVALID_ARGUMENT if a slot already holds more events. */
+int snncuda_sim_set_slot_capacity(snncuda_sim* sim, uint64_t capacity);
+
+/* ---- eviction: a simulation's device state to host memory and back ------
+ * Replaces, for a whole simulation, the reference's write-back of evicted
+ * neuron states to its NeuronStateStore and their reload on the next access
+ * (NeuronStateCache.cpp:22-43, LruCache.h:44-63): the reference pages single
+ * neuron states through an LRU cache; here the state stays resident on the
+ * device and a simulation whose device memory is needed elsewhere (a
+ * server's budget) is evicted as a whole.
+ * snncuda_sim_evict waits for the simulation's work, copies its state (neuron
+ * and synapse records, temporal patterns, the wheel's queued events, counters,
+ * the raster) to host memory and frees its device memory.
+ * snncuda_sim_restore allocates it again and copies the state back; every
+ * call that needs the device state (run_until, readers, toggles) restores an
+ * evicted simulation first.  Results are identical to never evicting.
+ * snncuda_sim_residency reports whether the state is on the device and how
+ * many times it was evicted. */
+int snncuda_sim_evict(snncuda_sim* sim);
+int snncuda_sim_restore(snncuda_sim* sim);
+int snncuda_sim_residency(snncuda_sim* sim, int32_t* resident, uint64_t* evictions);
 
 /* ---- batched form: many independent networks in one handle --------------
  * The reference runs one NetworkPropagator per network, one after the other
@@ -247,6 +305,10 @@ int snncuda_batch_read_neurons(snncuda_batch* batch, uint32_t network, const snn
 int snncuda_batch_read_synapses(snncuda_batch* batch, uint32_t network, const snncuda_synapse_state* out);
 /* Digests of every network (arrays of `count`), as snncuda_sim_state_digest. */
 int snncuda_batch_state_digests(snncuda_batch* batch, uint64_t* neuron_digests, uint64_t* synapse_digests);
+/* snncuda_sim_autotune on the batch's one tick loop. */
+int snncuda_batch_autotune(snncuda_batch* batch, uint64_t probe_ticks, snncuda_tuning* out);
+/* Checksums of every network (arrays of `count`), as snncuda_sim_state_checksum. */
+int snncuda_batch_state_checksums(snncuda_batch* batch, uint64_t* neuron_sums, uint64_t* synapse_sums);
 /* Network's fire records [first, first + count) in its own processing order. */
 int snncuda_batch_read_raster(snncuda_batch* batch, uint32_t network, uint64_t first, uint64_t count,
                               uint64_t* ticks, uint32_t* neurons);
@@ -268,6 +330,11 @@ typedef struct snncuda_server_config {
     uint32_t max_running;          /* jobs advanced side by side (0 = 64) */
     uint32_t slice_ticks;          /* ticks per job and scheduling round (0 = 64) */
     int32_t digests;               /* compute state digests of finished jobs */
+    int32_t evict;                 /* 1: a queued job that does not fit the budget
+                                      preempts running jobs with more remaining
+                                      work (synapses x ticks left), which are
+                                      evicted to host memory (snncuda_sim_evict)
+                                      and resume when the budget has room */
 } snncuda_server_config;
 int snncuda_server_create(const snncuda_server_config* config, snncuda_server** out);
 int snncuda_server_destroy(snncuda_server* server);
@@ -282,12 +349,14 @@ int snncuda_server_submit(snncuda_server* server, const snncuda_network* network
  * while they fit.  *active = jobs queued or running afterwards. */
 int snncuda_server_step(snncuda_server* server, uint32_t* active);
 typedef struct snncuda_job_result {
-    int32_t state;                 /* 0 queued, 1 running, 2 done, 3 failed */
+    int32_t state;                 /* 0 queued, 1 running, 2 done, 3 failed,
+                                      4 evicted (waiting in host memory) */
     int32_t error;                 /* SNNCUDA_ERR_* of a failed job */
     snncuda_counters counters;     /* of a finished job */
     uint64_t neuron_digest, synapse_digest;  /* when config.digests */
     uint64_t device_bytes;         /* the admission estimate */
     double submitted_s, admitted_s, finished_s;  /* seconds since server creation */
+    uint64_t evictions;            /* times the job was evicted to host memory */
 } snncuda_job_result;
 int snncuda_server_job(snncuda_server* server, uint64_t job_id, snncuda_job_result* out);
 /* Device bytes a simulation of `network` under `config` holds at most
@@ -317,6 +386,53 @@ int snncuda_sim_profile(snncuda_sim* sim, uint64_t inclusive_tick, snncuda_profi
  * synapse state). */
 int snncuda_sim_recognition(snncuda_sim* sim, uint64_t* neuron_matches, uint64_t* synapse_code_matches);
 const char* snncuda_kernel_name(int32_t index);
+
+/* ---- inference readouts -------------------------------------------------
+ * Replace the reference inference session's readout paths
+ * (CudaInferenceSession::run_feedforward_batch and
+ * run_recurrent_feedforward_batch, CudaBackend.h:115-121,
+ * CudaBackend.cu:1725-2100) over a network's initial weights.  Samples are
+ * CSR: sample s's inputs are input_neurons / input_weights
+ * [input_ptr[s], input_ptr[s+1]); a sample's inputs to one neuron are summed
+ * first (in input order) and delivered[s] receives the number of distinct
+ * input neurons.  scores and spikes are [samples][readout_count]: spikes
+ * are 1 where the score reaches the readout neuron's threshold.  Every sum
+ * is formed in a fixed order (a neuron's incoming synapses in Connectome
+ * order, time steps in order) where the reference adds with float atomics in
+ * an unspecified order.  A neuron listed twice among the readouts or among
+ * the hidden neurons is rejected (SNNCUDA_ERR_INVALID_ARGUMENT). */
+typedef struct snncuda_readout snncuda_readout;
+int snncuda_readout_create(const snncuda_network* network, snncuda_readout** out);
+int snncuda_readout_destroy(snncuda_readout* readout);
+/* One hop: score = sum over the readout's incoming synapses whose source is
+ * an input of input weight x synapse weight. */
+int snncuda_readout_feedforward(snncuda_readout* readout, uint32_t samples, const uint64_t* input_ptr,
+                                const uint32_t* input_neurons, const float* input_weights, uint32_t readout_count,
+                                const uint32_t* readout_neurons, float* scores, uint64_t* spikes,
+                                uint64_t* delivered);
+/* CudaRecurrentFeedforwardOptions (CudaBackend.h:69-79) without the
+ * full-spike-timing switch (that mode is the tick simulation itself). */
+typedef struct snncuda_recurrent_options {
+    uint32_t iterations;              /* 1 */
+    float feedback_decay;             /* 0.5 */
+    uint32_t top_k_feedback_readouts; /* 1; 0 = every readout at or above its threshold */
+    uint32_t top_k_hidden;            /* 0 = no hidden selection */
+    int32_t use_scores_not_spikes;    /* 1: gates carry the readout score, 0: 1 */
+} snncuda_recurrent_options;
+void snncuda_recurrent_options_default(snncuda_recurrent_options* options);
+/* max_delay x (1 + 2 x iterations) + 1 time steps (*time_steps): the inputs
+ * that are hidden neurons start as hidden events at step 0; each step keeps
+ * the top_k_hidden largest hidden events (when 0 < top_k_hidden <
+ * hidden_count), sends hidden events to the readouts (a synapse of delay d,
+ * at least 1, lands d steps later), gates the readouts of the step and feeds
+ * the gated readouts back to the hidden neurons scaled by feedback_decay;
+ * scores are the readout events summed over the steps.  hidden_count 0 =
+ * every neuron that is not a readout, in index order. */
+int snncuda_readout_recurrent(snncuda_readout* readout, uint32_t samples, const uint64_t* input_ptr,
+                              const uint32_t* input_neurons, const float* input_weights, uint32_t readout_count,
+                              const uint32_t* readout_neurons, uint32_t hidden_count, const uint32_t* hidden_neurons,
+                              const snncuda_recurrent_options* options, float* scores, uint64_t* spikes,
+                              uint64_t* delivered, uint64_t* time_steps);
 
 /* ---- building block: group a tick's due events by target ----------------
  * Replaces, for one tick, the due list SpikeScheduler::pop_due returns
@@ -348,7 +464,7 @@ int snncuda_group_events(const uint64_t* events, uint32_t count, uint32_t neuron
  * Same arguments and results as snncuda_group_events; the caller still
  * provides the inputs and outputs, but the scratch (per-neuron counters,
  * scan tiles, the unsorted groups) lives in one static device array compiled
- * into the library (about 15 MB, held on every GPU that loads the library
+ * into the library (about 11 MB, held on every GPU that loads the library
  * until the process exits).  Limits: count <= SNNCUDA_GROUP_STATIC_MAX_EVENTS
  * and neuron_count <= SNNCUDA_GROUP_STATIC_MAX_NEURONS, otherwise
  * SNNCUDA_ERR_CAPACITY.  The first call on a device looks up the array's

@@ -2,7 +2,8 @@
  * snncuda_gb300.hpp -- header-only C++ facade over the C ABI with the
  * reference's backend names (snncuda/backends/CudaBackend.h): CudaBackend::
  * run_resident_propagation -> CudaPropagationResult / CudaDebugMetrics, and
- * CudaInferenceSession::run_batch.  It takes any Connectome-shaped object
+ * CudaInferenceSession::run_batch / run_feedforward_batch /
+ * run_recurrent_feedforward_batch / reset_state.  It takes any Connectome-shaped object
  * with the reference's public fields (declarative/Connectome.h:13-37:
  * neurons[i].id / .params.{threshold, pattern_window_ticks,
  * similarity_threshold, max_reference_patterns}, synapses[k].{source, target,
@@ -20,6 +21,7 @@
  */
 #pragma once
 
+#include <algorithm>
 #include <chrono>
 #include <cstdint>
 #include <stdexcept>
@@ -87,6 +89,19 @@ struct CudaInferenceOptions {
     std::uint32_t max_steps{8};
     bool reset_state_between_samples{true};
     std::vector<std::uint64_t> readout_neurons;
+};
+
+// CudaRecurrentFeedforwardOptions (CudaBackend.h:69-79).
+struct CudaRecurrentFeedforwardOptions {
+    std::uint32_t iterations{1};
+    std::vector<std::uint64_t> readout_neurons;
+    std::vector<std::uint64_t> hidden_neurons;
+    float feedback_decay{0.5F};
+    std::uint32_t top_k_feedback_readouts{1};
+    std::uint32_t top_k_hidden{0};
+    bool use_scores_not_spikes{true};
+    bool use_full_spike_timing{false};
+    std::uint32_t max_timing_steps{0};
 };
 
 struct CudaInferenceSampleResult {
@@ -257,7 +272,10 @@ template <class Connectome>
 class CudaInferenceSession {
 public:
     explicit CudaInferenceSession(const Connectome& connectome) : flat_(connectome) {}
-    ~CudaInferenceSession() { reset_state(); }
+    ~CudaInferenceSession() {
+        reset_state();
+        if (readout_) snncuda_readout_destroy(readout_);
+    }
     CudaInferenceSession(const CudaInferenceSession&) = delete;
     CudaInferenceSession& operator=(const CudaInferenceSession&) = delete;
 
@@ -279,6 +297,72 @@ public:
         return out;
     }
 
+    // run_feedforward_batch (CudaBackend.cu:1725-1849): one hop from the
+    // samples' inputs to the readouts over the initial weights; scores are
+    // the weighted sums, spike counts 1 where a score reaches its readout's
+    // threshold.
+    CudaInferenceBatchResult run_feedforward_batch(const std::vector<CudaInferenceSample>& samples,
+                                                   const CudaInferenceOptions& options) {
+        CudaInferenceBatchResult out;
+        out.executed = true;
+        const auto t0 = std::chrono::steady_clock::now();
+        std::vector<std::uint32_t> readout = dense_list(options.readout_neurons);
+        Inputs in(flat_, samples);
+        const std::size_t S = samples.size(), R = readout.size();
+        std::vector<float> scores(S * R);
+        std::vector<std::uint64_t> spikes(S * R), delivered(S);
+        detail::check(snncuda_readout_feedforward(readout_handle(), static_cast<std::uint32_t>(S), in.ptr.data(),
+                                                  in.n.data(), in.w.data(), static_cast<std::uint32_t>(R),
+                                                  readout.data(), scores.data(), spikes.data(), delivered.data()));
+        readout_results(scores, spikes, delivered, R, 0, out);
+        out.elapsed_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return out;
+    }
+
+    // run_recurrent_feedforward_batch (CudaBackend.cu:1851-2100): hidden and
+    // readout events exchanged over max_delay x (1 + 2 x iterations) + 1 time
+    // steps; with use_full_spike_timing the samples run through the tick
+    // simulation instead (run_batch with that many ticks, or max_timing_steps).
+    CudaInferenceBatchResult run_recurrent_feedforward_batch(const std::vector<CudaInferenceSample>& samples,
+                                                             const CudaRecurrentFeedforwardOptions& options) {
+        if (options.use_full_spike_timing) {
+            CudaInferenceOptions timing;
+            std::uint32_t max_delay = 1;
+            for (std::uint32_t d : flat_.dly) max_delay = std::max(max_delay, std::max(1u, d));
+            timing.max_steps = options.max_timing_steps != 0
+                                   ? options.max_timing_steps
+                                   : max_delay * (1u + 2u * options.iterations) + 1u;
+            timing.reset_state_between_samples = true;
+            timing.readout_neurons = options.readout_neurons;
+            return run_batch(samples, timing);
+        }
+        CudaInferenceBatchResult out;
+        out.executed = true;
+        const auto t0 = std::chrono::steady_clock::now();
+        std::vector<std::uint32_t> readout = dense_list(options.readout_neurons);
+        std::vector<std::uint32_t> hidden = dense_list(options.hidden_neurons);
+        Inputs in(flat_, samples);
+        const std::size_t S = samples.size(), R = readout.size();
+        std::vector<float> scores(S * R);
+        std::vector<std::uint64_t> spikes(S * R), delivered(S);
+        snncuda_recurrent_options o;
+        snncuda_recurrent_options_default(&o);
+        o.iterations = options.iterations;
+        o.feedback_decay = options.feedback_decay;
+        o.top_k_feedback_readouts = options.top_k_feedback_readouts;
+        o.top_k_hidden = options.top_k_hidden;
+        o.use_scores_not_spikes = options.use_scores_not_spikes ? 1 : 0;
+        std::uint64_t steps = 0;
+        detail::check(snncuda_readout_recurrent(readout_handle(), static_cast<std::uint32_t>(S), in.ptr.data(),
+                                                in.n.data(), in.w.data(), static_cast<std::uint32_t>(R),
+                                                readout.data(), static_cast<std::uint32_t>(hidden.size()),
+                                                hidden.data(), &o, scores.data(), spikes.data(), delivered.data(),
+                                                &steps));
+        readout_results(scores, spikes, delivered, R, steps, out);
+        out.elapsed_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return out;
+    }
+
     void reset_state() {
         if (sim_) snncuda_sim_destroy(sim_);
         sim_ = nullptr;
@@ -286,6 +370,61 @@ public:
     }
 
 private:
+    // A batch's inputs as the readout entry points take them (unknown neuron
+    // ids are skipped, as the reference does).
+    struct Inputs {
+        std::vector<std::uint64_t> ptr{0};
+        std::vector<std::uint32_t> n;
+        std::vector<float> w;
+        Inputs(const detail::Flat& f, const std::vector<CudaInferenceSample>& samples) {
+            for (const auto& s : samples) {
+                for (const auto& in : s.inputs) {
+                    const auto it = f.index.find(in.neuron);
+                    if (it == f.index.end()) continue;
+                    n.push_back(it->second);
+                    w.push_back(in.weight);
+                }
+                ptr.push_back(n.size());
+            }
+            if (n.empty()) {
+                n.push_back(0);
+                w.push_back(0.0F);
+            }
+        }
+    };
+
+    std::vector<std::uint32_t> dense_list(const std::vector<std::uint64_t>& ids) const {
+        std::vector<std::uint32_t> out;
+        for (std::uint64_t id : ids) {
+            const auto it = flat_.index.find(id);
+            if (it != flat_.index.end()) out.push_back(it->second);
+        }
+        return out;
+    }
+
+    snncuda_readout* readout_handle() {
+        if (!readout_) detail::check(snncuda_readout_create(&flat_.net, &readout_));
+        return readout_;
+    }
+
+    static void readout_results(const std::vector<float>& scores, const std::vector<std::uint64_t>& spikes,
+                                const std::vector<std::uint64_t>& delivered, std::size_t R, std::uint64_t steps,
+                                CudaInferenceBatchResult& out) {
+        for (std::size_t s = 0; s < delivered.size(); ++s) {
+            CudaInferenceSampleResult r;
+            for (std::size_t k = 0; k < R; ++k) {
+                r.readout_scores.push_back(scores[s * R + k]);
+                r.readout_spike_counts.push_back(spikes[s * R + k]);
+                r.fired_spikes += spikes[s * R + k];
+            }
+            r.delivered_spikes = delivered[s];
+            r.debug.ticks_processed = steps;
+            r.debug.processed_events = delivered[s];
+            r.debug.dendritic_integrations = delivered[s];
+            out.samples.push_back(std::move(r));
+        }
+    }
+
     static void inputs_of(const detail::Flat& f, const CudaInferenceSample& s, std::uint64_t base,
                           std::vector<std::uint32_t>& n, std::vector<std::uint64_t>& t, std::vector<float>& w) {
         n.clear();
@@ -378,6 +517,7 @@ private:
 
     detail::Flat flat_;
     snncuda_sim* sim_{nullptr};
+    snncuda_readout* readout_{nullptr};
     std::uint64_t base_tick_{0};
 };
 

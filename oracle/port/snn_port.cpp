@@ -715,3 +715,4 @@ int snncuda_group_events_static(const uint64_t* events, uint32_t count, uint32_t
 
 
 #include "../batch_of_sims.inc"
+#include "../readout_port.inc"

@@ -9,6 +9,7 @@ from .connectome import (AMPA, APICAL, BASAL, GABA_A, GABA_B, INHIBITORY, NMDA, 
                          ExplicitConnection, NetworkBuilder, NeuronParams, Projection)
 from .simulation import (BACKEND_LIBRARY, Batch, NetworkPropagator, SNNCudaError, Server, Simulation, backend,
                          default_config)
+from .declarative import load as load_network
 
 
 def version() -> str:
@@ -25,5 +26,5 @@ __all__ = [
     "AMPA", "APICAL", "BASAL", "GABA_A", "GABA_B", "INHIBITORY", "NMDA", "SOMA", "Connectome",
     "ExplicitConnection", "NetworkBuilder", "NeuronParams", "Projection", "BACKEND_LIBRARY",
     "Batch", "NetworkPropagator", "SNNCudaError", "Server", "Simulation", "backend", "default_config", "version",
-    "cuda_available",
+    "cuda_available", "load_network",
 ]

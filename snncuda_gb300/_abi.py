@@ -80,12 +80,30 @@ class Counters(Structure):
     ]
 
 
+class Tuning(Structure):
+    _fields_ = [
+        ("grid_events", c_uint32), ("grid_walk", c_uint32), ("grid_bucket", c_uint32),
+        ("grid_temporal", c_uint32), ("ticks_per_graph", c_uint32), ("block_threads", c_uint32),
+        ("slot_event_capacity", c_uint64), ("max_slot_events", c_uint64),
+        ("ms_per_tick_before", ctypes.c_double), ("ms_per_tick_after", ctypes.c_double),
+        ("probes", c_uint32), ("probe_ticks", c_uint64),
+    ]
+
+
+class RecurrentOptions(Structure):
+    _fields_ = [
+        ("iterations", c_uint32), ("feedback_decay", c_float), ("top_k_feedback_readouts", c_uint32),
+        ("top_k_hidden", c_uint32), ("use_scores_not_spikes", c_int32),
+    ]
+
+
 class ServerConfig(Structure):
     _fields_ = [
         ("memory_budget_bytes", c_uint64),
         ("max_running", c_uint32),
         ("slice_ticks", c_uint32),
         ("digests", c_int32),
+        ("evict", c_int32),
     ]
 
 
@@ -100,6 +118,7 @@ class JobResult(Structure):
         ("submitted_s", ctypes.c_double),
         ("admitted_s", ctypes.c_double),
         ("finished_s", ctypes.c_double),
+        ("evictions", c_uint64),
     ]
 
 
@@ -195,6 +214,24 @@ _SIGNATURES = {
     "snncuda_server_step": (c_int, [c_void_p, POINTER(c_uint32)]),
     "snncuda_server_job": (c_int, [c_void_p, c_uint64, POINTER(JobResult)]),
     "snncuda_sim_estimate_bytes": (c_int, [POINTER(Network), POINTER(Config), POINTER(c_uint64)]),
+    "snncuda_sim_state_checksum": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64)]),
+    "snncuda_batch_state_checksums": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64)]),
+    "snncuda_sim_autotune": (c_int, [c_void_p, c_uint64, POINTER(Tuning)]),
+    "snncuda_batch_autotune": (c_int, [c_void_p, c_uint64, POINTER(Tuning)]),
+    "snncuda_sim_set_slot_capacity": (c_int, [c_void_p, c_uint64]),
+    "snncuda_readout_create": (c_int, [POINTER(Network), POINTER(c_void_p)]),
+    "snncuda_readout_destroy": (c_int, [c_void_p]),
+    "snncuda_readout_feedforward": (c_int, [c_void_p, c_uint32, POINTER(c_uint64), POINTER(c_uint32),
+                                            POINTER(c_float), c_uint32, POINTER(c_uint32), POINTER(c_float),
+                                            POINTER(c_uint64), POINTER(c_uint64)]),
+    "snncuda_recurrent_options_default": (None, [POINTER(RecurrentOptions)]),
+    "snncuda_readout_recurrent": (c_int, [c_void_p, c_uint32, POINTER(c_uint64), POINTER(c_uint32),
+                                          POINTER(c_float), c_uint32, POINTER(c_uint32), c_uint32,
+                                          POINTER(c_uint32), POINTER(RecurrentOptions), POINTER(c_float),
+                                          POINTER(c_uint64), POINTER(c_uint64), POINTER(c_uint64)]),
+    "snncuda_sim_evict": (c_int, [c_void_p]),
+    "snncuda_sim_restore": (c_int, [c_void_p]),
+    "snncuda_sim_residency": (c_int, [c_void_p, POINTER(c_int32), POINTER(c_uint64)]),
     "snncuda_group_events": (c_int, [c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]),
     "snncuda_group_events_static": (c_int, [c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]),
 }

@@ -215,17 +215,22 @@ struct Engine {
     unsigned long long* wheel;             // [W * slot_cap]
     uint32_t* slot_count;                  // [W]
 
-    // per-tick scratch
-    uint32_t* cnt;                         // [N] due events per target (zero between ticks)
-    uint32_t* seg_start;                   // [N]
-    uint32_t* tile_sum;                    // scan partials
-    uint32_t* tile_nz;
-    uint32_t* touched;                     // [N] target ids with due events, ascending
-    uint32_t* tbeg;                        // [N] group start of the k-th touched target (tick only)
-    unsigned long long* grp;               // [slot_cap] (payload << 32) | (due index | ext << 31)
-    unsigned long long* grp_sorted;        // grouping entry point only: grp with every group in due order
-    uint32_t* evt_tgt;                     // grouping entry point only: target of each grp_sorted entry
-    uint32_t* seg_len;                     // grouping entry point only: due events of each touched target
+    // per-tick scratch: grouping by target.  Targets are bucketed by
+    // bucket_shift (2^bucket_shift consecutive targets per bucket, at most
+    // kMaxBuckets buckets); grid_bucket blocks each count and place one
+    // contiguous chunk of the due list.
+    uint32_t bucket_shift;
+    uint32_t nbuckets;
+    uint32_t grid_bucket;
+    uint32_t* bcnt;                        // [grid_bucket][nbuckets] events of each (chunk, bucket)
+    uint32_t* btot;                        // [nbuckets] events per bucket (zero between ticks)
+    uint32_t* bstart;                      // [nbuckets + 1] first grouped position of each bucket
+    uint32_t* bcur;                        // [nbuckets] placement cursor of each bucket
+    uint32_t* seg_start;                   // [N + 1] first grouped position of each target
+    unsigned long long* grp;               // [slot_cap] due events grouped by target, due order inside
+                                           // a target: (payload << 32) | (due index | ext << 31)
+    unsigned long long* grp_tmp;           // [slot_cap] the due events in bucket order (unsorted inside)
+    uint16_t* grp_ltgt;                    // [slot_cap] target of each grp_tmp entry within its bucket
     EvIn* evin;                            // [slot_cap] per-event inputs of k_process, grouped, due order
     SynA* ev_a0;                           // [slot_cap] each synaptic event's SynA before the event
     uint32_t* fire_bits;                   // [slot_cap/32] bitmap of due positions that fired
@@ -246,14 +251,25 @@ struct Engine {
     TickState* ts;
     Tables tab;
 
-    // launch shapes
+    // launch shapes (results do not depend on them; snncuda_sim_autotune
+    // picks grid_events, grid_walk, grid_bucket and grid_process)
     uint32_t grid_wide;
-    uint32_t grid_process;
-    uint32_t grid_walk;  // k_process blocks
+    uint32_t grid_process;  // k_temporal blocks
+    uint32_t grid_walk;     // k_process blocks
     uint32_t grid_fire;
+    uint32_t grid_events;   // k_events blocks
 };
 
-constexpr int kScanTile = 1024;          // entries per scan tile (256 threads x 4)
+constexpr uint32_t kMaxBuckets = 16384;   // target buckets of the grouping (shared-memory counters)
+constexpr uint32_t kMaxBucketShift = 14;  // at most 2^14 targets per bucket: N <= 2^28
+
+// Targets per bucket (log2) for N targets: the smallest 2^s >= 256 with at
+// most kMaxBuckets buckets.  Returns 0 when N needs more than 2^28 targets.
+__host__ __device__ inline uint32_t bucket_shift_for(uint32_t N) {
+    uint32_t s = 8;
+    while (((static_cast<unsigned long long>(N) + (1ull << s) - 1) >> s) > kMaxBuckets) ++s;
+    return s <= kMaxBucketShift ? s : 0;
+}
 constexpr int kExpandFires = 8;          // fires per expansion block (one warp each)
 constexpr uint32_t kMaxClasses = 256;    // distinct delivery delays
 
@@ -273,7 +289,7 @@ const char* kernel_name(int index);
 void launch_inject(const Engine& e, const unsigned long long* ev, const uint32_t* slot_of_group,
                    const uint32_t* group_off, uint32_t groups, cudaStream_t stream);
 // Groups the W == 1 "wheel" of e (a caller's event buffer) by target: the
-// hist / scan / scatter / segment-sort kernels of a tick.
+// tick's four grouping kernels.
 void launch_group(const Engine& e, cudaStream_t stream);
 // Batched form: one handle simulates several networks side by side.
 // Sets kMetaRuleOffBit on target-major synapses [tm_begin, tm_end).
@@ -285,6 +301,11 @@ void launch_rule_off(const Engine& e, unsigned long long tm_begin, unsigned long
 // entries) must start at zero.
 void launch_range_counts(const Engine& e, uint32_t n_begin, uint32_t n_end, unsigned long long tm_begin,
                          unsigned long long tm_end, unsigned long long* out, cudaStream_t stream);
+// out[0] += checksum of neurons [n_begin, n_end), out[1] += checksum of
+// target-major synapses [tm_begin, tm_end) (k_checksum); out must start at
+// zero.
+void launch_checksum(const Engine& e, uint32_t n_begin, uint32_t n_end, unsigned long long tm_begin,
+                     unsigned long long tm_end, unsigned long long* out, cudaStream_t stream);
 // One-time kernel attributes (dynamic shared memory of k_process); call with
 // the device current before the first tick.
 void configure_kernels();

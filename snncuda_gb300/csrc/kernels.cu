@@ -5,14 +5,14 @@
 // (SpikeScheduler.cpp:25-47: bucket FIFO order).  Per tick, on the main
 // stream:
 //
-//  1. k_hist       count due events per target (and move far-future
-//                  injections that become reachable into the wheel)
-//  2. k_scan_tile  exclusive scan of the per-target counts (+ last block
-//                  scans the tile sums)
-//  3. k_scan_out   segment starts and the ascending list of touched targets
-//  4. k_scatter    group the due events by target (unordered inside a group)
-//  5. k_events     one warp per touched target: restore due order inside its
-//                  group, then per synapse (lanes in parallel) the event's
+//  1. k_bcount     count due events per bucket of consecutive targets, per
+//                   chunk of the due list (and move far-future injections
+//                   that become reachable into the wheel)
+//  2. k_bscan      bucket starts
+//  3. k_bscatter   place every event in its bucket
+//  4. k_bsort      per bucket: group by target, segment starts
+//  5. k_events     one warp per target with events: restore due order inside
+//                  its group, then per synapse (lanes in parallel) the event's
 //                  pre-spike STDP, pre-spike count and spike-code pattern
 //                  (SynapseDendriteProcessor.cpp:104-133, :318-365); writes
 //                  each event's input for the neuron walk
@@ -187,25 +187,6 @@ __device__ bool last_block(uint32_t* counter) {
     __syncthreads();
     if (is_last) __threadfence();
     return is_last;
-}
-
-// Exclusive scan of n values in place, run by a single block (carry loop).
-__device__ void block_scan_inplace(uint32_t* data, uint32_t n, uint32_t* total_out) {
-    __shared__ uint32_t carry;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    for (uint32_t base = 0; base < n; base += kThreads) {
-        const uint32_t i = base + threadIdx.x;
-        const uint32_t v = i < n ? __ldcg(data + i) : 0;
-        uint32_t tot;
-        const uint32_t ex = block_excl_scan(v, &tot);
-        if (i < n) data[i] = carry + ex;
-        __syncthreads();
-        if (threadIdx.x == 0) carry += tot;
-        __syncthreads();
-    }
-    if (total_out && threadIdx.x == 0) *total_out = carry;
-    __syncthreads();
 }
 
 // ---------------------------------------------------------------------------
@@ -685,47 +666,107 @@ __device__ void code_update(SynB& b, const NeuronParam& p, uint32_t t, uint16_t*
 // kernels
 // ---------------------------------------------------------------------------
 
-// Count due events per target; block 0 first moves far-future injections
-// whose delivery tick t + W - 1 just became addressable into the (empty)
-// slot of that tick.
-__global__ void k_hist(Engine e) {
-    tick_enter();
-    const uint32_t t = e.ts->tick;
-    if (blockIdx.x == 0) {
-        const uint32_t ft = e.ts->far_ticks;
-        if (ft > 0) {
-            const long long rel = static_cast<long long>(t) + e.W - 1 - e.ts->far_first_tick;
-            if (rel >= 0 && rel < ft) {
-                const uint32_t b = e.far_idx[rel], en = e.far_idx[rel + 1];
-                const uint32_t slot = (t + e.W - 1) & e.wmask;
-                const uint32_t base = e.slot_count[slot];
-                if (base + (en - b) > e.slot_cap) {
-                    if (threadIdx.x == 0) raise_status(e, kStatusSlotOverflow);
-                } else {
-                    unsigned long long* dst = e.wheel + static_cast<size_t>(slot) * e.slot_cap + base;
-                    for (uint32_t i = threadIdx.x; i < en - b; i += blockDim.x) dst[i] = e.far_ev[b + i];
-                    __syncthreads();
-                    if (threadIdx.x == 0) e.slot_count[slot] = base + (en - b);
-                }
-            }
-        }
+// ---------------------------------------------------------------------------
+// grouping: the tick's due list regrouped by target (ascending), each
+// target's events in due order, in four kernels:
+//   k_bcount    a block per contiguous chunk of the due list: events per
+//               bucket of 2^bucket_shift consecutive targets, counted in
+//               shared memory; the block's row of counts goes to bcnt and is
+//               added into the bucket totals (one atomic per nonzero bucket)
+//   k_bscan     one block: bucket starts (exclusive scan of the totals)
+//   k_bscatter  a block per chunk: one reservation per (chunk, bucket), then
+//               every event goes to its bucket's range of grp_tmp (order
+//               inside a bucket arbitrary)
+//   k_bsort     a block per bucket: a counting sort of the bucket's events by
+//               target (in shared memory when the bucket fits), segment
+//               starts written; inside a target the order stays arbitrary
+//               (k_events ranks a target's events by due index, the grouping
+//               entry point sorts them with k_segsort)
+// Per event that is two reads of the due list, one scattered write, and a
+// coalesced read and write per bucket: no per-target global atomics.
+// ---------------------------------------------------------------------------
+
+// Block-wide exclusive scan of a[0 .. n) in shared memory (n <= 64 *
+// kThreads), in place; returns the total.  Every thread takes a run of
+// consecutive entries.
+__device__ uint32_t block_scan_shared(uint32_t* a, uint32_t n) {
+    const uint32_t per = (n + kThreads - 1) / kThreads;
+    const uint32_t b = threadIdx.x * per;
+    const uint32_t en = b + per < n ? b + per : n;
+    uint32_t sum = 0;
+    for (uint32_t i = b; i < en; ++i) sum += a[i];
+    uint32_t total;
+    uint32_t run = block_excl_scan(sum, &total);
+    for (uint32_t i = b; i < en; ++i) {
+        const uint32_t v = a[i];
+        a[i] = run;
+        run += v;
     }
+    __syncthreads();
+    return total;
+}
+
+// Moves the far-future injections whose delivery tick t + W - 1 just became
+// addressable into the (empty) slot of that tick.  One block.
+__device__ void move_far_injections(const Engine& e, uint32_t t) {
+    const uint32_t ft = e.ts->far_ticks;
+    if (ft == 0) return;
+    const long long rel = static_cast<long long>(t) + e.W - 1 - e.ts->far_first_tick;
+    if (rel < 0 || rel >= ft) return;
+    const uint32_t b = e.far_idx[rel], en = e.far_idx[rel + 1];
+    const uint32_t slot = (t + e.W - 1) & e.wmask;
+    const uint32_t base = e.slot_count[slot];
+    if (base + (en - b) > e.slot_cap) {
+        if (threadIdx.x == 0) raise_status(e, kStatusSlotOverflow);
+        return;
+    }
+    unsigned long long* dst = e.wheel + static_cast<size_t>(slot) * e.slot_cap + base;
+    for (uint32_t i = threadIdx.x; i < en - b; i += blockDim.x) dst[i] = e.far_ev[b + i];
+    __syncthreads();
+    if (threadIdx.x == 0) e.slot_count[slot] = base + (en - b);
+}
+
+// This block's chunk [beg, end) of a due list of n events.
+__device__ __forceinline__ void chunk_of(uint32_t n, uint32_t& beg, uint32_t& end) {
+    const uint32_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const unsigned long long b = static_cast<unsigned long long>(blockIdx.x) * chunk;
+    beg = b < n ? static_cast<uint32_t>(b) : n;
+    end = n - beg < chunk ? n : beg + chunk;
+}
+
+__global__ void __launch_bounds__(kThreads) k_bcount(Engine e) {
+    tick_enter();
+    extern __shared__ uint32_t s_hist[];  // [nbuckets]
+    const uint32_t t = e.ts->tick;
+    if (blockIdx.x == 0) move_far_injections(e, t);
+    const uint32_t B = e.nbuckets;
+    for (uint32_t b = threadIdx.x; b < B; b += blockDim.x) s_hist[b] = 0;
+    __syncthreads();
     const uint32_t slot = t & e.wmask;
     const uint32_t n = e.slot_count[slot];
     const unsigned long long* ev = e.wheel + static_cast<size_t>(slot) * e.slot_cap;
+    uint32_t beg, end;
+    chunk_of(n, beg, end);
     uint32_t ext = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (uint32_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
         const uint32_t lo = static_cast<uint32_t>(ev[i]);
         const uint32_t tgt = lo & ~kExternalBit;
         if (tgt >= e.N) {  // only reachable through snncuda_group_events with bad input
             raise_status(e, kStatusBadEvent);
             continue;
         }
-        atomicAdd(&e.cnt[tgt], 1u);
+        atomicAdd(&s_hist[tgt >> e.bucket_shift], 1u);
         ext += lo >> 31;
     }
     ext = __reduce_add_sync(0xffffffffu, ext);
     if ((threadIdx.x & 31) == 0 && ext) atomicAdd(&e.ts->external, static_cast<unsigned long long>(ext));
+    __syncthreads();
+    uint32_t* row = e.bcnt + static_cast<size_t>(blockIdx.x) * B;
+    for (uint32_t b = threadIdx.x; b < B; b += blockDim.x) {
+        const uint32_t c = s_hist[b];
+        row[b] = c;
+        if (c) atomicAdd(&e.btot[b], c);
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         e.ts->n_due = n;
         e.ts->post_tick = t;        // the previous tick's k_post has finished
@@ -733,84 +774,68 @@ __global__ void k_hist(Engine e) {
     }
 }
 
-// Phase 1 of the per-target scan: tile sums of counts and of touched targets;
-// the last block turns them into exclusive tile bases.
-__global__ void k_scan_tile(Engine e) {
+// Bucket starts; the totals return to zero for the next tick.  One block.
+__global__ void __launch_bounds__(kThreads) k_bscan(Engine e) {
     tick_enter();
-    constexpr int kItems = kScanTile / kThreads;
-    const uint32_t tiles = (e.N + kScanTile - 1) / kScanTile;
-    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        uint32_t sum = 0, nz = 0;
-        const uint32_t base = tile * kScanTile + threadIdx.x * kItems;
+    const uint32_t B = e.nbuckets;
+    __shared__ uint32_t s_carry;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    // kThreads x 16 buckets per round, 16 consecutive per thread
+    constexpr uint32_t kPer = 16;
+    for (uint32_t base = 0; base < B; base += kThreads * kPer) {
+        const uint32_t b0 = base + threadIdx.x * kPer;
+        uint32_t v[kPer];
+        uint32_t sum = 0;
 #pragma unroll
-        for (int j = 0; j < kItems; ++j) {
-            const uint32_t i = base + j;
-            const uint32_t c = i < e.N ? e.cnt[i] : 0;
-            sum += c;
-            nz += c != 0;
+        for (uint32_t j = 0; j < kPer; ++j) {
+            v[j] = b0 + j < B ? __ldcg(e.btot + b0 + j) : 0u;
+            sum += v[j];
         }
-        uint32_t ts_sum, ts_nz;
-        block_excl_scan(sum, &ts_sum);
-        block_excl_scan(nz, &ts_nz);
-        if (threadIdx.x == 0) {
-            e.tile_sum[tile] = ts_sum;
-            e.tile_nz[tile] = ts_nz;
-        }
-    }
-    if (last_block(&e.ts->done_scan)) {
-        block_scan_inplace(e.tile_sum, tiles, nullptr);
-        block_scan_inplace(e.tile_nz, tiles, &e.ts->n_touched);
-    }
-}
-
-// Phase 2: per-target segment starts and the ascending touched list.
-__global__ void k_scan_out(Engine e) {
-    tick_enter();
-    constexpr int kItems = kScanTile / kThreads;
-    const uint32_t tiles = (e.N + kScanTile - 1) / kScanTile;
-    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        const uint32_t base = tile * kScanTile + threadIdx.x * kItems;
-        uint32_t c[kItems];
-        uint32_t sum = 0, nz = 0;
+        uint32_t total;
+        uint32_t run = s_carry + block_excl_scan(sum, &total);
 #pragma unroll
-        for (int j = 0; j < kItems; ++j) {
-            const uint32_t i = base + j;
-            c[j] = i < e.N ? e.cnt[i] : 0;
-            sum += c[j];
-            nz += c[j] != 0;
-        }
-        uint32_t seg = __ldcg(e.tile_sum + tile) + block_excl_scan(sum, nullptr);
-        uint32_t pos = __ldcg(e.tile_nz + tile) + block_excl_scan(nz, nullptr);
-#pragma unroll
-        for (int j = 0; j < kItems; ++j) {
-            const uint32_t i = base + j;
-            if (i < e.N) {
-                e.seg_start[i] = seg;  // also for targets without events (empty segment)
-                if (c[j] != 0) {
-                    if (e.tbeg) e.tbeg[pos] = seg;
-                    e.touched[pos++] = i;
-                }
+        for (uint32_t j = 0; j < kPer; ++j) {
+            if (b0 + j < B) {
+                e.bstart[b0 + j] = run;
+                e.bcur[b0 + j] = run;
+                e.btot[b0 + j] = 0;
             }
-            seg += c[j];
+            run += v[j];
         }
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        e.bstart[B] = s_carry;
+        e.seg_start[e.N] = s_carry;
     }
 }
 
-// Group due events by target: each event takes a position inside its
-// target's segment (counts return to zero for the next tick).
-__global__ void k_scatter(Engine e) {
+__global__ void __launch_bounds__(kThreads) k_bscatter(Engine e) {
     tick_enter();
-    const uint32_t t = e.ts->tick;
-    const uint32_t slot = t & e.wmask;
+    extern __shared__ uint32_t s_pos[];  // [nbuckets] next position of this chunk in each bucket
+    const uint32_t B = e.nbuckets;
+    const uint32_t* row = e.bcnt + static_cast<size_t>(blockIdx.x) * B;
+    for (uint32_t b = threadIdx.x; b < B; b += blockDim.x) {
+        const uint32_t c = row[b];
+        s_pos[b] = c ? atomicAdd(&e.bcur[b], c) : 0u;
+    }
+    __syncthreads();
+    const uint32_t slot = e.ts->tick & e.wmask;
     const uint32_t n = e.ts->n_due;
     const unsigned long long* ev = e.wheel + static_cast<size_t>(slot) * e.slot_cap;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    uint32_t beg, end;
+    chunk_of(n, beg, end);
+    for (uint32_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
         const unsigned long long v = ev[i];
         const uint32_t lo = static_cast<uint32_t>(v);
         const uint32_t tgt = lo & ~kExternalBit;
         if (tgt >= e.N) continue;
-        const uint32_t pos = e.seg_start[tgt] + atomicSub(&e.cnt[tgt], 1u) - 1u;
-        e.grp[pos] = (v & 0xFFFFFFFF00000000ull) | (i | (lo & kExternalBit));
+        const uint32_t pos = atomicAdd(&s_pos[tgt >> e.bucket_shift], 1u);
+        e.grp_tmp[pos] = (v & 0xFFFFFFFF00000000ull) | (i | (lo & kExternalBit));
+        e.grp_ltgt[pos] = static_cast<uint16_t>(tgt & ((1u << e.bucket_shift) - 1u));
     }
 }
 
@@ -890,32 +915,71 @@ __device__ void warp_merge_sort(unsigned long long* a, unsigned long long* b, ui
     }
 }
 
-// Restore due order inside every target's group (k_scatter leaves it in
-// arbitrary order; keys are unique due indices).  One warp per target:
-// groups of up to 32 events are bitonic-sorted in registers, longer ones are
-// merge-sorted (warp_merge_sort).  Output goes to grp_sorted.  Used by the
-// grouping entry point; the tick sorts inside k_events.
+
+
+// Events k_bsort places in shared memory before writing them out.
+constexpr uint32_t kSortSmemEvents = 4096;
+constexpr size_t kSortSmemBytes = kSortSmemEvents * sizeof(unsigned long long);
+
+// One block per bucket: a counting sort of the bucket's events by target.
+// The events of each target end up contiguous in grp (in arbitrary order;
+// k_events ranks them by due index) and the targets' segment starts are
+// written.  A bucket of at most kSortSmemEvents events is placed in shared
+// memory and written out coalesced; a larger one is placed in grp directly.
+__global__ void __launch_bounds__(kThreads) k_bsort(Engine e) {
+    tick_enter();
+    extern __shared__ __align__(16) unsigned long long s_sort[];  // kSortSmemEvents, then counters
+    uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_sort + kSortSmemEvents);  // [2^bucket_shift]
+    const uint32_t width = 1u << e.bucket_shift;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t b = blockIdx.x; b < e.nbuckets; b += gridDim.x) {
+        const uint32_t lo = e.bstart[b], hi = e.bstart[b + 1], m = hi - lo;
+        const uint32_t n0 = b << e.bucket_shift;
+        const uint32_t nw = e.N - n0 < width ? e.N - n0 : width;
+        for (uint32_t j = threadIdx.x; j < nw; j += blockDim.x) s_cnt[j] = 0;
+        __syncthreads();
+        const unsigned long long* in = e.grp_tmp + lo;
+        const uint16_t* lt = e.grp_ltgt + lo;
+        for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) atomicAdd(&s_cnt[lt[i]], 1u);
+        __syncthreads();
+        uint32_t nz = 0;  // targets with events (statistics)
+        for (uint32_t j = threadIdx.x; j < nw; j += blockDim.x) nz += s_cnt[j] != 0;
+        nz = __reduce_add_sync(0xffffffffu, nz);
+        if (lane == 0 && nz) atomicAdd(&e.ts->n_touched, nz);
+        block_scan_shared(s_cnt, nw);  // segment starts relative to lo
+        for (uint32_t j = threadIdx.x; j < nw; j += blockDim.x) e.seg_start[n0 + j] = lo + s_cnt[j];
+        __syncthreads();
+        const bool small = m <= kSortSmemEvents;
+        unsigned long long* P = small ? s_sort : e.grp + lo;
+        for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) P[atomicAdd(&s_cnt[lt[i]], 1u)] = in[i];
+        __syncthreads();
+        if (small)
+            for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) e.grp[lo + i] = s_sort[i];
+        __syncthreads();
+    }
+}
+
+// Grouping entry point only: due order inside every target's group of grp
+// (one warp per target: up to 32 events bitonic-sorted in registers, longer
+// groups merge-sorted with grp_tmp as scratch).
 __global__ void __launch_bounds__(kThreads) k_segsort(Engine e) {
-    const uint32_t n_touched = e.ts->n_touched;
-    const uint32_t n_due = e.ts->n_due;
     const int lane = threadIdx.x & 31;
     const uint32_t warps = gridDim.x * (blockDim.x / 32);
-    for (uint32_t k = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); k < n_touched; k += warps) {
-        const uint32_t n = e.touched[k];
+    for (uint32_t n = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); n < e.N; n += warps) {
         const uint32_t beg = e.seg_start[n];
-        const uint32_t end = k + 1 < n_touched ? e.seg_start[e.touched[k + 1]] : n_due;
-        const uint32_t len = end - beg;
-        unsigned long long* src = e.grp + beg;
-        unsigned long long* dst = e.grp_sorted + beg;
-        for (uint32_t j = lane; j < len; j += 32) e.evt_tgt[beg + j] = n;
-        if (lane == 0) e.seg_len[n] = len;
+        const uint32_t len = e.seg_start[n + 1] - beg;
+        if (len <= 1) continue;
+        unsigned long long* g = e.grp + beg;
         if (len <= 32) {
-            unsigned long long v = lane < static_cast<int>(len) ? src[lane] : ~0ull;
+            unsigned long long v = lane < static_cast<int>(len) ? g[lane] : ~0ull;
             uint32_t key = lane < static_cast<int>(len) ? grp_key(v) : 0xFFFFFFFFu;
             warp_bitonic(v, key);
-            if (lane < static_cast<int>(len)) dst[lane] = v;
+            if (lane < static_cast<int>(len)) g[lane] = v;
         } else {
-            warp_merge_sort(src, dst, len);
+            unsigned long long* tmp = e.grp_tmp + beg;
+            warp_merge_sort(g, tmp, len);  // sorted into tmp
+            for (uint32_t k = lane; k < len; k += 32) g[k] = tmp[k];
+            __syncwarp();
         }
     }
 }
@@ -977,7 +1041,7 @@ struct SortedDue {
 // each event's position in due order is its rank among the group's due
 // indices, and the events of each synapse are found with one match; the
 // synapse's earliest event's lane then processes all of them in due order.
-// Longer groups are placed by rank into grp_sorted and scanned.
+// Longer groups are merge-sorted into grp_tmp and scanned.
 // A synapse with a single event in its target's group this tick: the unit
 // of work k_events queues so that all 32 lanes of a warp carry one.
 struct EvItem {
@@ -1073,7 +1137,7 @@ __device__ __forceinline__ void events_of_target(const Engine& e, uint32_t n, ui
         __syncwarp();
         return;
     }
-    unsigned long long* srt = e.grp_sorted + beg;
+    unsigned long long* srt = e.grp_tmp + beg;  // grp_tmp is free once the groups are built
     warp_merge_sort(e.grp + beg, srt, len);
     const NeuronParam p = e.nparam[n];
     for (uint32_t j = lane; j < len; j += 32) {
@@ -1101,17 +1165,15 @@ __device__ __forceinline__ void events_of_target(const Engine& e, uint32_t n, ui
     __syncwarp();
 }
 
-// One warp per touched target (events_of_target).  Synapses with a single
-// event this tick go to a per-warp queue in shared memory and are processed
-// 32 at a time, one per lane, whatever targets they belong to; repeats and
-// long groups are processed in place.
+// One warp per target with due events (events_of_target).  Synapses with a
+// single event this tick go to a per-warp queue in shared memory and are
+// processed 32 at a time, one per lane, whatever targets they belong to;
+// repeats and long groups are processed in place.
 __global__ void __launch_bounds__(kThreads, SNNGB_EVENTS_MIN_BLOCKS) k_events(Engine e) {
     tick_enter();
     __shared__ uint32_t s_due[kThreads], s_rank[kThreads];
     __shared__ EvItem s_queue[kThreads / 32][64];
     const uint32_t t = e.ts->tick;
-    const uint32_t n_touched = e.ts->n_touched;
-    const uint32_t n_due = e.ts->n_due;
     const int stdp = e.ts->stdp_enabled;
     const int temporal = e.ts->temporal_enabled;
     const uint32_t lane = threadIdx.x & 31;
@@ -1119,10 +1181,10 @@ __global__ void __launch_bounds__(kThreads, SNNGB_EVENTS_MIN_BLOCKS) k_events(En
     EvItem* queue = s_queue[threadIdx.x >> 5];
     uint32_t qn = 0;  // warp-uniform
     const uint32_t warps = gridDim.x * (blockDim.x / 32);
-    for (uint32_t k = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); k < n_touched; k += warps) {
-        const uint32_t n = e.touched[k];
-        const uint32_t beg = e.tbeg[k];
-        const uint32_t end = k + 1 < n_touched ? e.tbeg[k + 1] : n_due;
+    for (uint32_t n = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); n < e.N; n += warps) {
+        const uint32_t beg = e.seg_start[n];
+        const uint32_t end = e.seg_start[n + 1];
+        if (end == beg) continue;
         events_of_target(e, n, beg, end - beg, t, stdp, temporal, s_due + wbase, s_rank + wbase, queue, qn);
         if (qn >= 32) {
             __syncwarp();
@@ -1361,8 +1423,7 @@ __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(
     __shared__ uint32_t s_lo, s_cnt;
     __shared__ float s_wt[kThreads / 32][32];  // per warp: weights of the events redone after a fire
     const uint32_t t = e.ts->tick;
-    const uint32_t n_touched = e.ts->n_touched;
-    const uint32_t n_due = e.ts->n_due;
+    const uint32_t N = e.N;
     const int stdp = e.ts->stdp_enabled;
     if (threadIdx.x == 0) mbar_init(&s_bar, 1);
     __syncthreads();
@@ -1373,16 +1434,17 @@ __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(
     const float* ltp = ltp_shared ? reinterpret_cast<const float*>(s_ev + kStageEvents) : e.tab.ltp;
     uint32_t parity = 0;
     bool staging = true;  // false after a copy outlived its wait: shared memory is no longer used
-    // `per` consecutive touched targets per block and round: the grid has at
-    // least three blocks per SM, so one wave of equal blocks spreads over
-    // every SM (the block scheduler fills each SM to its occupancy limit)
-    const uint32_t per_even = (n_touched + gridDim.x - 1) / gridDim.x;
+    // `per` consecutive targets per block and round (their events are one
+    // contiguous range of the grouped list): the grid has at least three
+    // blocks per SM, so one wave of equal blocks spreads over every SM (the
+    // block scheduler fills each SM to its occupancy limit)
+    const uint32_t per_even = (N + gridDim.x - 1) / gridDim.x;
     const uint32_t per = per_even < blockDim.x ? per_even : blockDim.x;
-    for (uint32_t k0 = blockIdx.x * per; k0 < n_touched; k0 += gridDim.x * per) {
+    for (uint32_t k0 = blockIdx.x * per; k0 < N; k0 += gridDim.x * per) {
         if (threadIdx.x == 0) {
-            const uint32_t k1 = k0 + per < n_touched ? k0 + per : n_touched;
-            const uint32_t lo = e.tbeg[k0];
-            const uint32_t hi = k1 < n_touched ? e.tbeg[k1] : n_due;
+            const uint32_t k1 = k0 + per < N ? k0 + per : N;
+            const uint32_t lo = e.seg_start[k0];
+            const uint32_t hi = e.seg_start[k1];
             const uint32_t cnt = staging ? (hi - lo < kStageEvents ? hi - lo : kStageEvents) : 0u;
             s_lo = lo;
             s_cnt = cnt;
@@ -1404,17 +1466,17 @@ __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(
             return ok;
         };
         const uint32_t k = k0 + threadIdx.x;
-        const bool mine_target = threadIdx.x < per && k < n_touched;
         Walk w;
         w.n = w.beg = w.len = w.i = w.fires = w.first_fire = 0;
+        if (threadIdx.x < per && k < N) {
+            w.n = k;
+            w.beg = e.seg_start[k];
+            w.len = e.seg_start[k + 1] - w.beg;
+        }
+        const bool mine_target = w.len > 0;  // a target with due events
         bool fired = false;
         Staged mine = st;
-        if (mine_target) {
-            w.n = e.touched[k];
-            w.beg = e.tbeg[k];
-            w.len = (k + 1 < n_touched ? e.tbeg[k + 1] : n_due) - w.beg;
-            fired = walk_to_first_fire(e, w, t, mine, ready);
-        }
+        if (mine_target) fired = walk_to_first_fire(e, w, t, mine, ready);
         if (!ready()) mine.cnt = 0;
         walk_fired_targets(e, w, fired, t, stdp, mine, ltp, s_wt[threadIdx.x >> 5]);
         if (mine_target) finish_walk(e, w);
@@ -1481,12 +1543,10 @@ __device__ __forceinline__ void temporal_target(const Engine& e, uint32_t n, uin
 
 __global__ void __launch_bounds__(kThreads) k_temporal(Engine e) {
     const uint32_t t = e.ts->tick;
-    const uint32_t n_touched = e.ts->n_touched;
-    const uint32_t n_due = e.ts->n_due;
     const int temporal = e.ts->temporal_enabled;
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n_touched; k += gridDim.x * blockDim.x) {
-        const uint32_t n = e.touched[k];
-        const uint32_t len = (k + 1 < n_touched ? e.tbeg[k + 1] : n_due) - e.tbeg[k];
+    for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < e.N; n += gridDim.x * blockDim.x) {
+        const uint32_t len = e.seg_start[n + 1] - e.seg_start[n];
+        if (len == 0) continue;
         if (e.nparam[n].max_refs == 1) {
             temporal_target<true>(e, n, len, t, temporal);
         } else {
@@ -1762,7 +1822,76 @@ __global__ void k_range_counts(Engine e, uint32_t nb, uint32_t ne, unsigned long
     if (code_matches) atomicAdd(out + 4, code_matches);
 }
 
+// 64-bit mix of one word into a running hash (multiply / xor-shift rounds).
+__device__ __forceinline__ unsigned long long mix64(unsigned long long h, unsigned long long w) {
+    h ^= w + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
+    h *= 0xbf58476d1ce4e5b9ull;
+    h ^= h >> 31;
+    return h;
+}
+
+template <int kWords>
+__device__ __forceinline__ unsigned long long record_hash(unsigned long long index, const uint32_t* w) {
+    unsigned long long h = mix64(0x6a09e667f3bcc908ull, index);
+#pragma unroll
+    for (int i = 0; i < kWords; ++i) h = mix64(h, w[i]);
+    return h;
+}
+
+// Order-independent checksums of neurons [nb, ne) (NeuronRec + NeuronTp)
+// and target-major synapses [tb, te) (the 64-byte record, its rule-off bit
+// masked): the sum over records of a hash of (index within the range,
+// record words).  A batch member and its solo run have the same records at
+// the same relative indices, so equal sums mean equal state (up to hash
+// collisions); the temporal-pattern contents enter through their counters.
+__global__ void k_checksum(Engine e, uint32_t nb, uint32_t ne, unsigned long long tb, unsigned long long te,
+                           unsigned long long* out) {
+    const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+    const unsigned long long first = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+    unsigned long long hn = 0, hs = 0;
+    for (unsigned long long n = nb + first; n < ne; n += stride) {
+        uint32_t w[24];
+        const uint4* r = reinterpret_cast<const uint4*>(e.nrec + n);
+        const uint4* q = reinterpret_cast<const uint4*>(e.ntp + n);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const uint4 v = r[i];
+            w[4 * i] = v.x; w[4 * i + 1] = v.y; w[4 * i + 2] = v.z; w[4 * i + 3] = v.w;
+        }
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const uint4 v = q[i];
+            w[16 + 4 * i] = v.x; w[17 + 4 * i] = v.y; w[18 + 4 * i] = v.z; w[19 + 4 * i] = v.w;
+        }
+        hn += record_hash<24>(n - nb, w);
+    }
+    for (unsigned long long i = tb + first; i < te; i += stride) {
+        uint32_t w[16];
+        const uint4* r = reinterpret_cast<const uint4*>(e.syn + i);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint4 v = r[k];
+            w[4 * k] = v.x; w[4 * k + 1] = v.y; w[4 * k + 2] = v.z; w[4 * k + 3] = v.w;
+        }
+        w[3] &= ~(1u << kMetaRuleOffBit);  // SynA.meta
+        hs += record_hash<16>(i - tb, w);
+    }
+    for (int d = 16; d > 0; d >>= 1) {
+        hn += __shfl_down_sync(0xffffffffu, hn, d);
+        hs += __shfl_down_sync(0xffffffffu, hs, d);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out, hn);
+        atomicAdd(out + 1, hs);
+    }
+}
+
 }  // namespace
+
+void launch_checksum(const Engine& e, uint32_t n_begin, uint32_t n_end, unsigned long long tm_begin,
+                     unsigned long long tm_end, unsigned long long* out, cudaStream_t stream) {
+    k_checksum<<<e.grid_wide * 2, kThreads, 0, stream>>>(e, n_begin, n_end, tm_begin, tm_end, out);
+}
 
 void launch_rule_off(const Engine& e, unsigned long long tm_begin, unsigned long long tm_end, cudaStream_t stream) {
     if (tm_end > tm_begin) k_rule_off<<<1024, kThreads, 0, stream>>>(e.syn, tm_begin, tm_end);
@@ -1791,10 +1920,15 @@ static void launch_main(void (*kernel)(Engine), uint32_t grid, uint32_t block, s
     cudaLaunchKernelEx(&cfg, kernel, e);
 }
 
+// Dynamic shared memory of the grouping kernels.
+static size_t bucket_smem(const Engine& e) { return static_cast<size_t>(e.nbuckets) * sizeof(uint32_t); }
+static size_t bsort_smem(const Engine& e) {
+    return kSortSmemBytes + (static_cast<size_t>(1) << e.bucket_shift) * sizeof(uint32_t);
+}
+static uint32_t bsort_grid(const Engine& e) { return e.nbuckets < 4 * e.grid_wide ? e.nbuckets : 4 * e.grid_wide; }
+
 void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
-    const uint32_t tiles = (e.N + kScanTile - 1) / kScanTile;
     const uint32_t wide = e.grid_wide;
-    const uint32_t scan_grid = tiles == 0 ? 1 : (tiles < wide ? tiles : wide);
     cudaStream_t stream = s.main;
     // Kernels that follow another kernel directly on the main stream are
     // programmatic dependents; the per-kernel profile (event marks between
@@ -1808,21 +1942,20 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     auto side_mark = [&](int index, bool after) {
         if (marks) cudaEventRecordWithFlags(marks[2 * index + (after ? 1 : 0)], s.side, cudaEventRecordExternal);
     };
-    // k_hist follows a wait on the side stream: a full dependency
-    mark(false); launch_main(k_hist, wide * 4, kThreads, 0, stream, false, e); mark(true);
-    mark(false); launch_main(k_scan_tile, scan_grid, kThreads, 0, stream, dep, e); mark(true);
-    mark(false); launch_main(k_scan_out, scan_grid, kThreads, 0, stream, dep, e); mark(true);
-    mark(false); launch_main(k_scatter, wide, kThreads, 0, stream, dep, e); mark(true);
+    // k_bcount follows a wait on the side stream: a full dependency
+    mark(false); launch_main(k_bcount, e.grid_bucket, kThreads, bucket_smem(e), stream, false, e); mark(true);
+    mark(false); launch_main(k_bscan, 1, kThreads, 0, stream, dep, e); mark(true);
+    mark(false); launch_main(k_bscatter, e.grid_bucket, kThreads, bucket_smem(e), stream, dep, e); mark(true);
+    mark(false); launch_main(k_bsort, bsort_grid(e), kThreads, bsort_smem(e), stream, dep, e); mark(true);
     // the temporal update forks off here and runs beside k_events / k_process
-    // (it needs only the touched list and the group sizes; started before
-    // k_scatter it slowed that kernel's atomics more than it gained)
+    // (it needs only the segment starts)
     cudaEventRecord(s.ev[0], stream);
     cudaStreamWaitEvent(s.side, s.ev[0], 0);
     side_mark(9, false);
     k_temporal<<<e.grid_process, kThreads, 0, s.side>>>(e);
     side_mark(9, true);
     cudaEventRecord(s.ev[1], s.side);
-    mark(false); launch_main(k_events, e.grid_wide * 4, kThreads, 0, stream, dep, e); mark(true);
+    mark(false); launch_main(k_events, e.grid_events, kThreads, 0, stream, dep, e); mark(true);
     mark(false); launch_main(k_process, e.grid_walk, kThreads, kProcessSmem, stream, dep, e); mark(true);
     // post-spike STDP of the fired targets runs beside the fire ordering and
     // the expansion (synapse records are not touched by those)
@@ -1840,25 +1973,28 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
 }
 
 const char* kernel_name(int index) {
-    static const char* names[kKernelCount] = {"k_hist",      "k_scan_tile",  "k_scan_out", "k_scatter",
+    static const char* names[kKernelCount] = {"k_bcount",    "k_bscan",      "k_bscatter",  "k_bsort",
                                               "k_events",    "k_process",    "k_fire_list", "k_fire_count",
                                               "k_expand",    "k_temporal",   "k_post"};
     return index >= 0 && index < kKernelCount ? names[index] : "";
 }
 
 void launch_group(const Engine& e, cudaStream_t stream) {
-    const uint32_t tiles = (e.N + kScanTile - 1) / kScanTile;
-    const uint32_t scan_grid = tiles == 0 ? 1 : (tiles < e.grid_wide ? tiles : e.grid_wide);
-    k_hist<<<e.grid_wide, kThreads, 0, stream>>>(e);
-    k_scan_tile<<<scan_grid, kThreads, 0, stream>>>(e);
-    k_scan_out<<<scan_grid, kThreads, 0, stream>>>(e);
-    k_scatter<<<e.grid_wide, kThreads, 0, stream>>>(e);
+    k_bcount<<<e.grid_bucket, kThreads, bucket_smem(e), stream>>>(e);
+    k_bscan<<<1, kThreads, 0, stream>>>(e);
+    k_bscatter<<<e.grid_bucket, kThreads, bucket_smem(e), stream>>>(e);
+    k_bsort<<<bsort_grid(e), kThreads, bsort_smem(e), stream>>>(e);
     k_segsort<<<e.grid_wide * 4, kThreads, 0, stream>>>(e);
 }
 
 void configure_kernels() {
     cudaFuncSetAttribute(k_process, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          static_cast<int>(kProcessSmem));
+    const int bucket_bytes = static_cast<int>(kMaxBuckets * sizeof(uint32_t));
+    cudaFuncSetAttribute(k_bcount, cudaFuncAttributeMaxDynamicSharedMemorySize, bucket_bytes);
+    cudaFuncSetAttribute(k_bscatter, cudaFuncAttributeMaxDynamicSharedMemorySize, bucket_bytes);
+    cudaFuncSetAttribute(k_bsort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(kSortSmemBytes + (1u << kMaxBucketShift) * sizeof(uint32_t)));
 }
 
 void launch_init_syn(const Engine& e, const SynA* a, cudaStream_t stream) {

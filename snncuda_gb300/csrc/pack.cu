@@ -252,7 +252,7 @@ uint32_t grid_for(unsigned long long n) {
 }  // namespace
 
 int pack_network_device(const snncuda_network* net, float cfg_max_weight, cudaStream_t st,
-                        std::vector<void*>& owned, PackOut& out, std::string& msg) {
+                        DeviceBuffers& owned, PackOut& out, std::string& msg) {
     const uint32_t N = net->neuron_count;
     const unsigned long long S = net->synapse_count;
     if (S >= (1ull << 31)) {
@@ -275,7 +275,7 @@ int pack_network_device(const snncuda_network* net, float cfg_max_weight, cudaSt
     auto persist = [&](size_t bytes) -> void* {
         void* p = nullptr;
         if (cudaMallocAsync(&p, bytes ? bytes : 1, st) != cudaSuccess) return nullptr;
-        owned.push_back(p);
+        owned.push_back({p, bytes ? bytes : 1, BufKind::kState});
         return p;
     };
 

@@ -12,6 +12,19 @@
 
 namespace snngb {
 
+// One device allocation of a simulation and what an eviction to host memory
+// keeps of it: the whole buffer (state), nothing (per-tick scratch whose
+// contents do not outlive a tick), or the live prefix of every wheel slot.
+// kZero buffers are scratch that must read zero between ticks (restored as
+// zeros).
+enum class BufKind : uint8_t { kState, kScratch, kWheel, kZero };
+struct DeviceBuffer {
+    void* p;
+    size_t bytes;
+    BufKind kind;
+};
+using DeviceBuffers = std::vector<DeviceBuffer>;
+
 struct PackOut {
     // device buffers, owned by the caller's `owned` list
     SynAB* syn{nullptr};                      // [S] target-major records
@@ -33,6 +46,9 @@ struct PackOut {
 // stream-ordered on `st` (cudaMallocAsync) and appended to `owned`.  Returns SNNCUDA_OK or an SNNCUDA_ERR_* code with
 // `msg` set.
 int pack_network_device(const snncuda_network* net, float cfg_max_weight, cudaStream_t st,
-                        std::vector<void*>& owned, PackOut& out, std::string& msg);
+                        DeviceBuffers& owned, PackOut& out, std::string& msg);
+
+// Sets the thread-local message snncuda_last_error() returns (sim.cu).
+void set_last_error_message(const std::string& msg);
 
 }  // namespace snngb

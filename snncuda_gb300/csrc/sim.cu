@@ -20,6 +20,7 @@
 #include <memory>
 #include <mutex>
 #include <thread>
+#include <type_traits>
 #include <condition_variable>
 #include <new>
 #include <stdexcept>
@@ -56,6 +57,12 @@ int set_error(int code, const std::string& msg) {
     g_last_error = msg;
     return code;
 }
+
+}  // namespace
+
+void snngb::set_last_error_message(const std::string& msg) { g_last_error = msg; }
+
+namespace {
 
 constexpr float kTauValue[4] = {5.0F, 100.0F, 10.0F, 150.0F};  // receptor_decay_tau (:245-257)
 
@@ -126,7 +133,7 @@ T* dalloc(std::vector<void*>& owned, size_t count) {
 
 struct snncuda_sim {
     Engine e{};
-    std::vector<void*> owned;
+    DeviceBuffers owned;
     cudaStream_t stream{nullptr};
     bool own_stream{false};
     snncuda_config config{};
@@ -160,11 +167,16 @@ struct snncuda_sim {
     cudaGraphExec_t graph_one{nullptr};
     cudaGraphExec_t graph_prof{nullptr};
     cudaEvent_t marks[2 * kKernelCount]{};
-    static constexpr int kTicksPerGraph = 16;
+    uint32_t ticks_per_graph{16};  // ticks captured in graph_many
+    uint32_t sms{1};
 
     // second stream of the tick graphs (k_temporal) and its fork/join events
     cudaStream_t side{nullptr};
     cudaEvent_t tick_ev[4]{};
+    // eviction: the device state held in host memory (evict_impl / restore_impl)
+    bool evicted{false};
+    std::vector<std::vector<unsigned char>> evicted_data;  // per owned buffer
+    uint64_t evictions{0};
     // asynchronous runs (run_enqueue / run_complete)
     TickState* ts_pinned{nullptr};  // tick state copied back at the end of a run
     cudaEvent_t run_done{nullptr};
@@ -184,7 +196,9 @@ struct snncuda_sim {
         // device buffers are stream-ordered: freeing them does not stall
         // other streams (a server runs many simulations side by side)
         if (stream) cudaStreamSynchronize(stream);
-        for (void* p : owned) cudaFreeAsync(p, stream);
+        if (!evicted)  // an evicted simulation's buffers are already freed
+            for (const DeviceBuffer& b : owned)
+                if (b.p) cudaFreeAsync(b.p, stream);
         if (far_ev) cudaFreeAsync(far_ev, stream);
         if (far_idx) cudaFreeAsync(far_idx, stream);
         if (inj_ev) cudaFreeAsync(inj_ev, stream);
@@ -291,13 +305,14 @@ struct snncuda_sim {
 
 namespace {
 
-// A persistent device buffer of the simulation, stream-ordered on its stream.
+// A persistent device buffer of the simulation, stream-ordered on its
+// stream; `kind` says what an eviction keeps of it.
 template <typename T>
-T* salloc(snncuda_sim* sim, size_t count) {
+T* salloc(snncuda_sim* sim, size_t count, BufKind kind = BufKind::kState) {
     void* p = nullptr;
     if (count == 0) count = 1;
     check(cudaMallocAsync(&p, count * sizeof(T), sim->stream), "device allocation");
-    sim->owned.push_back(p);
+    sim->owned.push_back({p, count * sizeof(T), kind});
     return static_cast<T*>(p);
 }
 
@@ -349,6 +364,14 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     if (S > 0) {
         check(cudaMemcpyAsync(sim->c_of_tm.data(), pk.c_of_tm_d, S * 4, cudaMemcpyDeviceToHost, sim->stream), "copy");
         check(cudaMemcpyAsync(sim->tm_of_c.data(), pk.tm_of_c_d, S * 4, cudaMemcpyDeviceToHost, sim->stream), "copy");
+    }
+    // the synapse order maps live on the host from here on
+    for (DeviceBuffer& b : sim->owned) {
+        if (b.p == pk.c_of_tm_d || b.p == pk.tm_of_c_d) {
+            check(cudaFreeAsync(b.p, sim->stream), "free");
+            b.p = nullptr;
+            b.bytes = 0;
+        }
     }
 
     // ---- neuron parameters and temporal storage ----
@@ -407,6 +430,15 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     const uint64_t fire_tiles = (bit_words + 255) / 256;
     e.fire_tiles_cap = static_cast<uint32_t>(fire_tiles);
 
+    // ---- grouping buckets and launch shapes ----
+    int sms = 0;
+    check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sim->device), "device attribute");
+    e.bucket_shift = bucket_shift_for(N);
+    if (e.bucket_shift == 0) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "at most 2^28 neurons");
+    e.nbuckets = static_cast<uint32_t>(std::max<uint64_t>(1, (static_cast<uint64_t>(N) + (1u << e.bucket_shift) - 1) >> e.bucket_shift));
+    e.grid_bucket = static_cast<uint32_t>(std::max(1, sms * 2));
+    const uint32_t grid_bucket_max = static_cast<uint32_t>(std::max(1, sms * 4));  // the autotuner's largest
+
     // ---- tables ----
     uint32_t decay_len = 0;
     const std::vector<float> decay = build_decay_table(decay_len);
@@ -422,27 +454,26 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.ring = salloc<unsigned long long>(sim, ring_total);
     e.lcode = salloc<uint16_t>(sim, lcode_total);
     auto* d_cls = salloc<uint32_t>(sim, D);
-    e.wheel = salloc<unsigned long long>(sim, static_cast<size_t>(W) * slot_cap);
+    e.wheel = salloc<unsigned long long>(sim, static_cast<size_t>(W) * slot_cap, BufKind::kWheel);
     e.slot_count = salloc<uint32_t>(sim, W);
-    e.cnt = salloc<uint32_t>(sim, N);
-    e.seg_start = salloc<uint32_t>(sim, N);
-    const uint32_t scan_tiles = (N + kScanTile - 1) / kScanTile;
-    e.tile_sum = salloc<uint32_t>(sim, scan_tiles + 2);
-    e.tile_nz = salloc<uint32_t>(sim, scan_tiles + 2);
-    e.touched = salloc<uint32_t>(sim, N);
-    e.tbeg = salloc<uint32_t>(sim, N);
-    e.grp = salloc<unsigned long long>(sim, slot_cap);
-    e.grp_sorted = salloc<unsigned long long>(sim, slot_cap);
-    e.evin = salloc<EvIn>(sim, slot_cap);
-    e.ev_a0 = salloc<SynA>(sim, slot_cap);
-    e.fire_bits = salloc<uint32_t>(sim, bit_words);
-    e.fire_at = salloc<uint32_t>(sim, slot_cap);
-    e.fire_tile = salloc<uint32_t>(sim, fire_tiles + 2);
-    e.fire_list = salloc<uint32_t>(sim, fire_cap);
-    e.fired_tgt = salloc<uint32_t>(sim, N);
-    e.fired_cnt = salloc<uint32_t>(sim, N);
-    e.xsum = salloc<uint32_t>(sim, xblocks * std::max<uint32_t>(D, 1));
-    e.xdst = salloc<unsigned long long>(sim, xblocks * std::max<uint32_t>(D, 1));
+    e.seg_start = salloc<uint32_t>(sim, static_cast<size_t>(N) + 1, BufKind::kScratch);
+    e.bcnt = salloc<uint32_t>(sim, static_cast<size_t>(grid_bucket_max) * e.nbuckets, BufKind::kScratch);
+    e.btot = salloc<uint32_t>(sim, e.nbuckets, BufKind::kZero);
+    e.bstart = salloc<uint32_t>(sim, static_cast<size_t>(e.nbuckets) + 1, BufKind::kScratch);
+    e.bcur = salloc<uint32_t>(sim, e.nbuckets, BufKind::kScratch);
+    e.grp = salloc<unsigned long long>(sim, slot_cap, BufKind::kScratch);
+    e.grp_tmp = salloc<unsigned long long>(sim, slot_cap, BufKind::kScratch);
+    e.grp_ltgt = salloc<uint16_t>(sim, slot_cap, BufKind::kScratch);
+    e.evin = salloc<EvIn>(sim, slot_cap, BufKind::kScratch);
+    e.ev_a0 = salloc<SynA>(sim, slot_cap, BufKind::kScratch);
+    e.fire_bits = salloc<uint32_t>(sim, bit_words, BufKind::kZero);
+    e.fire_at = salloc<uint32_t>(sim, slot_cap, BufKind::kScratch);
+    e.fire_tile = salloc<uint32_t>(sim, fire_tiles + 2, BufKind::kZero);
+    e.fire_list = salloc<uint32_t>(sim, fire_cap, BufKind::kScratch);
+    e.fired_tgt = salloc<uint32_t>(sim, N, BufKind::kScratch);
+    e.fired_cnt = salloc<uint32_t>(sim, N, BufKind::kScratch);
+    e.xsum = salloc<uint32_t>(sim, xblocks * std::max<uint32_t>(D, 1), BufKind::kZero);
+    e.xdst = salloc<unsigned long long>(sim, xblocks * std::max<uint32_t>(D, 1), BufKind::kScratch);
     e.xdst_ok = salloc<uint32_t>(sim, std::max<uint32_t>(D, 1));
     e.raster = salloc<uint32_t>(sim, cfg.raster_capacity > 0 ? 2 * cfg.raster_capacity : 1);
     e.ts = salloc<TickState>(sim, 1);
@@ -464,10 +495,9 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     zero(e.lcode, sizeof(uint16_t) * lcode_total);
     h2d(d_cls, cls_delta.data(), cls_delta.size() * sizeof(uint32_t));
     zero(e.slot_count, sizeof(uint32_t) * W);
-    zero(e.cnt, sizeof(uint32_t) * N);
+    zero(e.btot, sizeof(uint32_t) * e.nbuckets);
     zero(e.fire_bits, sizeof(uint32_t) * bit_words);
     zero(e.xsum, sizeof(uint32_t) * xblocks * std::max<uint32_t>(D, 1));
-    zero(e.tile_sum, sizeof(uint32_t) * (scan_tiles + 2));
     zero(e.fire_tile, sizeof(uint32_t) * (fire_tiles + 2));
     h2d(d_decay, decay.data(), decay.size() * sizeof(float));
     h2d(d_ltp, ltp.data(), ltp.size() * sizeof(float));
@@ -492,9 +522,9 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     check(cudaGetLastError(), "init launch");
     sim->in_ptr = std::move(in_ptr);
 
-    int sms = 0;
-    check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sim->device), "device attribute");
     e.grid_wide = static_cast<uint32_t>(std::max(1, sms * 2));
+    e.grid_events = e.grid_wide * 4;
+    sim->sms = static_cast<uint32_t>(std::max(1, sms));
     e.grid_process = static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>((N + 255) / 256, sms * 8ull)));
     // k_process: at least three blocks per SM (of at least 64 targets) so its
     // one wave covers every SM; at most eight per SM
@@ -504,6 +534,326 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.grid_fire = static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>(fire_tiles, sms * 8ull)));
     sim->ensure_far(1, 2);
     check(cudaStreamSynchronize(st), "create synchronize");
+}
+
+// ---------------------------------------------------------------------------
+// eviction: a simulation's device state moves to host memory and back
+// (the reference's NeuronStateCache writes evicted NeuronStates to its
+// backing store and loads them again on demand, NeuronStateCache.cpp:22-43;
+// here the unit is a whole simulation, whose device memory a server needs
+// for other jobs)
+// ---------------------------------------------------------------------------
+
+// Every device pointer of the engine that points into `from[i]` is moved to
+// the same offset in `to[i]`.
+void remap_engine(Engine& e, const DeviceBuffers& from, const DeviceBuffers& to) {
+    auto fix = [&](auto& ptr) {
+        if (ptr == nullptr) return;
+        const auto* c = reinterpret_cast<const unsigned char*>(ptr);
+        for (size_t i = 0; i < from.size(); ++i) {
+            const auto* b = static_cast<const unsigned char*>(from[i].p);
+            if (b != nullptr && c >= b && c < b + from[i].bytes) {
+                ptr = reinterpret_cast<std::remove_reference_t<decltype(ptr)>>(static_cast<unsigned char*>(to[i].p) +
+                                                                               (c - b));
+                return;
+            }
+        }
+        throw_fail(SNNCUDA_ERR_DEVICE, "eviction: a device pointer outside the simulation's buffers");
+    };
+    fix(e.in_ptr); fix(e.nparam); fix(e.nrec); fix(e.ntp); fix(e.cand); fix(e.refmeta); fix(e.ring); fix(e.syn);
+    fix(e.lcode); fix(e.pre_base); fix(e.pre_off); fix(e.pre_ev); fix(e.cls_delta); fix(e.wheel);
+    fix(e.slot_count); fix(e.bcnt); fix(e.btot); fix(e.bstart); fix(e.bcur); fix(e.seg_start); fix(e.grp);
+    fix(e.grp_tmp); fix(e.grp_ltgt); fix(e.evin); fix(e.ev_a0); fix(e.fire_bits); fix(e.fire_at);
+    fix(e.fire_tile); fix(e.fire_list); fix(e.fired_tgt); fix(e.fired_cnt); fix(e.xsum); fix(e.xdst);
+    fix(e.xdst_ok); fix(e.raster); fix(e.ts); fix(e.tab.decay); fix(e.tab.ltp); fix(e.tab.ltd);
+}
+
+bool run_complete(snncuda_sim* sim, bool wait);
+
+// Copies the simulation's device state to host memory and frees its device
+// buffers: state buffers whole, the wheel slot by slot up to each slot's
+// event count, per-tick scratch not at all.
+void evict_impl(snncuda_sim* sim) {
+    if (sim->evicted) return;
+    run_complete(sim, true);
+    cudaStream_t st = sim->stream;
+    Engine& e = sim->e;
+    std::vector<uint32_t> counts(e.W);
+    check(cudaMemcpyAsync(counts.data(), e.slot_count, e.W * sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+          "eviction copy");
+    check(cudaStreamSynchronize(st), "eviction synchronize");
+    sim->evicted_data.assign(sim->owned.size(), {});
+    for (size_t i = 0; i < sim->owned.size(); ++i) {
+        const DeviceBuffer& b = sim->owned[i];
+        std::vector<unsigned char>& h = sim->evicted_data[i];
+        if (b.p == nullptr || b.kind == BufKind::kScratch || b.kind == BufKind::kZero) continue;
+        if (b.kind == BufKind::kState) {
+            h.resize(b.bytes);
+            check(cudaMemcpyAsync(h.data(), b.p, b.bytes, cudaMemcpyDeviceToHost, st), "eviction copy");
+            continue;
+        }
+        size_t total = 0;  // the wheel: the live prefix of every slot
+        for (uint32_t c : counts) total += c;
+        h.resize(total * 8);
+        size_t at = 0;
+        for (uint32_t slot = 0; slot < e.W; ++slot) {
+            if (counts[slot] == 0) continue;
+            check(cudaMemcpyAsync(h.data() + at * 8, static_cast<unsigned char*>(b.p) + slot * e.slot_cap * 8,
+                                  counts[slot] * 8ull, cudaMemcpyDeviceToHost, st), "eviction copy");
+            at += counts[slot];
+        }
+    }
+    check(cudaStreamSynchronize(st), "eviction synchronize");
+    sim->drop_graphs();
+    for (DeviceBuffer& b : sim->owned)
+        if (b.p) check(cudaFreeAsync(b.p, st), "eviction free");
+    for (void** p : {reinterpret_cast<void**>(&sim->far_ev), reinterpret_cast<void**>(&sim->far_idx),
+                     reinterpret_cast<void**>(&sim->inj_ev), reinterpret_cast<void**>(&sim->inj_slot),
+                     reinterpret_cast<void**>(&sim->inj_off)}) {
+        if (*p) check(cudaFreeAsync(*p, st), "eviction free");
+        *p = nullptr;
+    }
+    sim->far_ev_cap = sim->far_idx_cap = sim->inj_cap = sim->inj_groups_cap = 0;
+    e.far_ev = nullptr;
+    e.far_idx = nullptr;
+    check(cudaStreamSynchronize(st), "eviction synchronize");
+    sim->evicted = true;
+    sim->evictions += 1;
+}
+
+// Allocates the simulation's device buffers again, copies the evicted state
+// back and points the engine at the new buffers.
+void restore_impl(snncuda_sim* sim) {
+    if (!sim->evicted) return;
+    cudaStream_t st = sim->stream;
+    Engine& e = sim->e;
+    DeviceBuffers fresh = sim->owned;
+    size_t made = 0;
+    try {
+        for (; made < fresh.size(); ++made) {
+            DeviceBuffer& b = fresh[made];
+            if (b.p == nullptr) continue;
+            b.p = nullptr;
+            check(cudaMallocAsync(&b.p, b.bytes, st), "restore allocation");
+        }
+    } catch (...) {
+        for (size_t i = 0; i < made; ++i)
+            if (fresh[i].p && sim->owned[i].p) cudaFreeAsync(fresh[i].p, st);
+        cudaStreamSynchronize(st);
+        throw;
+    }
+    std::vector<uint32_t> counts;
+    for (size_t i = 0; i < fresh.size(); ++i) {
+        const DeviceBuffer& b = fresh[i];
+        const std::vector<unsigned char>& h = sim->evicted_data[i];
+        if (b.p == nullptr || b.kind != BufKind::kState) continue;
+        check(cudaMemcpyAsync(b.p, h.data(), b.bytes, cudaMemcpyHostToDevice, st), "restore copy");
+        if (sim->owned[i].p == e.slot_count) {
+            counts.resize(e.W);
+            std::memcpy(counts.data(), h.data(), e.W * sizeof(uint32_t));
+        }
+    }
+    for (size_t i = 0; i < fresh.size(); ++i) {
+        if (fresh[i].p == nullptr || fresh[i].kind != BufKind::kWheel) continue;
+        const std::vector<unsigned char>& h = sim->evicted_data[i];
+        size_t at = 0;
+        for (uint32_t slot = 0; slot < e.W && slot < counts.size(); ++slot) {
+            if (counts[slot] == 0) continue;
+            check(cudaMemcpyAsync(static_cast<unsigned char*>(fresh[i].p) + slot * e.slot_cap * 8,
+                                  h.data() + at * 8, counts[slot] * 8ull, cudaMemcpyHostToDevice, st),
+                  "restore copy");
+            at += counts[slot];
+        }
+    }
+    // scratch that reads zero between ticks comes back as zeros; the rest of
+    // the scratch needs no contents
+    for (const DeviceBuffer& b : fresh)
+        if (b.p != nullptr && b.kind == BufKind::kZero) check(cudaMemsetAsync(b.p, 0, b.bytes, st), "restore zero");
+    remap_engine(e, sim->owned, fresh);
+    sim->owned = std::move(fresh);
+    check(cudaStreamSynchronize(st), "restore synchronize");
+    sim->evicted_data.clear();
+    sim->evicted = false;
+    sim->ensure_far(1, 2);
+}
+
+// ---------------------------------------------------------------------------
+// wheel slot capacity and launch shapes
+// ---------------------------------------------------------------------------
+
+// Sizes that follow from the wheel slot capacity.
+struct SlotSizes {
+    uint64_t slot_cap, fire_cap, xblocks, bit_words, fire_tiles;
+};
+SlotSizes slot_sizes(uint64_t slot_cap, uint32_t N) {
+    SlotSizes z;
+    z.slot_cap = slot_cap;
+    z.fire_cap = std::min<uint64_t>(slot_cap, std::max<uint64_t>(65536, 4ull * N));
+    z.xblocks = (z.fire_cap + kExpandFires - 1) / kExpandFires;
+    z.bit_words = slot_cap / 32;
+    z.fire_tiles = (z.bit_words + 255) / 256;
+    return z;
+}
+
+// Gives the wheel slots capacity `cap` (a multiple of 32 that holds every
+// slot's queued events): the wheel moves slot by slot into a new buffer,
+// the per-tick buffers sized by the capacity are allocated again (zeroed
+// where they must read zero between ticks), and the graphs are recaptured
+// on the next run.
+void resize_slots(snncuda_sim* sim, uint64_t cap) {
+    Engine& e = sim->e;
+    cudaStream_t st = sim->stream;
+    run_complete(sim, true);
+    const std::vector<uint32_t> counts = sim->d2h(e.slot_count, e.W);
+    for (uint32_t c : counts)
+        if (c > cap) throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "a wheel slot holds more events than the new capacity");
+    const SlotSizes z = slot_sizes(cap, sim->N);
+    const uint32_t D = std::max<uint32_t>(e.D, 1);
+    auto entry = [&](const void* p) -> DeviceBuffer& {
+        for (DeviceBuffer& b : sim->owned)
+            if (b.p == p) return b;
+        throw_fail(SNNCUDA_ERR_DEVICE, "resize: unknown buffer");
+    };
+    auto realloc_buf = [&](auto*& field, size_t bytes) {
+        DeviceBuffer& b = entry(field);
+        void* fresh = nullptr;
+        check(cudaMallocAsync(&fresh, bytes, st), "resize allocation");
+        if (b.kind == BufKind::kZero) check(cudaMemsetAsync(fresh, 0, bytes, st), "resize zero");
+        if (b.kind == BufKind::kWheel) {
+            for (uint32_t slot = 0; slot < e.W; ++slot)
+                if (counts[slot])
+                    check(cudaMemcpyAsync(static_cast<unsigned long long*>(fresh) + slot * cap,
+                                          e.wheel + slot * e.slot_cap, counts[slot] * 8ull, cudaMemcpyDeviceToDevice,
+                                          st), "resize copy");
+        }
+        check(cudaFreeAsync(b.p, st), "resize free");
+        b.p = fresh;
+        b.bytes = bytes;
+        field = static_cast<std::remove_reference_t<decltype(field)>>(fresh);
+    };
+    sim->drop_graphs();
+    realloc_buf(e.wheel, static_cast<size_t>(e.W) * cap * 8);
+    realloc_buf(e.grp, cap * 8);
+    realloc_buf(e.grp_tmp, cap * 8);
+    realloc_buf(e.grp_ltgt, cap * 2);
+    realloc_buf(e.evin, cap * sizeof(EvIn));
+    realloc_buf(e.ev_a0, cap * sizeof(SynA));
+    realloc_buf(e.fire_at, cap * 4);
+    realloc_buf(e.fire_bits, std::max<uint64_t>(z.bit_words, 1) * 4);
+    realloc_buf(e.fire_tile, (z.fire_tiles + 2) * 4);
+    realloc_buf(e.fire_list, z.fire_cap * 4);
+    realloc_buf(e.xsum, z.xblocks * D * 4);
+    realloc_buf(e.xdst, z.xblocks * D * 8);
+    e.slot_cap = cap;
+    e.fire_cap = static_cast<uint32_t>(z.fire_cap);
+    e.fire_tiles_cap = static_cast<uint32_t>(z.fire_tiles);
+    e.grid_fire = static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>(z.fire_tiles, sim->sms * 8ull)));
+    sim->config.slot_event_capacity = cap;
+    check(cudaStreamSynchronize(st), "resize synchronize");
+}
+
+void run_enqueue(snncuda_sim* sim, uint64_t T, snncuda_profile* prof);
+void resident(snncuda_sim* sim);
+
+// Device time per tick of the next `ticks` ticks (they are the simulation's
+// own ticks: launch shapes do not change results).
+double probe_ms_per_tick(snncuda_sim* sim, uint64_t ticks) {
+    cudaEvent_t a = nullptr, b = nullptr;
+    check(cudaEventCreate(&a), "event");
+    check(cudaEventCreate(&b), "event");
+    float ms = 0.0F;
+    cudaError_t err = cudaEventRecord(a, sim->stream);
+    try {
+        // the first launch of freshly captured graphs is not timed
+        run_enqueue(sim, sim->next_tick + std::min<uint64_t>(ticks, sim->ticks_per_graph) - 1, nullptr);
+        run_complete(sim, true);
+        if (err == cudaSuccess) err = cudaEventRecord(a, sim->stream);
+        run_enqueue(sim, sim->next_tick + ticks - 1, nullptr);
+        if (err == cudaSuccess) err = cudaEventRecord(b, sim->stream);
+        run_complete(sim, true);
+    } catch (...) {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        throw;
+    }
+    if (err == cudaSuccess) err = cudaEventSynchronize(b);
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    check(err, "probe timing");
+    return ms / static_cast<double>(ticks);
+}
+
+// Picks the launch shapes by timed probes of the next ticks (coordinate
+// descent over k_events, k_process, grouping and k_temporal blocks per SM
+// and the ticks per captured graph), then sizes the wheel slots to twice the
+// largest due list seen plus 2^16 events when that is smaller than the
+// current capacity.
+void autotune_impl(snncuda_sim* sim, uint64_t probe_ticks, snncuda_tuning* out) {
+    if (probe_ticks == 0) throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "probe_ticks must be nonzero");
+    resident(sim);
+    run_complete(sim, true);
+    Engine& e = sim->e;
+    const uint32_t sms = sim->sms;
+    const uint32_t walk_max = static_cast<uint32_t>(std::max<uint64_t>(1, (static_cast<uint64_t>(sim->N) + 63) / 64));
+    uint32_t probes = 0;
+    double best = probe_ms_per_tick(sim, probe_ticks);
+    ++probes;
+    const double first = best;
+    struct Knob {
+        uint32_t* field;
+        std::vector<uint32_t> cands;
+    };
+    std::vector<Knob> knobs = {
+        {&e.grid_events, {sms * 4, sms * 8, sms * 16}},
+        {&e.grid_walk, {std::min(walk_max, sms * 2), std::min(walk_max, sms * 3), std::min(walk_max, sms * 4),
+                        std::min(walk_max, sms * 6)}},
+        {&e.grid_bucket, {sms, sms * 2, sms * 4}},
+        {&e.grid_process, {sms * 2, sms * 4, sms * 8}},
+        {&sim->ticks_per_graph, {8, 16, 32}},
+    };
+    for (Knob& k : knobs) {
+        const uint32_t keep = *k.field;
+        uint32_t pick = keep;
+        for (uint32_t c : k.cands) {
+            if (c == keep || c == 0) continue;
+            *k.field = c;
+            sim->drop_graphs();
+            const double ms = probe_ms_per_tick(sim, probe_ticks);
+            ++probes;
+            if (ms < best * 0.98) {
+                best = ms;
+                pick = c;
+            }
+        }
+        *k.field = pick;
+        sim->drop_graphs();
+    }
+    const TickState ts = sim->read_ts();
+    const uint64_t want = (std::max<uint64_t>(65536, 2 * ts.max_slot_events + 65536) + 31) & ~31ull;
+    if (want < e.slot_cap * 3 / 4) resize_slots(sim, want);
+    const double last = probe_ms_per_tick(sim, probe_ticks);
+    ++probes;
+    if (out) {
+        out->grid_events = e.grid_events;
+        out->grid_walk = e.grid_walk;
+        out->grid_bucket = e.grid_bucket;
+        out->grid_temporal = e.grid_process;
+        out->ticks_per_graph = sim->ticks_per_graph;
+        out->block_threads = 256;
+        out->slot_event_capacity = e.slot_cap;
+        out->max_slot_events = ts.max_slot_events;
+        out->ms_per_tick_before = first;
+        out->ms_per_tick_after = last;
+        out->probes = probes;
+        out->probe_ticks = probe_ticks;
+    }
+}
+
+// The simulation's state on the device (restored on demand, as the
+// reference's cache loads an evicted neuron state on its next use).
+void resident(snncuda_sim* sim) {
+    if (sim->evicted) restore_impl(sim);
 }
 
 int status_to_error(uint32_t status, std::string& msg) {
@@ -540,7 +890,7 @@ void sort_pending(snncuda_sim* sim) {
 
 // Enqueues ticks next_tick .. T on the simulation's stream and returns
 // without waiting; run_complete() waits and checks the device status.
-void run_enqueue(snncuda_sim* sim, uint64_t T, snncuda_profile* prof = nullptr) {
+void run_enqueue(snncuda_sim* sim, uint64_t T, snncuda_profile* prof) {
     const uint64_t p = sim->next_tick;
     if (sim->run_in_flight) throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "a run is already in flight");
     if (T < p) return;
@@ -641,12 +991,12 @@ void run_enqueue(snncuda_sim* sim, uint64_t T, snncuda_profile* prof = nullptr) 
         prof->touched_targets += after.touched_total - before.touched_total;
         ticks = 0;
     }
-    if (ticks >= static_cast<uint64_t>(snncuda_sim::kTicksPerGraph) && sim->graph_many == nullptr)
-        sim->graph_many = sim->capture(snncuda_sim::kTicksPerGraph);
+    if (ticks >= sim->ticks_per_graph && sim->graph_many == nullptr)
+        sim->graph_many = sim->capture(static_cast<int>(sim->ticks_per_graph));
     if (ticks > 0 && sim->graph_one == nullptr) sim->graph_one = sim->capture(1);
-    while (ticks >= static_cast<uint64_t>(snncuda_sim::kTicksPerGraph)) {
+    while (ticks >= sim->ticks_per_graph) {
         check(cudaGraphLaunch(sim->graph_many, st), "graph launch");
-        ticks -= snncuda_sim::kTicksPerGraph;
+        ticks -= sim->ticks_per_graph;
     }
     while (ticks > 0) {
         check(cudaGraphLaunch(sim->graph_one, st), "graph launch");
@@ -854,7 +1204,10 @@ int snncuda_sim_inject(snncuda_sim* sim, uint64_t count, const uint32_t* neurons
 int snncuda_sim_run_until(snncuda_sim* sim, uint64_t inclusive_tick) {
     if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
     if (sim->poisoned) return set_error(SNNCUDA_ERR_POISONED, "simulation poisoned by an earlier device error");
-    const int rc = guarded([&] { run_impl(sim, inclusive_tick); });
+    const int rc = guarded([&] {
+        resident(sim);
+        run_impl(sim, inclusive_tick);
+    });
     if (rc == SNNCUDA_ERR_DEVICE) sim->poisoned = true;
     return rc;
 }
@@ -862,6 +1215,7 @@ int snncuda_sim_run_until(snncuda_sim* sim, uint64_t inclusive_tick) {
 static int set_flag(snncuda_sim* sim, size_t offset, int32_t v) {
     if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
     return guarded([&] {
+        resident(sim);
         check(cudaMemcpyAsync(reinterpret_cast<char*>(sim->e.ts) + offset, &v, 4, cudaMemcpyHostToDevice,
                               sim->stream), "toggle");
         check(cudaStreamSynchronize(sim->stream), "toggle");
@@ -879,6 +1233,7 @@ int snncuda_sim_set_temporal_learning(snncuda_sim* sim, int32_t enabled) {
 int snncuda_sim_counters(snncuda_sim* sim, snncuda_counters* out) {
     if (sim == nullptr || out == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
     return guarded([&] {
+        resident(sim);
         const TickState ts = sim->read_ts();
         const std::vector<uint32_t> counts = sim->d2h(sim->e.slot_count, sim->e.W);
         uint64_t pending = sim->pending.size() - sim->pend_head;
@@ -926,7 +1281,10 @@ static void read_neurons_range(snncuda_sim* sim, uint32_t n0, uint32_t n1, const
 
 int snncuda_sim_read_neurons(snncuda_sim* sim, const snncuda_neuron_state* o) {
     if (sim == nullptr || o == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
-    return guarded([&] { read_neurons_range(sim, 0, sim->N, o); });
+    return guarded([&] {
+        resident(sim);
+        read_neurons_range(sim, 0, sim->N, o);
+    });
 }
 
 // Synapses of Connectome indices [c0, c1), whose target-major slots are
@@ -955,13 +1313,17 @@ static void read_synapses_range(snncuda_sim* sim, uint64_t c0, uint64_t c1, uint
 
 int snncuda_sim_read_synapses(snncuda_sim* sim, const snncuda_synapse_state* o) {
     if (sim == nullptr || o == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
-    return guarded([&] { read_synapses_range(sim, 0, sim->S, 0, sim->S, o); });
+    return guarded([&] {
+        resident(sim);
+        read_synapses_range(sim, 0, sim->S, 0, sim->S, o);
+    });
 }
 
 int snncuda_sim_read_pattern(snncuda_sim* sim, int32_t kind, uint64_t index, uint64_t which, uint32_t* values,
                              uint64_t capacity, uint64_t* len) {
     if (sim == nullptr || len == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
     return guarded([&] {
+        resident(sim);
         std::vector<uint32_t> v;
         if (kind == 0 || kind == 1) {
             if (index >= sim->N) throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "neuron out of range");
@@ -1074,6 +1436,7 @@ static void digest_range(snncuda_sim* sim, const HostState& h, uint32_t n0, uint
 int snncuda_sim_state_digest(snncuda_sim* sim, uint64_t* neuron_digest, uint64_t* synapse_digest) {
     if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
     return guarded([&] {
+        resident(sim);
         const HostState h = fetch_all(sim, true);
         digest_range(sim, h, 0, sim->N, 0, sim->S, neuron_digest, synapse_digest);
     });
@@ -1082,7 +1445,10 @@ int snncuda_sim_state_digest(snncuda_sim* sim, uint64_t* neuron_digest, uint64_t
 int snncuda_sim_profile(snncuda_sim* sim, uint64_t inclusive_tick, snncuda_profile* out) {
     if (sim == nullptr || out == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
     if (sim->poisoned) return set_error(SNNCUDA_ERR_POISONED, "simulation poisoned by an earlier device error");
-    const int rc = guarded([&] { run_impl(sim, inclusive_tick, out); });
+    const int rc = guarded([&] {
+        resident(sim);
+        run_impl(sim, inclusive_tick, out);
+    });
     if (rc == SNNCUDA_ERR_DEVICE) sim->poisoned = true;
     return rc;
 }
@@ -1091,24 +1457,98 @@ const char* snncuda_kernel_name(int32_t index) { return kernel_name(index); }
 
 namespace {
 
+// Device checksums of a range of neurons and target-major synapses.
+void checksum_range(snncuda_sim* sim, uint32_t n0, uint32_t n1, uint64_t t0, uint64_t t1, uint64_t* neuron_sum,
+                    uint64_t* synapse_sum) {
+    cudaStream_t st = sim->stream;
+    unsigned long long* d = nullptr;
+    check(cudaMallocAsync(&d, 2 * sizeof(unsigned long long), st), "device allocation");
+    unsigned long long c[2] = {};
+    cudaError_t err = cudaMemsetAsync(d, 0, sizeof(c), st);
+    if (err == cudaSuccess) {
+        launch_checksum(sim->e, n0, n1, t0, t1, d, st);
+        err = cudaGetLastError();
+    }
+    if (err == cudaSuccess) err = cudaMemcpyAsync(c, d, sizeof(c), cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d, st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+    check(err, "state checksum");
+    if (neuron_sum) *neuron_sum = c[0];
+    if (synapse_sum) *synapse_sum = c[1];
+}
+
+}  // namespace
+
+int snncuda_sim_state_checksum(snncuda_sim* sim, uint64_t* neuron_sum, uint64_t* synapse_sum) {
+    if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
+    return guarded([&] {
+        resident(sim);
+        checksum_range(sim, 0, sim->N, 0, sim->S, neuron_sum, synapse_sum);
+    });
+}
+
+int snncuda_sim_autotune(snncuda_sim* sim, uint64_t probe_ticks, snncuda_tuning* out) {
+    if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
+    if (sim->poisoned) return set_error(SNNCUDA_ERR_POISONED, "simulation poisoned by an earlier device error");
+    const int rc = guarded([&] { autotune_impl(sim, probe_ticks, out); });
+    if (rc == SNNCUDA_ERR_DEVICE) sim->poisoned = true;
+    return rc;
+}
+
+int snncuda_sim_set_slot_capacity(snncuda_sim* sim, uint64_t capacity) {
+    if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
+    if (capacity == 0 || capacity >= (1ull << 31))
+        return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "slot capacity must be in [1, 2^31)");
+    return guarded([&] {
+        resident(sim);
+        resize_slots(sim, (capacity + 31) & ~31ull);
+    });
+}
+
+int snncuda_sim_evict(snncuda_sim* sim) {
+    if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
+    return guarded([&] { evict_impl(sim); });
+}
+
+int snncuda_sim_restore(snncuda_sim* sim) {
+    if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
+    return guarded([&] { restore_impl(sim); });
+}
+
+int snncuda_sim_residency(snncuda_sim* sim, int32_t* resident_out, uint64_t* evictions) {
+    if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
+    if (resident_out) *resident_out = sim->evicted ? 0 : 1;
+    if (evictions) *evictions = sim->evictions;
+    return SNNCUDA_OK;
+}
+
+namespace {
+
 // Scratch of one grouping call (device pointers).
 struct GroupScratch {
-    uint32_t* cnt;
-    uint32_t* tiles;      // tile_sum then tile_nz, (tiles + 2) each
-    uint32_t* touched;
-    uint32_t* seg_len;
-    unsigned long long* grp;
-    uint32_t* evt_tgt;
+    uint32_t* bcnt;       // kGroupGrid x buckets
+    uint32_t* btot;       // buckets
+    uint32_t* bstart;     // buckets + 1
+    uint32_t* bcur;       // buckets
+    unsigned long long* grp_tmp;  // count
+    uint16_t* grp_ltgt;   // count
     uint32_t* slot_count;
     TickState* ts;
 };
 
-size_t group_tiles(uint32_t n) { return (static_cast<size_t>(n) + kScanTile - 1) / kScanTile + 2; }
+// Blocks of the grouping entry points' counting and placing kernels (fixed,
+// so the static scratch has a fixed size).
+constexpr uint32_t kGroupGrid = 256;
 
-// The tick's grouping kernels (k_hist .. k_segsort) on a caller's event
-// buffer seen as a one-slot wheel.  Scratch must hold neuron_count (cnt,
-// touched, seg_len), group_tiles() (tiles, twice) and count (grp, evt_tgt)
-// entries; cnt and the tick state are cleared here.
+uint32_t group_buckets(uint32_t neuron_count) {
+    const uint32_t shift = bucket_shift_for(neuron_count);
+    return static_cast<uint32_t>(std::max<uint64_t>(1, (static_cast<uint64_t>(neuron_count) + (1u << shift) - 1) >> shift));
+}
+
+// The tick's grouping kernels (k_bcount .. k_bsort) on a caller's event
+// buffer seen as a one-slot wheel.  Scratch sizes: kGroupGrid x
+// group_buckets() counts, group_buckets() (+1) bucket totals, starts and
+// cursors, `count` entries of bucket-ordered events and their targets.
 void group_run(const uint64_t* events, uint32_t count, uint32_t neuron_count, uint64_t* grouped,
                uint32_t* segment_start, cudaStream_t st, const GroupScratch& sc) {
     int dev = 0, sms = 0;
@@ -1121,25 +1561,25 @@ void group_run(const uint64_t* events, uint32_t count, uint32_t neuron_count, ui
     e.slot_cap = count;
     e.wheel = const_cast<unsigned long long*>(reinterpret_cast<const unsigned long long*>(events));
     e.slot_count = sc.slot_count;
-    e.cnt = sc.cnt;
+    e.bucket_shift = bucket_shift_for(neuron_count);
+    e.nbuckets = group_buckets(neuron_count);
+    e.grid_bucket = kGroupGrid;
+    e.bcnt = sc.bcnt;
+    e.btot = sc.btot;
+    e.bstart = sc.bstart;
+    e.bcur = sc.bcur;
     e.seg_start = segment_start;
-    e.tile_sum = sc.tiles;
-    e.tile_nz = sc.tiles + group_tiles(neuron_count);
-    e.touched = sc.touched;
-    e.grp = sc.grp;
-    e.grp_sorted = reinterpret_cast<unsigned long long*>(grouped);
-    e.evt_tgt = sc.evt_tgt;
-    e.seg_len = sc.seg_len;
+    e.grp = reinterpret_cast<unsigned long long*>(grouped);
+    e.grp_tmp = sc.grp_tmp;
+    e.grp_ltgt = sc.grp_ltgt;
     e.ts = sc.ts;
     e.grid_wide = static_cast<uint32_t>(std::max(1, sms * 2));
-    check(cudaMemsetAsync(sc.cnt, 0, sizeof(uint32_t) * std::max<uint32_t>(neuron_count, 1), st), "memset");
+    configure_kernels();
+    check(cudaMemsetAsync(sc.btot, 0, sizeof(uint32_t) * e.nbuckets, st), "memset");
     check(cudaMemsetAsync(sc.ts, 0, sizeof(TickState), st), "memset");
-    check(cudaMemsetAsync(sc.tiles, 0, sizeof(uint32_t) * 2 * group_tiles(neuron_count), st), "memset");
     check(cudaMemcpyAsync(sc.slot_count, &count, sizeof(uint32_t), cudaMemcpyHostToDevice, st), "count");
     launch_group(e, st);
     check(cudaGetLastError(), "group launch");
-    check(cudaMemcpyAsync(segment_start + neuron_count, &count, sizeof(uint32_t), cudaMemcpyHostToDevice, st),
-          "segment end");
     TickState ts;
     check(cudaMemcpyAsync(&ts, sc.ts, sizeof(ts), cudaMemcpyDeviceToHost, st), "status");
     check(cudaStreamSynchronize(st), "group synchronize");
@@ -1154,18 +1594,19 @@ int snncuda_group_events(const uint64_t* events, uint32_t count, uint32_t neuron
         return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null array");
     if (count > 0 && events < grouped + count && grouped < events + count)
         return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "events and grouped overlap");
-    if (count >= (1u << 31) || neuron_count >= (1u << 31))
-        return set_error(SNNCUDA_ERR_UNSUPPORTED, "at most 2^31-1 events and neurons");
+    if (count >= (1u << 31)) return set_error(SNNCUDA_ERR_UNSUPPORTED, "at most 2^31-1 events");
+    if (bucket_shift_for(neuron_count) == 0) return set_error(SNNCUDA_ERR_UNSUPPORTED, "at most 2^28 neurons");
     cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
     std::vector<void*> owned;
     const int rc = guarded([&] {
+        const uint32_t buckets = group_buckets(neuron_count);
         GroupScratch sc;
-        sc.cnt = dalloc<uint32_t>(owned, neuron_count);
-        sc.tiles = dalloc<uint32_t>(owned, 2 * group_tiles(neuron_count));
-        sc.touched = dalloc<uint32_t>(owned, neuron_count);
-        sc.seg_len = dalloc<uint32_t>(owned, neuron_count);
-        sc.grp = dalloc<unsigned long long>(owned, count);
-        sc.evt_tgt = dalloc<uint32_t>(owned, count);
+        sc.bcnt = dalloc<uint32_t>(owned, static_cast<size_t>(kGroupGrid) * buckets);
+        sc.btot = dalloc<uint32_t>(owned, buckets);
+        sc.bstart = dalloc<uint32_t>(owned, static_cast<size_t>(buckets) + 1);
+        sc.bcur = dalloc<uint32_t>(owned, buckets);
+        sc.grp_tmp = dalloc<unsigned long long>(owned, count);
+        sc.grp_ltgt = dalloc<uint16_t>(owned, count);
         sc.slot_count = dalloc<uint32_t>(owned, 1);
         sc.ts = dalloc<TickState>(owned, 1);
         group_run(events, count, neuron_count, grouped, segment_start, st, sc);
@@ -1177,18 +1618,21 @@ int snncuda_group_events(const uint64_t* events, uint32_t count, uint32_t neuron
 
 namespace {
 
-// Static scratch of snncuda_group_events_static: counters, tiles and groups
-// for at most kStaticEvents events over kStaticNeurons neurons.
+// Static scratch of snncuda_group_events_static: bucket counters and the
+// bucket-ordered events for at most kStaticEvents events over kStaticNeurons
+// neurons (about 11 MB).
 constexpr size_t kStaticEvents = SNNCUDA_GROUP_STATIC_MAX_EVENTS;
 constexpr size_t kStaticNeurons = SNNCUDA_GROUP_STATIC_MAX_NEURONS;
+constexpr size_t kStaticBuckets = (kStaticNeurons + 255) / 256;  // bucket_shift_for(2^18) == 8
+static_assert(kStaticBuckets <= kMaxBuckets, "static grouping buckets");
 constexpr size_t align256(size_t b) { return (b + 255) / 256 * 256; }
-constexpr size_t kOffCnt = 0;
-constexpr size_t kOffTouched = kOffCnt + align256(kStaticNeurons * 4);
-constexpr size_t kOffSegLen = kOffTouched + align256(kStaticNeurons * 4);
-constexpr size_t kOffTiles = kOffSegLen + align256(kStaticNeurons * 4);
-constexpr size_t kOffGrp = kOffTiles + align256(2 * ((kStaticNeurons + kScanTile - 1) / kScanTile + 2) * 4);
-constexpr size_t kOffEvtTgt = kOffGrp + align256(kStaticEvents * 8);
-constexpr size_t kOffSlot = kOffEvtTgt + align256(kStaticEvents * 4);
+constexpr size_t kOffBcnt = 0;
+constexpr size_t kOffBtot = kOffBcnt + align256(kGroupGrid * kStaticBuckets * 4);
+constexpr size_t kOffBstart = kOffBtot + align256(kStaticBuckets * 4);
+constexpr size_t kOffBcur = kOffBstart + align256((kStaticBuckets + 1) * 4);
+constexpr size_t kOffGrpTmp = kOffBcur + align256(kStaticBuckets * 4);
+constexpr size_t kOffLtgt = kOffGrpTmp + align256(kStaticEvents * 8);
+constexpr size_t kOffSlot = kOffLtgt + align256(kStaticEvents * 2);
 constexpr size_t kOffTs = kOffSlot + 256;
 constexpr size_t kStaticBytes = kOffTs + align256(sizeof(TickState));
 
@@ -1235,12 +1679,12 @@ int snncuda_group_events_static(const uint64_t* events, uint32_t count, uint32_t
     const int rc = guarded([&] {
         unsigned char* base = static_scratch(st);
         GroupScratch sc;
-        sc.cnt = reinterpret_cast<uint32_t*>(base + kOffCnt);
-        sc.touched = reinterpret_cast<uint32_t*>(base + kOffTouched);
-        sc.seg_len = reinterpret_cast<uint32_t*>(base + kOffSegLen);
-        sc.tiles = reinterpret_cast<uint32_t*>(base + kOffTiles);
-        sc.grp = reinterpret_cast<unsigned long long*>(base + kOffGrp);
-        sc.evt_tgt = reinterpret_cast<uint32_t*>(base + kOffEvtTgt);
+        sc.bcnt = reinterpret_cast<uint32_t*>(base + kOffBcnt);
+        sc.btot = reinterpret_cast<uint32_t*>(base + kOffBtot);
+        sc.bstart = reinterpret_cast<uint32_t*>(base + kOffBstart);
+        sc.bcur = reinterpret_cast<uint32_t*>(base + kOffBcur);
+        sc.grp_tmp = reinterpret_cast<unsigned long long*>(base + kOffGrpTmp);
+        sc.grp_ltgt = reinterpret_cast<uint16_t*>(base + kOffLtgt);
         sc.slot_count = reinterpret_cast<uint32_t*>(base + kOffSlot);
         sc.ts = reinterpret_cast<TickState*>(base + kOffTs);
         group_run(events, count, neuron_count, grouped, segment_start, st, sc);
@@ -1254,6 +1698,7 @@ int snncuda_group_events_static(const uint64_t* events, uint32_t count, uint32_t
 int snncuda_sim_read_raster(snncuda_sim* sim, uint64_t first, uint64_t count, uint64_t* ticks, uint32_t* neurons) {
     if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
     return guarded([&] {
+        resident(sim);
         const TickState ts = sim->read_ts();
         const uint64_t have = std::min<uint64_t>(ts.raster_count, sim->e.raster_cap);
         if (first + count > have) throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "raster range out of bounds");
@@ -1269,6 +1714,7 @@ int snncuda_sim_read_raster(snncuda_sim* sim, uint64_t first, uint64_t count, ui
 int snncuda_sim_recognition(snncuda_sim* sim, uint64_t* neuron_matches, uint64_t* synapse_code_matches) {
     if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
     return guarded([&] {
+        resident(sim);
         cudaStream_t st = sim->stream;
         unsigned long long* d = nullptr;
         check(cudaMallocAsync(&d, 5 * sizeof(unsigned long long), st), "device allocation");
@@ -1500,6 +1946,20 @@ int snncuda_batch_state_digests(snncuda_batch* b, uint64_t* neuron_digests, uint
     });
 }
 
+int snncuda_batch_state_checksums(snncuda_batch* b, uint64_t* neuron_sums, uint64_t* synapse_sums) {
+    if (b == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null batch");
+    return guarded([&] {
+        for (uint32_t i = 0; i < b->count; ++i)
+            checksum_range(b->sim, b->nbase[i], b->nbase[i + 1], b->tm_begin(i), b->tm_end(i),
+                           neuron_sums ? neuron_sums + i : nullptr, synapse_sums ? synapse_sums + i : nullptr);
+    });
+}
+
+int snncuda_batch_autotune(snncuda_batch* b, uint64_t probe_ticks, snncuda_tuning* out) {
+    if (b == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null batch");
+    return snncuda_sim_autotune(b->sim, probe_ticks, out);
+}
+
 int snncuda_batch_read_raster(snncuda_batch* b, uint32_t i, uint64_t first, uint64_t count, uint64_t* ticks,
                               uint32_t* neurons) {
     if (b == nullptr || i >= b->count) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "bad argument");
@@ -1557,8 +2017,10 @@ static uint64_t estimate_bytes_impl(const snncuda_network* net, const snncuda_co
     if (slot_cap == 0) slot_cap = std::min<uint64_t>(1ull << 27, std::max<uint64_t>(1ull << 16, pre_total / 8));
     const uint64_t fire_cap = std::min<uint64_t>(slot_cap, std::max<uint64_t>(65536, 4ull * N));
     const uint64_t lcode = refs_max > 1 ? 2ull * S * refs_max * kMaxExpected : 0;
+    // grouping: bucket counters of up to 512 chunks
+    const uint64_t buckets = (N + 255) / 256 < kMaxBuckets ? (N + 255) / 256 + 1 : kMaxBuckets;
     const uint64_t persistent = 64 * S + 8 * S + 8 * pre_total + neuron_bytes + lcode +
-                                W * slot_cap * 8 + slot_cap * (8 + 8 + 16 + 32 + 4 + 1) +
+                                W * slot_cap * 8 + slot_cap * (8 + 8 + 2 + 16 + 32 + 4 + 1) + 512 * 4 * buckets +
                                 fire_cap * 4 + (fire_cap / 8 + 1) * 12 * std::max<uint64_t>(D, 1) +
                                 16 * cfg.raster_capacity + (16u << 20);
     const uint64_t transient = S * (23 + 8 + 12 + 8) + 4 * (has_codes ? net->code_offset_ptr[S] : 0) +
@@ -1644,6 +2106,7 @@ struct snncuda_server {
     std::vector<std::unique_ptr<ServerJob>> jobs;
     std::deque<uint64_t> queue;     // submitted, not admitted
     std::vector<uint64_t> running;  // created, advanced by step()
+    std::deque<uint64_t> evicted;   // preempted to host memory, waiting to run again
     uint64_t used{0};               // admission estimate of admitted jobs
     uint32_t creating{0};           // admitted, not yet created
     int device{0};
@@ -1777,7 +2240,7 @@ int snncuda_server_step(snncuda_server* sv, uint32_t* active) {
                 finished = true;
                 return;
             }
-            run_enqueue(j.sim, std::min<uint64_t>(j.sim->next_tick + slice, j.ticks) - 1);
+            run_enqueue(j.sim, std::min<uint64_t>(j.sim->next_tick + slice, j.ticks) - 1, nullptr);
         });
         if (rc == SNNCUDA_OK && finished) {
             rc = snncuda_sim_counters(j.sim, &j.res.counters);
@@ -1806,7 +2269,7 @@ int snncuda_server_step(snncuda_server* sv, uint32_t* active) {
             rc = j.res.error;
         }
         if (rc == SNNCUDA_OK && j.ticks > 0)
-            rc = guarded([&] { run_enqueue(j.sim, std::min<uint64_t>(slice, j.ticks) - 1); });
+            rc = guarded([&] { run_enqueue(j.sim, std::min<uint64_t>(slice, j.ticks) - 1, nullptr); });
         if (rc != SNNCUDA_OK) {
             server_finish(sv, j, 3, rc);
             continue;
@@ -1815,11 +2278,55 @@ int snncuda_server_step(snncuda_server* sv, uint32_t* active) {
         sv->running.push_back(id);
     }
     // admit queued jobs in submission order while they fit; the worker
-    // creates them
+    // creates them.  With eviction on, a queued job that does not fit takes
+    // the device memory of running jobs with more remaining work than its
+    // own (synapses x ticks left), largest first, which wait in host memory
+    // until the budget has room again.
+    auto remaining = [](const ServerJob& j, uint64_t done) { return (j.ticks - done) * std::max<uint64_t>(1, j.net.synapse_count); };
     while (!sv->queue.empty() && sv->running.size() + sv->creating < sv->cfg.max_running) {
         const uint64_t id = sv->queue.front();
         ServerJob& j = *sv->jobs_at(id);
-        if (sv->used + j.bytes > sv->cfg.memory_budget_bytes && (!sv->running.empty() || sv->creating > 0)) break;
+        if (sv->used + j.bytes > sv->cfg.memory_budget_bytes && (!sv->running.empty() || sv->creating > 0)) {
+            if (!sv->cfg.evict) break;
+            const uint64_t need = remaining(j, 0);
+            std::vector<std::pair<uint64_t, size_t>> cand;  // (remaining work, index in running)
+            uint64_t freeable = 0;
+            for (size_t i = 0; i < sv->running.size(); ++i) {
+                const ServerJob& r = *sv->jobs_at(sv->running[i]);
+                const uint64_t left = remaining(r, std::min(r.sim->run_target + 1, r.ticks));
+                if (left > need) {
+                    cand.emplace_back(left, i);
+                    freeable += r.bytes;
+                }
+            }
+            // room after evicting every candidate (or nothing left running)?
+            const bool room = sv->used - std::min(sv->used, freeable) + j.bytes <= sv->cfg.memory_budget_bytes ||
+                              (cand.size() == sv->running.size() && sv->creating == 0);
+            if (cand.empty() || !room) break;
+            std::sort(cand.begin(), cand.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+            std::vector<size_t> gone;
+            for (const auto& c : cand) {
+                if (sv->used + j.bytes <= sv->cfg.memory_budget_bytes) break;
+                const uint64_t rid = sv->running[c.second];
+                ServerJob& r = *sv->jobs_at(rid);
+                const int rc = guarded([&] { evict_impl(r.sim); });
+                gone.push_back(c.second);
+                if (rc != SNNCUDA_OK) {
+                    server_finish(sv, r, 3, rc);
+                    continue;
+                }
+                sv->used -= r.bytes;
+                {
+                    std::lock_guard<std::mutex> lock(sv->mu);
+                    r.res.state = 4;
+                    r.res.evictions += 1;
+                }
+                sv->evicted.push_back(rid);
+            }
+            std::sort(gone.rbegin(), gone.rend());
+            for (size_t g : gone) sv->running.erase(sv->running.begin() + static_cast<std::ptrdiff_t>(g));
+            if (sv->used + j.bytes > sv->cfg.memory_budget_bytes && (!sv->running.empty() || sv->creating > 0)) break;
+        }
         sv->queue.pop_front();
         j.res.admitted_s = sv->now();
         sv->used += j.bytes;
@@ -1830,7 +2337,29 @@ int snncuda_server_step(snncuda_server* sv, uint32_t* active) {
         }
         sv->cv.notify_one();
     }
-    if (active) *active = static_cast<uint32_t>(sv->queue.size() + sv->running.size() + sv->creating);
+    // evicted jobs come back, in the order they left, while they fit
+    while (!sv->evicted.empty() && sv->running.size() + sv->creating < sv->cfg.max_running) {
+        const uint64_t id = sv->evicted.front();
+        ServerJob& j = *sv->jobs_at(id);
+        if (sv->used + j.bytes > sv->cfg.memory_budget_bytes && (!sv->running.empty() || sv->creating > 0)) break;
+        sv->evicted.pop_front();
+        sv->used += j.bytes;
+        const int rc = guarded([&] {
+            restore_impl(j.sim);
+            run_enqueue(j.sim, std::min<uint64_t>(j.sim->next_tick + slice, j.ticks) - 1, nullptr);
+        });
+        if (rc != SNNCUDA_OK) {
+            server_finish(sv, j, 3, rc);
+            continue;
+        }
+        {
+            std::lock_guard<std::mutex> lock(sv->mu);
+            j.res.state = 1;
+        }
+        sv->running.push_back(id);
+    }
+    if (active)
+        *active = static_cast<uint32_t>(sv->queue.size() + sv->running.size() + sv->creating + sv->evicted.size());
     return SNNCUDA_OK;
 }
 

@@ -248,6 +248,34 @@ class Simulation:
         _check(self.lib, self.lib.snncuda_sim_state_digest(self.handle, ctypes.byref(a), ctypes.byref(b)))
         return int(a.value), int(b.value)
 
+    def checksum(self) -> tuple:
+        """Device-computed (neuron, synapse) state checksums (GPU engine only)."""
+        a, b = c_uint64(), c_uint64()
+        _check(self.lib, self.lib.snncuda_sim_state_checksum(self.handle, ctypes.byref(a), ctypes.byref(b)))
+        return int(a.value), int(b.value)
+
+    def autotune(self, probe_ticks: int = 20) -> Dict[str, object]:
+        """Pick launch shapes and the wheel-slot capacity from timed probes of
+        the next ticks (engine extension; results are unchanged)."""
+        out = _abi.Tuning()
+        _check(self.lib, self.lib.snncuda_sim_autotune(self.handle, int(probe_ticks), ctypes.byref(out)))
+        return {name: (float(v) if isinstance(v, float) else int(v))
+                for name, v in ((n, getattr(out, n)) for n, _ in _abi.Tuning._fields_)}
+
+    def evict(self) -> None:
+        """Move the state to host memory and free the device memory; the next
+        call that needs the device brings it back (engine extension)."""
+        _check(self.lib, self.lib.snncuda_sim_evict(self.handle))
+
+    def restore(self) -> None:
+        _check(self.lib, self.lib.snncuda_sim_restore(self.handle))
+
+    def residency(self) -> tuple:
+        """(state on the device, times evicted)."""
+        r, n = c_int32(), c_uint64()
+        _check(self.lib, self.lib.snncuda_sim_residency(self.handle, ctypes.byref(r), ctypes.byref(n)))
+        return bool(r.value), int(n.value)
+
     def raster(self, first: int = 0, count: Optional[int] = None) -> tuple:
         """Fire records [first, first+count) as (ticks, neurons); all by default."""
         if count is None:
@@ -346,6 +374,22 @@ class Batch:
                                                               _abi.ptr(b, c_uint64)))
         return [(int(a[i]), int(b[i])) for i in range(self.count)]
 
+    def autotune(self, probe_ticks: int = 20) -> Dict[str, object]:
+        """Simulation.autotune on the batch's tick loop."""
+        out = _abi.Tuning()
+        _check(self.lib, self.lib.snncuda_batch_autotune(self.handle, int(probe_ticks), ctypes.byref(out)))
+        return {name: (float(v) if isinstance(v, float) else int(v))
+                for name, v in ((n, getattr(out, n)) for n, _ in _abi.Tuning._fields_)}
+
+    def checksums(self) -> List[tuple]:
+        """Device-computed (neuron, synapse) checksums of every network, equal
+        to Simulation.checksum() of its solo run (GPU engine only)."""
+        a = np.zeros(max(self.count, 1), np.uint64)
+        b = np.zeros(max(self.count, 1), np.uint64)
+        _check(self.lib, self.lib.snncuda_batch_state_checksums(self.handle, _abi.ptr(a, c_uint64),
+                                                                _abi.ptr(b, c_uint64)))
+        return [(int(a[i]), int(b[i])) for i in range(self.count)]
+
     def raster(self, network: int) -> tuple:
         count = self.counters(network)["raster_count"]
         ticks = np.zeros(count, np.uint64)
@@ -359,13 +403,15 @@ class Batch:
 class Server:
     """Serving: jobs admitted in submission order under a device-memory
     budget and advanced `slice_ticks` at a time, each on its own stream.
-    The caller drives it with step(); a job's network arrays must stay alive
-    until the job is admitted (the Server keeps them until it has finished)."""
+    With `evict`, a queued job that does not fit preempts running jobs with
+    more remaining work; they wait in host memory and resume later.  The
+    caller drives it with step(); submit copies the job's arrays."""
 
     def __init__(self, memory_budget_bytes: int = 0, max_running: int = 0, slice_ticks: int = 0,
-                 digests: bool = False, lib: Optional[ctypes.CDLL] = None):
+                 digests: bool = False, evict: bool = False, lib: Optional[ctypes.CDLL] = None):
         self.lib = lib or backend()
-        cfg = _abi.ServerConfig(memory_budget_bytes, max_running, slice_ticks, 1 if digests else 0)
+        cfg = _abi.ServerConfig(memory_budget_bytes, max_running, slice_ticks, 1 if digests else 0,
+                                1 if evict else 0)
         handle = c_void_p()
         _check(self.lib, self.lib.snncuda_server_create(ctypes.byref(cfg), ctypes.byref(handle)))
         self.handle = handle
@@ -391,7 +437,6 @@ class Server:
         _check(self.lib, self.lib.snncuda_server_submit(
             self.handle, ctypes.byref(net), ctypes.byref(cfg), n.size, _abi.ptr(n, c_uint32), _abi.ptr(t, c_uint64),
             _abi.ptr(w, c_float), int(ticks), ctypes.byref(job)))
-        self._keep[int(job.value)] = (net, keep)
         return int(job.value)
 
     def step(self) -> int:
@@ -402,12 +447,82 @@ class Server:
     def job(self, job_id: int) -> Dict[str, object]:
         r = _abi.JobResult()
         _check(self.lib, self.lib.snncuda_server_job(self.handle, int(job_id), ctypes.byref(r)))
-        if r.state >= 2:
-            self._keep.pop(int(job_id), None)  # finished: its arrays are no longer read
         return {"state": r.state, "error": r.error,
                 "counters": {name: int(getattr(r.counters, name)) for name, _ in _abi.Counters._fields_},
                 "digest": (int(r.neuron_digest), int(r.synapse_digest)), "device_bytes": int(r.device_bytes),
-                "submitted_s": r.submitted_s, "admitted_s": r.admitted_s, "finished_s": r.finished_s}
+                "submitted_s": r.submitted_s, "admitted_s": r.admitted_s, "finished_s": r.finished_s,
+                "evictions": int(r.evictions)}
+
+
+class Readout:
+    """The inference session's readout paths over a network's initial weights
+    (CudaInferenceSession::run_feedforward_batch / run_recurrent_feedforward_batch).
+    Samples are lists of (neuron, weight) pairs (0-based neurons)."""
+
+    def __init__(self, connectome: Connectome, lib: Optional[ctypes.CDLL] = None):
+        connectome.validate()
+        self.lib = lib or backend()
+        net, keep = _network_struct(connectome)
+        handle = c_void_p()
+        _check(self.lib, self.lib.snncuda_readout_create(ctypes.byref(net), ctypes.byref(handle)))
+        self.handle = handle
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.snncuda_readout_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _samples(samples):
+        ptr = np.zeros(len(samples) + 1, np.uint64)
+        ptr[1:] = np.cumsum([len(s) for s in samples])
+        n = np.ascontiguousarray([int(a) for s in samples for a, _ in s] or [0], np.uint32)
+        w = np.ascontiguousarray([float(b) for s in samples for _, b in s] or [0.0], np.float32)
+        return ptr, n, w
+
+    def feedforward(self, samples, readouts):
+        """(scores [samples, readouts] float32, spikes uint64, delivered per sample)."""
+        ptr, n, w = self._samples(samples)
+        ro = np.ascontiguousarray(readouts, np.uint32)
+        S, R = len(samples), ro.size
+        scores = np.zeros((S, R), np.float32)
+        spikes = np.zeros((S, R), np.uint64)
+        delivered = np.zeros(max(S, 1), np.uint64)
+        _check(self.lib, self.lib.snncuda_readout_feedforward(
+            self.handle, S, _abi.ptr(ptr, c_uint64), _abi.ptr(n, c_uint32), _abi.ptr(w, c_float), R,
+            _abi.ptr(ro if R else np.zeros(1, np.uint32), c_uint32), _abi.ptr(scores, c_float),
+            _abi.ptr(spikes, c_uint64), _abi.ptr(delivered, c_uint64)))
+        return scores, spikes, delivered[:S]
+
+    def recurrent(self, samples, readouts, hidden=None, **options):
+        """(scores, spikes, delivered, time steps); options are the fields of
+        snncuda_recurrent_options (iterations, feedback_decay,
+        top_k_feedback_readouts, top_k_hidden, use_scores_not_spikes)."""
+        opt = _abi.RecurrentOptions()
+        self.lib.snncuda_recurrent_options_default(ctypes.byref(opt))
+        for k, v in options.items():
+            setattr(opt, k, v)
+        ptr, n, w = self._samples(samples)
+        ro = np.ascontiguousarray(readouts, np.uint32)
+        hid = np.ascontiguousarray(hidden if hidden is not None else [], np.uint32)
+        S, R = len(samples), ro.size
+        scores = np.zeros((S, R), np.float32)
+        spikes = np.zeros((S, R), np.uint64)
+        delivered = np.zeros(max(S, 1), np.uint64)
+        steps = c_uint64()
+        _check(self.lib, self.lib.snncuda_readout_recurrent(
+            self.handle, S, _abi.ptr(ptr, c_uint64), _abi.ptr(n, c_uint32), _abi.ptr(w, c_float), R,
+            _abi.ptr(ro if R else np.zeros(1, np.uint32), c_uint32), hid.size,
+            _abi.ptr(hid if hid.size else np.zeros(1, np.uint32), c_uint32), ctypes.byref(opt),
+            _abi.ptr(scores, c_float), _abi.ptr(spikes, c_uint64), _abi.ptr(delivered, c_uint64),
+            ctypes.byref(steps)))
+        return scores, spikes, delivered[:S], int(steps.value)
 
 
 # ---------------------------------------------------------------------------

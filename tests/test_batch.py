@@ -153,3 +153,57 @@ def test_device_batch_readers(gpu_lib, members):
             assert np.array_equal(bs[k], ss[k]), (i, k)
         sim.close()
     b.close()
+
+
+@pytest.mark.gpu
+def test_autotuned_batch_keeps_results_and_checksums_match_solo(gpu_lib, port_lib, members):
+    """The autotuner probes launch shapes on the batch's own ticks and
+    shrinks the wheel slots: every network still equals its oracle run, and
+    the device checksums of each member equal those of its solo run."""
+    b = Batch([c for _, c, _ in members], _config(gpu_lib), gpu_lib, stdp_enabled=RULE)
+    for i, (_, _, d) in enumerate(members):
+        b.inject(i, *d)
+    b.run_until(59)
+    tuning = b.autotune(probe_ticks=8)
+    assert tuning["probes"] >= 5 and tuning["max_slot_events"] > 0
+    assert tuning["slot_event_capacity"] >= 2 * tuning["max_slot_events"]
+    b.run_until(299)
+    got = [(b.digests()[i], b.counters(i), b.raster(i)) for i in range(b.count)]
+    sums = b.checksums()
+    b.close()
+    for i, (w, c, d) in enumerate(members):
+        cfg = _config(port_lib)
+        cfg.stdp_enabled = 1 if RULE[i] else 0
+        ref = Simulation(c, cfg, port_lib)
+        ref.inject(*d)
+        ref.run_until(299)
+        assert got[i][0] == ref.digest(), i
+        assert got[i][1]["fired_spikes"] == ref.counters()["fired_spikes"], i
+        ref.close()
+        cfg = _config(gpu_lib)
+        cfg.stdp_enabled = 1 if RULE[i] else 0
+        solo = Simulation(c, cfg, gpu_lib)
+        solo.inject(*d)
+        solo.run_until(299)
+        assert solo.checksum() == sums[i], i
+        solo.close()
+
+
+@pytest.mark.gpu
+def test_slot_capacity_change_keeps_queued_events(gpu_lib, port_lib, members):
+    w, c, d = members[3]
+    sims = []
+    for lib in (gpu_lib, port_lib):
+        cfg = _config(lib)
+        sim = Simulation(c, cfg, lib)
+        sim.inject(*d)
+        sim.run_until(100)
+        if lib is gpu_lib:
+            peak = sim.counters()["max_slot_events"]
+            assert lib.snncuda_sim_set_slot_capacity(sim.handle, 2 * peak + 1000) == 0
+        sim.run_until(299)
+        sims.append(sim)
+    assert sims[0].digest() == sims[1].digest()
+    assert sims[0].counters()["fired_spikes"] == sims[1].counters()["fired_spikes"]
+    for s in sims:
+        s.close()

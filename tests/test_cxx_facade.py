@@ -117,6 +117,29 @@ int main() {
         }
         std::printf("]");
     }
+    // the readout paths: one hop, and the recurrent hidden/readout iteration
+    opt.reset_state_between_samples = true;
+    const auto ff = session.run_feedforward_batch(samples, opt);
+    snncuda_gb300::CudaRecurrentFeedforwardOptions ro;
+    ro.readout_neurons = {2, 5};
+    ro.iterations = 2;
+    ro.top_k_feedback_readouts = 1;
+    const auto rec = session.run_recurrent_feedforward_batch(samples, ro);
+    for (int which = 0; which < 2; ++which) {
+        const auto& b = which == 0 ? ff : rec;
+        std::printf(", \"%s\": [", which == 0 ? "feedforward" : "recurrent");
+        for (std::size_t i = 0; i < b.samples.size(); ++i) {
+            const auto& s = b.samples[i];
+            std::printf("%s{\"scores\": [", i ? ", " : "");
+            for (std::size_t k = 0; k < s.readout_scores.size(); ++k)
+                std::printf("%s%.9g", k ? ", " : "", s.readout_scores[k]);
+            std::printf("], \"spikes\": [");
+            for (std::size_t k = 0; k < s.readout_spike_counts.size(); ++k)
+                std::printf("%s%llu", k ? ", " : "", (unsigned long long)s.readout_spike_counts[k]);
+            std::printf("], \"delivered\": %llu}", (unsigned long long)s.delivered_spikes);
+        }
+        std::printf("]");
+    }
     std::printf("}\n");
     return 0;
 }
@@ -194,6 +217,14 @@ def _expected(lib):
     sim.close()
     want["stateless"] = stateless
     want["stateful"] = stateful
+    from snncuda_gb300.simulation import Readout
+    r = Readout(c, lib)
+    rs = [[(a, w) for a, w, _ in smp] for smp in samples]
+    for key, (sc, sp, dl) in (("feedforward", r.feedforward(rs, [1, 2, 4])),
+                              ("recurrent", r.recurrent(rs, [1, 4], iterations=2)[:3])):
+        want[key] = [{"scores": [float(x) for x in sc[i]], "spikes": [int(x) for x in sp[i]], "delivered": int(dl[i])}
+                     for i in range(len(rs))]
+    r.close()
     return want
 
 
@@ -202,6 +233,11 @@ def _compare(got, want):
     for key in want:
         if key == "weights":
             assert np.array_equal(np.float32(got[key]), np.float32(want[key]))
+        elif key in ("feedforward", "recurrent"):
+            # readout sums: the oracle adds in the reference's push order
+            for g, w in zip(got[key], want[key]):
+                np.testing.assert_allclose(np.float32(g["scores"]), np.float32(w["scores"]), rtol=2e-6, atol=1e-6)
+                assert g["spikes"] == w["spikes"] and g["delivered"] == w["delivered"], key
         else:
             assert got[key] == want[key], key
 
@@ -223,6 +259,7 @@ def test_facade_compiles_against_the_reference_connectome(tmp_path, port_lib):
 
 
 @pytest.mark.gpu
-def test_facade_on_the_gpu(tmp_path, gpu_lib):
+def test_facade_on_the_gpu(tmp_path, gpu_lib, port_lib):
+    """The facade linked to the GPU library against the oracle's results."""
     got = _build_and_run(tmp_path, GPU_PATH, MOCK)
-    _compare(got, _expected(gpu_lib))
+    _compare(got, _expected(port_lib))

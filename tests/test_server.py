@@ -48,9 +48,10 @@ def _solo(lib, job, i):
     return out
 
 
-def _serve(lib, jobs, **server_args):
+def _serve(lib, jobs, configs=None, **server_args):
     sv = Server(digests=True, lib=lib, **server_args)
-    ids = [sv.submit(c, _config(lib, i), d, w.ticks) for i, (w, c, d) in enumerate(jobs)]
+    configs = configs or list(range(len(jobs)))
+    ids = [sv.submit(c, _config(lib, k), d, w.ticks) for k, (w, c, d) in zip(configs, jobs)]
     for _ in range(100_000):
         if sv.step() == 0:
             break
@@ -99,3 +100,23 @@ def test_server_matches_oracle(gpu_lib, port_lib, jobs):
     for g, w in zip(got, want):
         assert g["digest"] == w["digest"]
         assert g["counters"]["fired_spikes"] == w["counters"]["fired_spikes"]
+
+
+@pytest.mark.gpu
+def test_server_eviction_preempts_long_job(gpu_lib, jobs):
+    """With eviction on and a budget of about one job, a long job admitted
+    first is evicted to host memory when shorter jobs arrive and resumes
+    afterwards; every job still equals its solo run."""
+    long_job = jobs[5]                  # 1500 neurons x 50, 175 ticks
+    w, c, d = long_job
+    long_job = (w.scaled(ticks=400), c, synthetic.build_drive(w.scaled(ticks=400), 400))
+    order = [long_job, jobs[2], jobs[4]]
+    one = max(_serve(gpu_lib, [long_job], [5])[0]["device_bytes"], 1)
+    results = _serve(gpu_lib, order, [5, 2, 4], memory_budget_bytes=one + 1, slice_ticks=20, evict=True)
+    assert results[0]["evictions"] >= 1
+    assert results[1]["finished_s"] < results[0]["finished_s"]
+    for i, (r, job) in enumerate(zip(results, order)):
+        assert r["state"] == 2, (i, r)
+        counters, digest = _solo(gpu_lib, job, [5, 2, 4][i])
+        assert r["counters"]["fired_spikes"] == counters["fired_spikes"]
+        assert r["digest"] == digest
