@@ -93,12 +93,13 @@ MINIMAL_BYTES = {
 # Bytes of this engine's own layout (snncuda_gb300/csrc/engine.h) per
 # synaptic event, external event and touched target:
 #   k_events   grouped entry (8), synapse record read + write (2 x 64), event
-#              input (16), STDP snapshot (32); externals: entry + input; per
-#              target its parameters (64) and segment bounds (8)
+#              input (16), the record's changing fields before the event (16);
+#              externals: entry + input; per target its parameters (64) and
+#              segment bounds (8)
 #   k_process  event input (16); per target its threshold (4) and the
 #              physics fields of its record, read + write (2 x 52)
 LAYOUT_BYTES = {
-    "k_events": (8 + 64 + 64 + 16 + 32, 8 + 16, 64 + 8),
+    "k_events": (8 + 64 + 64 + 16 + 16, 8 + 16, 64 + 8),
     "k_process": (16, 16, 4 + 2 * 52),
 }
 # DRAM bytes (read + write) per synaptic event of a kernel, from one ncu
@@ -662,7 +663,7 @@ def run_serving(args):
         return sim_config(lib, plan[0][1])
 
     sv = Server(memory_budget_bytes=int(args.serve_budget_gb * (1 << 30)), max_running=args.serve_running,
-                slice_ticks=args.serve_slice, lib=lib)
+                slice_ticks=args.serve_slice, evict=args.serve_evict, lib=lib)
     ids = [None] * len(built)
     start = time.perf_counter()
     nxt = 0
@@ -711,6 +712,7 @@ def run_serving(args):
                       "p99": float(np.percentile(lat, 99)) if lat.size else None,
                       "max": float(lat.max()) if lat.size else None},
         "events": int(events), "wall_s": wall, "failed_jobs": failed,
+        "evictions": int(sum(r["evictions"] for r in res)), "evict": bool(args.serve_evict),
         "solo_vs_mix_equal": mixed == solo,
     }
 
@@ -767,6 +769,8 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=120.0)
     ap.add_argument("--serve-slice", type=int, default=32, help="ticks per job and scheduling round")
     ap.add_argument("--serve-running", type=int, default=32, help="jobs advanced side by side")
+    ap.add_argument("--serve-evict", action="store_true",
+                    help="queued jobs preempt running jobs with more remaining work (eviction to host memory)")
     args = ap.parse_args()
     if args.serve:
         print(json.dumps(run_serving(args)), flush=True)

@@ -84,6 +84,16 @@ struct alignas(16) EvIn {
     uint32_t tm;    // target-major synapse index (synaptic events)
     uint32_t due;   // position in the tick's due list
 };
+// The fields of a synapse record that an event's pre-spike work changes, as
+// they were before the event (k_events writes one per synaptic event; the
+// per-target walk redoes an event that follows a fire of its target from
+// them and the record's other fields, which that work does not change).
+struct alignas(16) SynPre {
+    float weight;
+    uint32_t last_pre1;
+    uint32_t updates;
+    float last_delta;
+};
 constexpr uint32_t kEvExternal = 1u << 4;
 constexpr uint32_t kEvRepeat = 1u << 5;  // not the first event of its synapse in this tick
 
@@ -232,7 +242,7 @@ struct Engine {
     unsigned long long* grp_tmp;           // [slot_cap] the due events in bucket order (unsorted inside)
     uint16_t* grp_ltgt;                    // [slot_cap] target of each grp_tmp entry within its bucket
     EvIn* evin;                            // [slot_cap] per-event inputs of k_process, grouped, due order
-    SynA* ev_a0;                           // [slot_cap] each synaptic event's SynA before the event
+    SynPre* ev_a0;                         // [slot_cap] each synaptic event's changing fields before it
     uint32_t* fire_bits;                   // [slot_cap/32] bitmap of due positions that fired
     uint32_t* fire_at;                     // [slot_cap] firing neuron at a due position
     uint32_t* fire_tile;                   // fires per bitmap tile of kThreads words (zero between ticks)
@@ -302,10 +312,10 @@ void launch_rule_off(const Engine& e, unsigned long long tm_begin, unsigned long
 void launch_range_counts(const Engine& e, uint32_t n_begin, uint32_t n_end, unsigned long long tm_begin,
                          unsigned long long tm_end, unsigned long long* out, cudaStream_t stream);
 // out[0] += checksum of neurons [n_begin, n_end), out[1] += checksum of
-// target-major synapses [tm_begin, tm_end) (k_checksum); out must start at
-// zero.
+// their incoming synapses, whose target-major range starts at tm_begin
+// (k_checksum); out must start at zero.
 void launch_checksum(const Engine& e, uint32_t n_begin, uint32_t n_end, unsigned long long tm_begin,
-                     unsigned long long tm_end, unsigned long long* out, cudaStream_t stream);
+                     unsigned long long* out, cudaStream_t stream);
 // One-time kernel attributes (dynamic shared memory of k_process); call with
 // the device current before the first tick.
 void configure_kernels();

@@ -734,7 +734,13 @@ __device__ __forceinline__ void chunk_of(uint32_t n, uint32_t& beg, uint32_t& en
     end = n - beg < chunk ? n : beg + chunk;
 }
 
-__global__ void __launch_bounds__(kThreads) k_bcount(Engine e) {
+// Threads of the counting and placing blocks, and the due-list entries each
+// thread has in flight per round (independent loads: the kernels stream the
+// due list and would otherwise wait a DRAM latency per entry).
+constexpr int kBucketThreads = 1024;
+constexpr int kBucketUnroll = 4;
+
+__global__ void __launch_bounds__(kBucketThreads) k_bcount(Engine e) {
     tick_enter();
     extern __shared__ uint32_t s_hist[];  // [nbuckets]
     const uint32_t t = e.ts->tick;
@@ -748,15 +754,24 @@ __global__ void __launch_bounds__(kThreads) k_bcount(Engine e) {
     uint32_t beg, end;
     chunk_of(n, beg, end);
     uint32_t ext = 0;
-    for (uint32_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
-        const uint32_t lo = static_cast<uint32_t>(ev[i]);
-        const uint32_t tgt = lo & ~kExternalBit;
-        if (tgt >= e.N) {  // only reachable through snncuda_group_events with bad input
-            raise_status(e, kStatusBadEvent);
-            continue;
+    for (uint32_t i0 = beg + threadIdx.x; i0 < end; i0 += blockDim.x * kBucketUnroll) {
+        uint32_t lo[kBucketUnroll];
+#pragma unroll
+        for (int u = 0; u < kBucketUnroll; ++u) {
+            const uint32_t i = i0 + u * blockDim.x;
+            lo[u] = i < end ? static_cast<uint32_t>(ev[i]) : 0xFFFFFFFFu;
         }
-        atomicAdd(&s_hist[tgt >> e.bucket_shift], 1u);
-        ext += lo >> 31;
+#pragma unroll
+        for (int u = 0; u < kBucketUnroll; ++u) {
+            if (i0 + u * blockDim.x >= end) continue;
+            const uint32_t tgt = lo[u] & ~kExternalBit;
+            if (tgt >= e.N) {  // only reachable through snncuda_group_events with bad input
+                raise_status(e, kStatusBadEvent);
+                continue;
+            }
+            atomicAdd(&s_hist[tgt >> e.bucket_shift], 1u);
+            ext += lo[u] >> 31;
+        }
     }
     ext = __reduce_add_sync(0xffffffffu, ext);
     if ((threadIdx.x & 31) == 0 && ext) atomicAdd(&e.ts->external, static_cast<unsigned long long>(ext));
@@ -813,7 +828,7 @@ __global__ void __launch_bounds__(kThreads) k_bscan(Engine e) {
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_bscatter(Engine e) {
+__global__ void __launch_bounds__(kBucketThreads) k_bscatter(Engine e) {
     tick_enter();
     extern __shared__ uint32_t s_pos[];  // [nbuckets] next position of this chunk in each bucket
     const uint32_t B = e.nbuckets;
@@ -826,16 +841,27 @@ __global__ void __launch_bounds__(kThreads) k_bscatter(Engine e) {
     const uint32_t slot = e.ts->tick & e.wmask;
     const uint32_t n = e.ts->n_due;
     const unsigned long long* ev = e.wheel + static_cast<size_t>(slot) * e.slot_cap;
+    const uint32_t lmask = (1u << e.bucket_shift) - 1u;
     uint32_t beg, end;
     chunk_of(n, beg, end);
-    for (uint32_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
-        const unsigned long long v = ev[i];
-        const uint32_t lo = static_cast<uint32_t>(v);
-        const uint32_t tgt = lo & ~kExternalBit;
-        if (tgt >= e.N) continue;
-        const uint32_t pos = atomicAdd(&s_pos[tgt >> e.bucket_shift], 1u);
-        e.grp_tmp[pos] = (v & 0xFFFFFFFF00000000ull) | (i | (lo & kExternalBit));
-        e.grp_ltgt[pos] = static_cast<uint16_t>(tgt & ((1u << e.bucket_shift) - 1u));
+    for (uint32_t i0 = beg + threadIdx.x; i0 < end; i0 += blockDim.x * kBucketUnroll) {
+        unsigned long long v[kBucketUnroll];
+#pragma unroll
+        for (int u = 0; u < kBucketUnroll; ++u) {
+            const uint32_t i = i0 + u * blockDim.x;
+            v[u] = i < end ? ev[i] : 0ull;
+        }
+#pragma unroll
+        for (int u = 0; u < kBucketUnroll; ++u) {
+            const uint32_t i = i0 + u * blockDim.x;
+            if (i >= end) continue;
+            const uint32_t lo = static_cast<uint32_t>(v[u]);
+            const uint32_t tgt = lo & ~kExternalBit;
+            if (tgt >= e.N) continue;
+            const uint32_t pos = atomicAdd(&s_pos[tgt >> e.bucket_shift], 1u);
+            e.grp_tmp[pos] = (v[u] & 0xFFFFFFFF00000000ull) | (i | (lo & kExternalBit));
+            e.grp_ltgt[pos] = static_cast<uint16_t>(tgt & lmask);
+        }
     }
 }
 
@@ -917,15 +943,19 @@ __device__ void warp_merge_sort(unsigned long long* a, unsigned long long* b, ui
 
 
 
-// Events k_bsort places in shared memory before writing them out.
+// Events k_bsort places in shared memory before writing them out; each
+// thread holds its share of such a bucket in registers.
 constexpr uint32_t kSortSmemEvents = 4096;
+constexpr uint32_t kSortPerThread = kSortSmemEvents / kThreads;
 constexpr size_t kSortSmemBytes = kSortSmemEvents * sizeof(unsigned long long);
 
 // One block per bucket: a counting sort of the bucket's events by target.
 // The events of each target end up contiguous in grp (in arbitrary order;
 // k_events ranks them by due index) and the targets' segment starts are
-// written.  A bucket of at most kSortSmemEvents events is placed in shared
-// memory and written out coalesced; a larger one is placed in grp directly.
+// written.  A bucket of at most kSortSmemEvents events is loaded once into
+// registers (every load in flight at once), counted, placed in shared memory
+// and written out coalesced; a larger one is counted and placed in grp
+// directly from global memory.
 __global__ void __launch_bounds__(kThreads) k_bsort(Engine e) {
     tick_enter();
     extern __shared__ __align__(16) unsigned long long s_sort[];  // kSortSmemEvents, then counters
@@ -936,11 +966,28 @@ __global__ void __launch_bounds__(kThreads) k_bsort(Engine e) {
         const uint32_t lo = e.bstart[b], hi = e.bstart[b + 1], m = hi - lo;
         const uint32_t n0 = b << e.bucket_shift;
         const uint32_t nw = e.N - n0 < width ? e.N - n0 : width;
-        for (uint32_t j = threadIdx.x; j < nw; j += blockDim.x) s_cnt[j] = 0;
-        __syncthreads();
         const unsigned long long* in = e.grp_tmp + lo;
         const uint16_t* lt = e.grp_ltgt + lo;
-        for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) atomicAdd(&s_cnt[lt[i]], 1u);
+        const bool small = m <= kSortSmemEvents;
+        unsigned long long v[kSortPerThread];
+        uint32_t t16[kSortPerThread];
+        if (small) {
+#pragma unroll
+            for (uint32_t k = 0; k < kSortPerThread; ++k) {
+                const uint32_t i = threadIdx.x + k * kThreads;
+                t16[k] = i < m ? lt[i] : 0u;
+                v[k] = i < m ? in[i] : 0ull;
+            }
+        }
+        for (uint32_t j = threadIdx.x; j < nw; j += blockDim.x) s_cnt[j] = 0;
+        __syncthreads();
+        if (small) {
+#pragma unroll
+            for (uint32_t k = 0; k < kSortPerThread; ++k)
+                if (threadIdx.x + k * kThreads < m) atomicAdd(&s_cnt[t16[k]], 1u);
+        } else {
+            for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) atomicAdd(&s_cnt[lt[i]], 1u);
+        }
         __syncthreads();
         uint32_t nz = 0;  // targets with events (statistics)
         for (uint32_t j = threadIdx.x; j < nw; j += blockDim.x) nz += s_cnt[j] != 0;
@@ -949,12 +996,15 @@ __global__ void __launch_bounds__(kThreads) k_bsort(Engine e) {
         block_scan_shared(s_cnt, nw);  // segment starts relative to lo
         for (uint32_t j = threadIdx.x; j < nw; j += blockDim.x) e.seg_start[n0 + j] = lo + s_cnt[j];
         __syncthreads();
-        const bool small = m <= kSortSmemEvents;
-        unsigned long long* P = small ? s_sort : e.grp + lo;
-        for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) P[atomicAdd(&s_cnt[lt[i]], 1u)] = in[i];
-        __syncthreads();
-        if (small)
+        if (small) {
+#pragma unroll
+            for (uint32_t k = 0; k < kSortPerThread; ++k)
+                if (threadIdx.x + k * kThreads < m) s_sort[atomicAdd(&s_cnt[t16[k]], 1u)] = v[k];
+            __syncthreads();
             for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) e.grp[lo + i] = s_sort[i];
+        } else {
+            for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) e.grp[lo + atomicAdd(&s_cnt[lt[i]], 1u)] = in[i];
+        }
         __syncthreads();
     }
 }
@@ -1002,6 +1052,26 @@ __device__ __forceinline__ void pre_event(SynAB& r, const NeuronParam& p, uint32
     code_update(r.b, p, t, lc, e.code_stride, temporal, inl);
 }
 
+__device__ __forceinline__ SynPre pre_fields(const SynA& a) {
+    SynPre f;
+    f.weight = a.weight;
+    f.last_pre1 = a.last_pre1;
+    f.updates = a.updates;
+    f.last_delta = a.last_delta;
+    return f;
+}
+
+// The record as it was before an event: the fields pre_event changes from
+// the event's SynPre, the others (static fields, last_post1, post_cnt) from
+// the record, which nothing but the post-spike catch-up changes.
+__device__ __forceinline__ SynA before_event(SynA a, const SynPre& f) {
+    a.weight = f.weight;
+    a.last_pre1 = f.last_pre1;
+    a.updates = f.updates;
+    a.last_delta = f.last_delta;
+    return a;
+}
+
 __device__ __forceinline__ uint32_t ev_bits(const SynA& a) {
     return ((a.meta >> kMetaCompShift) & 3u) | (((a.meta >> kMetaRecShift) & 3u) << 2);
 }
@@ -1019,7 +1089,7 @@ __device__ __forceinline__ void synapse_events(const Engine& e, const NeuronPara
     SynAB r = e.syn[tm];
     for (uint32_t q = first; q <= last; ++q) {
         if (q != first && !more(q)) continue;
-        e.ev_a0[beg + q] = r.a;
+        e.ev_a0[beg + q] = pre_fields(r.a);
         pre_event(r, p, t, lc, e, stdp, temporal, inl);
         EvIn in;
         in.weight = r.a.weight;
@@ -1055,7 +1125,7 @@ __device__ __forceinline__ void synapse_item(const Engine& e, const EvItem& it, 
     uint16_t* lc =
         inl ? nullptr : e.lcode + p.lcode_base + static_cast<size_t>(it.tm - p.in_begin) * p.max_refs * e.code_stride;
     SynAB r = e.syn[it.tm];
-    e.ev_a0[it.pos] = r.a;
+    e.ev_a0[it.pos] = pre_fields(r.a);
     pre_event(r, p, t, lc, e, stdp, temporal, inl);
     EvIn in;
     in.weight = r.a.weight;
@@ -1122,7 +1192,7 @@ __device__ __forceinline__ void events_of_target(const Engine& e, uint32_t n, ui
                     }
                 }
                 rest &= ~(1u << j);
-                e.ev_a0[beg + best] = r.a;
+                e.ev_a0[beg + best] = pre_fields(r.a);
                 pre_event(r, p, t, lc, e, stdp, temporal, inl);
                 EvIn in;
                 in.weight = r.a.weight;
@@ -1347,7 +1417,7 @@ __device__ __forceinline__ void walk_fired_targets(const Engine& e, Walk& w, boo
             float wt = x.weight;
             bool done = !syn;
             if (syn && !wait) {
-                a = pred != 0xFFFFFFFFu ? e.syn[x.tm].a : e.ev_a0[beg + j];
+                a = pred != 0xFFFFFFFFu ? e.syn[x.tm].a : before_event(e.syn[x.tm].a, e.ev_a0[beg + j]);
                 wt = redo_pre_stdp(e, a, t, fires, stdp, ltp);
                 done = true;
             }
@@ -1670,21 +1740,23 @@ __global__ void __launch_bounds__(kFireCountThreads, 1) k_fire_count(Engine e) {
     if (nfires > e.fire_cap && threadIdx.x == 0) raise_status(e, kStatusFireOverflow);
     const uint32_t blocks = (nf + kExpandFires - 1) / kExpandFires;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // one warp per class; lane i scans a contiguous run of expansion blocks
+    // (its loads are independent, so they are all in flight at once), then
+    // the lanes' totals are scanned across the warp
+    const uint32_t per = (blocks + 31) / 32;
+    const uint32_t b0 = lane * per < blocks ? lane * per : blocks;
+    const uint32_t b1 = b0 + per < blocks ? b0 + per : blocks;
     for (uint32_t d = warp; d < D; d += blockDim.x / 32) {
         const uint32_t slot = (t + e.cls_delta[d]) & e.wmask;
         const uint32_t start = e.slot_count[slot];
-        uint32_t carry = 0;
-        uint32_t v = static_cast<uint32_t>(lane) < blocks ? __ldcg(e.xsum + static_cast<size_t>(lane) * D + d) : 0;
-        for (uint32_t b0 = 0; b0 < blocks; b0 += 32) {
-            const uint32_t b = b0 + lane;
-            // the next chunk's counts are fetched before this chunk's stores
-            const uint32_t vn = b + 32 < blocks ? __ldcg(e.xsum + static_cast<size_t>(b + 32) * D + d) : 0;
-            const uint32_t incl = warp_incl_scan(v);
-            if (b < blocks)
-                e.xdst[static_cast<size_t>(b) * D + d] =
-                    static_cast<unsigned long long>(slot) * e.slot_cap + start + carry + incl - v;
-            carry += __shfl_sync(0xffffffffu, incl, 31);
-            v = vn;
+        uint32_t sum = 0;
+        for (uint32_t b = b0; b < b1; ++b) sum += __ldcg(e.xsum + static_cast<size_t>(b) * D + d);
+        const uint32_t incl = warp_incl_scan(sum);
+        const uint32_t carry = __shfl_sync(0xffffffffu, incl, 31);
+        unsigned long long pos = static_cast<unsigned long long>(slot) * e.slot_cap + start + (incl - sum);
+        for (uint32_t b = b0; b < b1; ++b) {
+            e.xdst[static_cast<size_t>(b) * D + d] = pos;
+            pos += __ldcg(e.xsum + static_cast<size_t>(b) * D + d);
         }
         if (lane == 0) {
             if (static_cast<unsigned long long>(start) + carry > e.slot_cap) {
@@ -1839,13 +1911,14 @@ __device__ __forceinline__ unsigned long long record_hash(unsigned long long ind
 }
 
 // Order-independent checksums of neurons [nb, ne) (NeuronRec + NeuronTp)
-// and target-major synapses [tb, te) (the 64-byte record, its rule-off bit
-// masked): the sum over records of a hash of (index within the range,
-// record words).  A batch member and its solo run have the same records at
-// the same relative indices, so equal sums mean equal state (up to hash
-// collisions); the temporal-pattern contents enter through their counters.
-__global__ void k_checksum(Engine e, uint32_t nb, uint32_t ne, unsigned long long tb, unsigned long long te,
-                           unsigned long long* out) {
+// and of their incoming synapses: the sum over records of a hash of (index
+// within the range, the record's meaning).  A synapse contributes its SynA
+// words (the rule-off bit masked), its code-pattern counters, its code
+// offsets and its learned code patterns, wherever the layout keeps them
+// (inline in the record or in the pattern pool, which depends on the widest
+// code of the whole simulation), so a batch member and its solo run give
+// equal sums exactly when their states are equal (up to hash collisions).
+__global__ void k_checksum(Engine e, uint32_t nb, uint32_t ne, unsigned long long tb, unsigned long long* out) {
     const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
     const unsigned long long first = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
     unsigned long long hn = 0, hs = 0;
@@ -1865,16 +1938,39 @@ __global__ void k_checksum(Engine e, uint32_t nb, uint32_t ne, unsigned long lon
         }
         hn += record_hash<24>(n - nb, w);
     }
-    for (unsigned long long i = tb + first; i < te; i += stride) {
-        uint32_t w[16];
-        const uint4* r = reinterpret_cast<const uint4*>(e.syn + i);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const uint4 v = r[k];
-            w[4 * k] = v.x; w[4 * k + 1] = v.y; w[4 * k + 2] = v.z; w[4 * k + 3] = v.w;
+    // synapses: a warp per target
+    const uint32_t lane = threadIdx.x & 31;
+    const unsigned long long warps = stride / 32;
+    for (unsigned long long n = nb + first / 32; n < ne; n += warps) {
+        const NeuronParam p = e.nparam[n];
+        const bool inl = inline_code_pattern(p.max_refs, e.code_stride);
+        for (unsigned long long i = e.in_ptr[n] + lane; i < e.in_ptr[n + 1]; i += 32) {
+            const SynAB rec = e.syn[i];
+            const SynA& a = rec.a;
+            const SynB& sb = rec.b;
+            unsigned long long h = mix64(0x6a09e667f3bcc908ull, i - tb);
+            h = mix64(h, __float_as_uint(a.weight));
+            h = mix64(h, a.last_pre1);
+            h = mix64(h, a.last_post1);
+            h = mix64(h, a.meta & ~(1u << kMetaRuleOffBit));
+            h = mix64(h, __float_as_uint(a.clamp_hi));
+            h = mix64(h, a.updates);
+            h = mix64(h, __float_as_uint(a.last_delta));
+            h = mix64(h, a.post_cnt);
+            h = mix64(h, sb.pre_count);
+            h = mix64(h, sb.code_ws);
+            h = mix64(h, sb.code_matches);
+            h = mix64(h, sb.code_len | (static_cast<uint32_t>(sb.flags) << 8) |
+                             (static_cast<uint32_t>(sb.learned_count) << 16));
+            for (uint32_t j = 0; j < sb.code_len; ++j) h = mix64(h, ring_get(sb.ring_lo, sb.ring_hi, j));
+            const uint32_t expected = (a.meta >> kMetaExpectedShift) & 15u;
+            const uint16_t* lc =
+                e.lcode + p.lcode_base + static_cast<size_t>(i - p.in_begin) * p.max_refs * e.code_stride;
+            for (uint32_t k = 0; k < sb.learned_count; ++k)
+                for (uint32_t j = 0; j < expected; ++j)
+                    h = mix64(h, inl ? ring_get(sb.ring_hi, 0ull, j) : lc[static_cast<size_t>(k) * e.code_stride + j]);
+            hs += h;
         }
-        w[3] &= ~(1u << kMetaRuleOffBit);  // SynA.meta
-        hs += record_hash<16>(i - tb, w);
     }
     for (int d = 16; d > 0; d >>= 1) {
         hn += __shfl_down_sync(0xffffffffu, hn, d);
@@ -1889,8 +1985,8 @@ __global__ void k_checksum(Engine e, uint32_t nb, uint32_t ne, unsigned long lon
 }  // namespace
 
 void launch_checksum(const Engine& e, uint32_t n_begin, uint32_t n_end, unsigned long long tm_begin,
-                     unsigned long long tm_end, unsigned long long* out, cudaStream_t stream) {
-    k_checksum<<<e.grid_wide * 2, kThreads, 0, stream>>>(e, n_begin, n_end, tm_begin, tm_end, out);
+                     unsigned long long* out, cudaStream_t stream) {
+    k_checksum<<<e.grid_wide * 2, kThreads, 0, stream>>>(e, n_begin, n_end, tm_begin, out);
 }
 
 void launch_rule_off(const Engine& e, unsigned long long tm_begin, unsigned long long tm_end, cudaStream_t stream) {
@@ -1925,7 +2021,7 @@ static size_t bucket_smem(const Engine& e) { return static_cast<size_t>(e.nbucke
 static size_t bsort_smem(const Engine& e) {
     return kSortSmemBytes + (static_cast<size_t>(1) << e.bucket_shift) * sizeof(uint32_t);
 }
-static uint32_t bsort_grid(const Engine& e) { return e.nbuckets < 4 * e.grid_wide ? e.nbuckets : 4 * e.grid_wide; }
+static uint32_t bsort_grid(const Engine& e) { return e.nbuckets; }
 
 void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     const uint32_t wide = e.grid_wide;
@@ -1943,9 +2039,9 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
         if (marks) cudaEventRecordWithFlags(marks[2 * index + (after ? 1 : 0)], s.side, cudaEventRecordExternal);
     };
     // k_bcount follows a wait on the side stream: a full dependency
-    mark(false); launch_main(k_bcount, e.grid_bucket, kThreads, bucket_smem(e), stream, false, e); mark(true);
+    mark(false); launch_main(k_bcount, e.grid_bucket, kBucketThreads, bucket_smem(e), stream, false, e); mark(true);
     mark(false); launch_main(k_bscan, 1, kThreads, 0, stream, dep, e); mark(true);
-    mark(false); launch_main(k_bscatter, e.grid_bucket, kThreads, bucket_smem(e), stream, dep, e); mark(true);
+    mark(false); launch_main(k_bscatter, e.grid_bucket, kBucketThreads, bucket_smem(e), stream, dep, e); mark(true);
     mark(false); launch_main(k_bsort, bsort_grid(e), kThreads, bsort_smem(e), stream, dep, e); mark(true);
     // the temporal update forks off here and runs beside k_events / k_process
     // (it needs only the segment starts)
@@ -1980,9 +2076,9 @@ const char* kernel_name(int index) {
 }
 
 void launch_group(const Engine& e, cudaStream_t stream) {
-    k_bcount<<<e.grid_bucket, kThreads, bucket_smem(e), stream>>>(e);
+    k_bcount<<<e.grid_bucket, kBucketThreads, bucket_smem(e), stream>>>(e);
     k_bscan<<<1, kThreads, 0, stream>>>(e);
-    k_bscatter<<<e.grid_bucket, kThreads, bucket_smem(e), stream>>>(e);
+    k_bscatter<<<e.grid_bucket, kBucketThreads, bucket_smem(e), stream>>>(e);
     k_bsort<<<bsort_grid(e), kThreads, bsort_smem(e), stream>>>(e);
     k_segsort<<<e.grid_wide * 4, kThreads, 0, stream>>>(e);
 }

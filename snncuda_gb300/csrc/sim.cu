@@ -465,7 +465,7 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.grp_tmp = salloc<unsigned long long>(sim, slot_cap, BufKind::kScratch);
     e.grp_ltgt = salloc<uint16_t>(sim, slot_cap, BufKind::kScratch);
     e.evin = salloc<EvIn>(sim, slot_cap, BufKind::kScratch);
-    e.ev_a0 = salloc<SynA>(sim, slot_cap, BufKind::kScratch);
+    e.ev_a0 = salloc<SynPre>(sim, slot_cap, BufKind::kScratch);
     e.fire_bits = salloc<uint32_t>(sim, bit_words, BufKind::kZero);
     e.fire_at = salloc<uint32_t>(sim, slot_cap, BufKind::kScratch);
     e.fire_tile = salloc<uint32_t>(sim, fire_tiles + 2, BufKind::kZero);
@@ -737,7 +737,7 @@ void resize_slots(snncuda_sim* sim, uint64_t cap) {
     realloc_buf(e.grp_tmp, cap * 8);
     realloc_buf(e.grp_ltgt, cap * 2);
     realloc_buf(e.evin, cap * sizeof(EvIn));
-    realloc_buf(e.ev_a0, cap * sizeof(SynA));
+    realloc_buf(e.ev_a0, cap * sizeof(SynPre));
     realloc_buf(e.fire_at, cap * 4);
     realloc_buf(e.fire_bits, std::max<uint64_t>(z.bit_words, 1) * 4);
     realloc_buf(e.fire_tile, (z.fire_tiles + 2) * 4);
@@ -1466,7 +1466,8 @@ void checksum_range(snncuda_sim* sim, uint32_t n0, uint32_t n1, uint64_t t0, uin
     unsigned long long c[2] = {};
     cudaError_t err = cudaMemsetAsync(d, 0, sizeof(c), st);
     if (err == cudaSuccess) {
-        launch_checksum(sim->e, n0, n1, t0, t1, d, st);
+        launch_checksum(sim->e, n0, n1, t0, d, st);
+        (void)t1;
         err = cudaGetLastError();
     }
     if (err == cudaSuccess) err = cudaMemcpyAsync(c, d, sizeof(c), cudaMemcpyDeviceToHost, st);
@@ -2020,7 +2021,7 @@ static uint64_t estimate_bytes_impl(const snncuda_network* net, const snncuda_co
     // grouping: bucket counters of up to 512 chunks
     const uint64_t buckets = (N + 255) / 256 < kMaxBuckets ? (N + 255) / 256 + 1 : kMaxBuckets;
     const uint64_t persistent = 64 * S + 8 * S + 8 * pre_total + neuron_bytes + lcode +
-                                W * slot_cap * 8 + slot_cap * (8 + 8 + 2 + 16 + 32 + 4 + 1) + 512 * 4 * buckets +
+                                W * slot_cap * 8 + slot_cap * (8 + 8 + 2 + 16 + 16 + 4 + 1) + 512 * 4 * buckets +
                                 fire_cap * 4 + (fire_cap / 8 + 1) * 12 * std::max<uint64_t>(D, 1) +
                                 16 * cfg.raster_capacity + (16u << 20);
     const uint64_t transient = S * (23 + 8 + 12 + 8) + 4 * (has_codes ? net->code_offset_ptr[S] : 0) +
@@ -2337,7 +2338,13 @@ int snncuda_server_step(snncuda_server* sv, uint32_t* active) {
         }
         sv->cv.notify_one();
     }
-    // evicted jobs come back, in the order they left, while they fit
+    // evicted jobs come back while they fit, the least remaining work first
+    // (the rule that preempted them)
+    std::stable_sort(sv->evicted.begin(), sv->evicted.end(), [&](uint64_t x, uint64_t y) {
+        const ServerJob& a = *sv->jobs[x];
+        const ServerJob& b = *sv->jobs[y];
+        return remaining(a, a.sim->next_tick) < remaining(b, b.sim->next_tick);
+    });
     while (!sv->evicted.empty() && sv->running.size() + sv->creating < sv->cfg.max_running) {
         const uint64_t id = sv->evicted.front();
         ServerJob& j = *sv->jobs_at(id);
