@@ -565,7 +565,7 @@ def batched_leg(lib, count, nmin, nmax, T, stream, wave_synapses=1.2e9, probe_ti
 
     ms_b = ms_s = 0.0
     ev_b = ev_s = 0
-    parity, tunings, timed_ticks = [], [], []
+    parity, tunings, timed_ticks, solo = [], [], [], []
     for wave in member_waves(members, wave_synapses):
         nets = [synthetic.build_network(w) for w, _ in wave]
         drives = [synthetic.build_drive(w, T) for w, _ in wave]
@@ -587,8 +587,11 @@ def batched_leg(lib, count, nmin, nmax, T, stream, wave_synapses=1.2e9, probe_ti
             sim.inject(*d)
             sim.run_until(t0 - 1)
             c0 = sim.counters()["synaptic_events"]
-            ms_s += timed(lambda: sim.run_until(T - 1))
-            ev_s += sim.counters()["synaptic_events"] - c0
+            ms_one = timed(lambda: sim.run_until(T - 1))
+            ev_one = sim.counters()["synaptic_events"] - c0
+            ms_s += ms_one
+            ev_s += ev_one
+            solo.append((w.neurons, ev_one, ms_one))
             parity.append(sim.checksum() == sums[k])
             sim.close()
         del nets, drives
@@ -598,6 +601,7 @@ def batched_leg(lib, count, nmin, nmax, T, stream, wave_synapses=1.2e9, probe_ti
         "speedup_vs_sequential": (ev_b / ms_b) / (ev_s / ms_s) if ev_s else None,
         "ms_batched": ms_b, "events": ev_b, "parity_per_network": all(parity),
         "networks_equal": int(sum(parity)),
+        "sequential_by_size": sequential_by_size(solo),
         "config": {"networks": count, "neurons_log_uniform": [nmin, nmax], "fanout_uniform": [100, 1000],
                    "ticks": T, "timed_ticks_per_wave": timed_ticks, "waves": len(tunings),
                    "wave_synapses_max": wave_synapses, "stdp_rule_on_even": True, "seeds": "1000 + i",
@@ -605,6 +609,27 @@ def batched_leg(lib, count, nmin, nmax, T, stream, wave_synapses=1.2e9, probe_ti
                    "weights": "stdp_100k distributions, initial and per-synapse max weight x 1000 / fan-out"},
         "autotune": tunings,
     }
+
+
+def sequential_by_size(solo):
+    """Where the one-handle-per-network time goes: per band of network size,
+    the networks, their synaptic events, their summed time and the rate one
+    handle reaches on them; plus the speed-up the batch would show if it ran
+    every event at the best single-handle rate (the bound that the large
+    members, already near that rate alone, put on batched / sequential)."""
+    bands = [(0, 10_000), (10_000, 50_000), (50_000, 1 << 40)]
+    out = []
+    for lo, hi in bands:
+        sel = [(e, ms) for n, e, ms in solo if lo <= n < hi]
+        ev = sum(e for e, _ in sel)
+        ms = sum(ms for _, ms in sel)
+        out.append({"neurons": [lo, hi if hi < (1 << 40) else None], "networks": len(sel), "events": ev,
+                    "ms": ms, "events_per_s": ev / (ms / 1e3) if ms else None})
+    best = max((e / (ms / 1e3) for _, e, ms in solo if ms > 0), default=0.0)
+    ev = sum(e for _, e, _ in solo)
+    ms = sum(ms for _, _, ms in solo)
+    return {"bands": out, "best_single_rate": best,
+            "speedup_if_batched_at_best_single_rate": (best * ms / 1e3) / ev if ev else None}
 
 
 def run_batched(args):
