@@ -786,6 +786,8 @@ def main():
                     help="networks of the batched leg of the default run (0 skips it)")
     ap.add_argument("--rmw-floor", action="store_true",
                     help="time random 64-byte record read-modify-writes (the per-event access floor)")
+    ap.add_argument("--rmw-args", default="",
+                    help="records events [bands band_len picks rows row_len] for --rmw-floor")
     ap.add_argument("--serve", action="store_true", help="serving: Poisson arrivals under a memory budget")
     ap.add_argument("--serve-rate", type=float, default=4.0, help="job arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=15.0, help="arrival window")
@@ -803,7 +805,8 @@ def main():
     if args.rmw_floor:
         import __graft_entry__
         exe = __graft_entry__.build_rmw_floor()
-        out = subprocess.run([str(exe)], check=True, stdout=subprocess.PIPE, text=True).stdout
+        out = subprocess.run([str(exe), *args.rmw_args.split()], check=True, stdout=subprocess.PIPE,
+                             text=True).stdout
         print(out.strip(), flush=True)
         return
     if args.batched:

@@ -256,8 +256,17 @@ typedef struct snncuda_tuning {
     double ms_per_tick_after;       /* last probe, with the chosen shapes */
     uint32_t probes;
     uint64_t probe_ticks;
+    uint32_t scatter_pass_events;   /* due-list events per grouping pass (0: one pass) */
+    uint32_t side_serial;           /* 1: the neuron temporal update and post-spike STDP run in
+                                       tick order instead of beside the synapse kernels */
 } snncuda_tuning;
 int snncuda_sim_autotune(snncuda_sim* sim, uint64_t probe_ticks, snncuda_tuning* out);
+/* Applies a tuning found earlier (by snncuda_sim_autotune on this or another
+ * simulation; results do not depend on it).  Every field must lie in the
+ * range the autotuner searches (SNNCUDA_ERR_INVALID_ARGUMENT otherwise);
+ * slot_event_capacity 0 keeps the current capacity; the statistics fields
+ * are ignored.  No reference counterpart (engine extension). */
+int snncuda_sim_apply_tuning(snncuda_sim* sim, const snncuda_tuning* tuning);
 /* Sets the wheel-slot capacity (rounded up to a multiple of 32); fails with
  * SNNCUDA_ERR_INVALID_ARGUMENT if a slot already holds more events. */
 int snncuda_sim_set_slot_capacity(snncuda_sim* sim, uint64_t capacity);
@@ -307,6 +316,8 @@ int snncuda_batch_read_synapses(snncuda_batch* batch, uint32_t network, const sn
 int snncuda_batch_state_digests(snncuda_batch* batch, uint64_t* neuron_digests, uint64_t* synapse_digests);
 /* snncuda_sim_autotune on the batch's one tick loop. */
 int snncuda_batch_autotune(snncuda_batch* batch, uint64_t probe_ticks, snncuda_tuning* out);
+/* snncuda_sim_apply_tuning on the batch's tick loop. */
+int snncuda_batch_apply_tuning(snncuda_batch* batch, const snncuda_tuning* tuning);
 /* Checksums of every network (arrays of `count`), as snncuda_sim_state_checksum. */
 int snncuda_batch_state_checksums(snncuda_batch* batch, uint64_t* neuron_sums, uint64_t* synapse_sums);
 /* Network's fire records [first, first + count) in its own processing order. */

@@ -86,7 +86,8 @@ class Tuning(Structure):
         ("grid_temporal", c_uint32), ("ticks_per_graph", c_uint32), ("block_threads", c_uint32),
         ("slot_event_capacity", c_uint64), ("max_slot_events", c_uint64),
         ("ms_per_tick_before", ctypes.c_double), ("ms_per_tick_after", ctypes.c_double),
-        ("probes", c_uint32), ("probe_ticks", c_uint64),
+        ("probes", c_uint32), ("probe_ticks", c_uint64), ("scatter_pass_events", c_uint32),
+        ("side_serial", c_uint32),
     ]
 
 
@@ -218,6 +219,8 @@ _SIGNATURES = {
     "snncuda_batch_state_checksums": (c_int, [c_void_p, POINTER(c_uint64), POINTER(c_uint64)]),
     "snncuda_sim_autotune": (c_int, [c_void_p, c_uint64, POINTER(Tuning)]),
     "snncuda_batch_autotune": (c_int, [c_void_p, c_uint64, POINTER(Tuning)]),
+    "snncuda_sim_apply_tuning": (c_int, [c_void_p, POINTER(Tuning)]),
+    "snncuda_batch_apply_tuning": (c_int, [c_void_p, POINTER(Tuning)]),
     "snncuda_sim_set_slot_capacity": (c_int, [c_void_p, c_uint64]),
     "snncuda_readout_create": (c_int, [POINTER(Network), POINTER(c_void_p)]),
     "snncuda_readout_destroy": (c_int, [c_void_p]),

@@ -232,6 +232,16 @@ struct Engine {
     uint32_t bucket_shift;
     uint32_t nbuckets;
     uint32_t grid_bucket;
+    // Due-list events per placing pass of k_bscatter (0: one pass): a due
+    // list longer than this is placed in passes over disjoint bucket ranges,
+    // so the lines of grp_tmp / grp_ltgt being filled stay in L2 until
+    // complete instead of going to DRAM half-written.
+    uint32_t scatter_pass_events;
+    // 1: k_temporal and k_post run on the main stream in tick order instead
+    // of beside k_events / k_process and the fire ordering on the side
+    // stream (two random-access kernels side by side can take longer than
+    // one after the other)
+    uint32_t side_serial;
     uint32_t* bcnt;                        // [grid_bucket][nbuckets] events of each (chunk, bucket)
     uint32_t* btot;                        // [nbuckets] events per bucket (zero between ticks)
     uint32_t* bstart;                      // [nbuckets + 1] first grouped position of each bucket
@@ -271,6 +281,7 @@ struct Engine {
 };
 
 constexpr uint32_t kMaxBuckets = 16384;   // target buckets of the grouping (shared-memory counters)
+constexpr uint32_t kScatterPassEvents = 1u << 22;  // default Engine::scatter_pass_events (42 MB of grp_tmp + grp_ltgt)
 constexpr uint32_t kMaxBucketShift = 14;  // at most 2^14 targets per bucket: N <= 2^28
 
 // Targets per bucket (log2) for N targets: the smallest 2^s >= 256 with at

@@ -682,8 +682,10 @@ __device__ void code_update(SynB& b, const NeuronParam& p, uint32_t t, uint16_t*
 //               starts written; inside a target the order stays arbitrary
 //               (k_events ranks a target's events by due index, the grouping
 //               entry point sorts them with k_segsort)
-// Per event that is two reads of the due list, one scattered write, and a
-// coalesced read and write per bucket: no per-target global atomics.
+// Per event that is two or more reads of the due list (k_bscatter places a
+// long list in passes over disjoint bucket ranges, so the lines it fills stay
+// in L2 until complete), one scattered write, and a coalesced read and write
+// per bucket: no per-target global atomics.
 // ---------------------------------------------------------------------------
 
 // Block-wide exclusive scan of a[0 .. n) in shared memory (n <= 64 *
@@ -759,7 +761,7 @@ __global__ void __launch_bounds__(kBucketThreads) k_bcount(Engine e) {
 #pragma unroll
         for (int u = 0; u < kBucketUnroll; ++u) {
             const uint32_t i = i0 + u * blockDim.x;
-            lo[u] = i < end ? static_cast<uint32_t>(ev[i]) : 0xFFFFFFFFu;
+            lo[u] = i < end ? static_cast<uint32_t>(__ldcs(ev + i)) : 0xFFFFFFFFu;
         }
 #pragma unroll
         for (int u = 0; u < kBucketUnroll; ++u) {
@@ -844,23 +846,34 @@ __global__ void __launch_bounds__(kBucketThreads) k_bscatter(Engine e) {
     const uint32_t lmask = (1u << e.bucket_shift) - 1u;
     uint32_t beg, end;
     chunk_of(n, beg, end);
-    for (uint32_t i0 = beg + threadIdx.x; i0 < end; i0 += blockDim.x * kBucketUnroll) {
-        unsigned long long v[kBucketUnroll];
+    // passes over disjoint bucket ranges (Engine::scatter_pass_events); the
+    // due list is re-read per pass with evict-first loads, which keep the
+    // L2 for the lines being filled
+    const uint32_t per = e.scatter_pass_events;
+    const uint32_t passes = per != 0 && n > per ? (n + per - 1) / per : 1u;
+    for (uint32_t pass = 0; pass < passes; ++pass) {
+        const uint32_t blo = static_cast<uint32_t>(static_cast<unsigned long long>(B) * pass / passes);
+        const uint32_t bhi = static_cast<uint32_t>(static_cast<unsigned long long>(B) * (pass + 1) / passes);
+        for (uint32_t i0 = beg + threadIdx.x; i0 < end; i0 += blockDim.x * kBucketUnroll) {
+            unsigned long long v[kBucketUnroll];
 #pragma unroll
-        for (int u = 0; u < kBucketUnroll; ++u) {
-            const uint32_t i = i0 + u * blockDim.x;
-            v[u] = i < end ? ev[i] : 0ull;
-        }
+            for (int u = 0; u < kBucketUnroll; ++u) {
+                const uint32_t i = i0 + u * blockDim.x;
+                v[u] = i < end ? __ldcs(ev + i) : 0ull;
+            }
 #pragma unroll
-        for (int u = 0; u < kBucketUnroll; ++u) {
-            const uint32_t i = i0 + u * blockDim.x;
-            if (i >= end) continue;
-            const uint32_t lo = static_cast<uint32_t>(v[u]);
-            const uint32_t tgt = lo & ~kExternalBit;
-            if (tgt >= e.N) continue;
-            const uint32_t pos = atomicAdd(&s_pos[tgt >> e.bucket_shift], 1u);
-            e.grp_tmp[pos] = (v[u] & 0xFFFFFFFF00000000ull) | (i | (lo & kExternalBit));
-            e.grp_ltgt[pos] = static_cast<uint16_t>(tgt & lmask);
+            for (int u = 0; u < kBucketUnroll; ++u) {
+                const uint32_t i = i0 + u * blockDim.x;
+                if (i >= end) continue;
+                const uint32_t lo = static_cast<uint32_t>(v[u]);
+                const uint32_t tgt = lo & ~kExternalBit;
+                if (tgt >= e.N) continue;
+                const uint32_t b = tgt >> e.bucket_shift;
+                if (b < blo || b >= bhi) continue;
+                const uint32_t pos = atomicAdd(&s_pos[b], 1u);
+                e.grp_tmp[pos] = (v[u] & 0xFFFFFFFF00000000ull) | (i | (lo & kExternalBit));
+                e.grp_ltgt[pos] = static_cast<uint16_t>(tgt & lmask);
+            }
         }
     }
 }
@@ -2036,13 +2049,31 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
         if (after) ++k;
     };
     auto side_mark = [&](int index, bool after) {
-        if (marks) cudaEventRecordWithFlags(marks[2 * index + (after ? 1 : 0)], s.side, cudaEventRecordExternal);
+        if (marks)
+            cudaEventRecordWithFlags(marks[2 * index + (after ? 1 : 0)], e.side_serial ? stream : s.side,
+                                     cudaEventRecordExternal);
     };
     // k_bcount follows a wait on the side stream: a full dependency
     mark(false); launch_main(k_bcount, e.grid_bucket, kBucketThreads, bucket_smem(e), stream, false, e); mark(true);
     mark(false); launch_main(k_bscan, 1, kThreads, 0, stream, dep, e); mark(true);
     mark(false); launch_main(k_bscatter, e.grid_bucket, kBucketThreads, bucket_smem(e), stream, dep, e); mark(true);
     mark(false); launch_main(k_bsort, bsort_grid(e), kThreads, bsort_smem(e), stream, dep, e); mark(true);
+    if (e.side_serial) {
+        // everything in tick order on the main stream; k_temporal and k_post
+        // take a full dependency (they do not wait on a programmatic launch)
+        side_mark(9, false);
+        k_temporal<<<e.grid_process, kThreads, 0, stream>>>(e);
+        side_mark(9, true);
+        mark(false); launch_main(k_events, e.grid_events, kThreads, 0, stream, false, e); mark(true);
+        mark(false); launch_main(k_process, e.grid_walk, kThreads, kProcessSmem, stream, dep, e); mark(true);
+        side_mark(10, false);
+        k_post<<<wide * 4, kThreads, 0, stream>>>(e);
+        side_mark(10, true);
+        mark(false); launch_main(k_fire_list, e.grid_fire, kThreads, 0, stream, false, e); mark(true);
+        mark(false); launch_main(k_fire_count, e.grid_wide / 4 + 1, kFireCountThreads, 0, stream, false, e); mark(true);
+        mark(false); launch_main(k_expand, e.grid_wide * 4, kThreads, 0, stream, dep, e); mark(true);
+        return;
+    }
     // the temporal update forks off here and runs beside k_events / k_process
     // (it needs only the segment starts)
     cudaEventRecord(s.ev[0], stream);

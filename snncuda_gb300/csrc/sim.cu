@@ -437,6 +437,7 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     if (e.bucket_shift == 0) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "at most 2^28 neurons");
     e.nbuckets = static_cast<uint32_t>(std::max<uint64_t>(1, (static_cast<uint64_t>(N) + (1u << e.bucket_shift) - 1) >> e.bucket_shift));
     e.grid_bucket = static_cast<uint32_t>(std::max(1, sms * 2));
+    e.scatter_pass_events = kScatterPassEvents;
     const uint32_t grid_bucket_max = static_cast<uint32_t>(std::max(1, sms * 4));  // the autotuner's largest
 
     // ---- tables ----
@@ -809,6 +810,8 @@ void autotune_impl(snncuda_sim* sim, uint64_t probe_ticks, snncuda_tuning* out) 
         {&e.grid_walk, {std::min(walk_max, sms * 2), std::min(walk_max, sms * 3), std::min(walk_max, sms * 4),
                         std::min(walk_max, sms * 6)}},
         {&e.grid_bucket, {sms, sms * 2, sms * 4}},
+        {&e.scatter_pass_events, {kScatterPassEvents / 2, kScatterPassEvents * 2, 0u}},
+        {&e.side_serial, {0u, 1u}},
         {&e.grid_process, {sms * 2, sms * 4, sms * 8}},
         {&sim->ticks_per_graph, {8, 16, 32}},
     };
@@ -838,6 +841,8 @@ void autotune_impl(snncuda_sim* sim, uint64_t probe_ticks, snncuda_tuning* out) 
         out->grid_events = e.grid_events;
         out->grid_walk = e.grid_walk;
         out->grid_bucket = e.grid_bucket;
+        out->scatter_pass_events = e.scatter_pass_events;
+        out->side_serial = e.side_serial;
         out->grid_temporal = e.grid_process;
         out->ticks_per_graph = sim->ticks_per_graph;
         out->block_threads = 256;
@@ -847,6 +852,35 @@ void autotune_impl(snncuda_sim* sim, uint64_t probe_ticks, snncuda_tuning* out) 
         out->ms_per_tick_after = last;
         out->probes = probes;
         out->probe_ticks = probe_ticks;
+    }
+}
+
+// Applies launch shapes found earlier (by autotune_impl, here or on another
+// simulation of the same network); every field must lie in the range the
+// autotuner itself searches, and a slot capacity of 0 keeps the current one.
+void apply_tuning_impl(snncuda_sim* sim, const snncuda_tuning& t) {
+    resident(sim);
+    run_complete(sim, true);
+    Engine& e = sim->e;
+    const uint32_t sms = sim->sms;
+    const uint32_t walk_max = static_cast<uint32_t>(std::max<uint64_t>(1, (static_cast<uint64_t>(sim->N) + 63) / 64));
+    auto in = [](uint32_t v, uint32_t lo, uint32_t hi) { return v >= lo && v <= hi; };
+    if (!in(t.grid_events, 1, sms * 16) || !in(t.grid_walk, 1, std::max(walk_max, sms * 8)) ||
+        !in(t.grid_bucket, 1, sms * 4) || !in(t.grid_temporal, 1, sms * 8) || !in(t.ticks_per_graph, 1, 64) ||
+        t.side_serial > 1 || (t.block_threads != 0 && t.block_threads != 256))
+        throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "tuning field outside the autotuner's ranges");
+    e.grid_events = t.grid_events;
+    e.grid_walk = t.grid_walk;
+    e.grid_bucket = t.grid_bucket;
+    e.grid_process = t.grid_temporal;
+    e.scatter_pass_events = t.scatter_pass_events;
+    e.side_serial = t.side_serial;
+    sim->ticks_per_graph = t.ticks_per_graph;
+    sim->drop_graphs();
+    if (t.slot_event_capacity != 0 && t.slot_event_capacity != e.slot_cap) {
+        if (t.slot_event_capacity >= (1ull << 31))
+            throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "slot capacity must be below 2^31");
+        resize_slots(sim, (t.slot_event_capacity + 31) & ~31ull);
     }
 }
 
@@ -1496,6 +1530,12 @@ int snncuda_sim_autotune(snncuda_sim* sim, uint64_t probe_ticks, snncuda_tuning*
     return rc;
 }
 
+int snncuda_sim_apply_tuning(snncuda_sim* sim, const snncuda_tuning* tuning) {
+    if (sim == nullptr || tuning == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null argument");
+    if (sim->poisoned) return set_error(SNNCUDA_ERR_POISONED, "simulation poisoned by an earlier device error");
+    return guarded([&] { apply_tuning_impl(sim, *tuning); });
+}
+
 int snncuda_sim_set_slot_capacity(snncuda_sim* sim, uint64_t capacity) {
     if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
     if (capacity == 0 || capacity >= (1ull << 31))
@@ -1565,6 +1605,7 @@ void group_run(const uint64_t* events, uint32_t count, uint32_t neuron_count, ui
     e.bucket_shift = bucket_shift_for(neuron_count);
     e.nbuckets = group_buckets(neuron_count);
     e.grid_bucket = kGroupGrid;
+    e.scatter_pass_events = kScatterPassEvents;
     e.bcnt = sc.bcnt;
     e.btot = sc.btot;
     e.bstart = sc.bstart;
@@ -1959,6 +2000,11 @@ int snncuda_batch_state_checksums(snncuda_batch* b, uint64_t* neuron_sums, uint6
 int snncuda_batch_autotune(snncuda_batch* b, uint64_t probe_ticks, snncuda_tuning* out) {
     if (b == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null batch");
     return snncuda_sim_autotune(b->sim, probe_ticks, out);
+}
+
+int snncuda_batch_apply_tuning(snncuda_batch* b, const snncuda_tuning* tuning) {
+    if (b == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null batch");
+    return snncuda_sim_apply_tuning(b->sim, tuning);
 }
 
 int snncuda_batch_read_raster(snncuda_batch* b, uint32_t i, uint64_t first, uint64_t count, uint64_t* ticks,

@@ -66,6 +66,15 @@ def _check(lib, status: int) -> None:
         raise SNNCudaError(status, lib.snncuda_last_error().decode("utf-8", "replace"))
 
 
+def _tuning_struct(tuning: Dict[str, object]) -> _abi.Tuning:
+    """A Tuning from the dict autotune returns (missing fields stay 0)."""
+    t = _abi.Tuning()
+    for name, _ in _abi.Tuning._fields_:
+        if name in tuning:
+            setattr(t, name, tuning[name])
+    return t
+
+
 def _network_struct(c: Connectome):
     """snncuda_network view of a Connectome plus the arrays it points into
     (keep them alive until the create call returns)."""
@@ -262,6 +271,11 @@ class Simulation:
         return {name: (float(v) if isinstance(v, float) else int(v))
                 for name, v in ((n, getattr(out, n)) for n, _ in _abi.Tuning._fields_)}
 
+    def apply_tuning(self, tuning: Dict[str, object]) -> None:
+        """Apply launch shapes found earlier by autotune (its returned dict);
+        results do not depend on them (engine extension)."""
+        _check(self.lib, self.lib.snncuda_sim_apply_tuning(self.handle, ctypes.byref(_tuning_struct(tuning))))
+
     def evict(self) -> None:
         """Move the state to host memory and free the device memory; the next
         call that needs the device brings it back (engine extension)."""
@@ -380,6 +394,10 @@ class Batch:
         _check(self.lib, self.lib.snncuda_batch_autotune(self.handle, int(probe_ticks), ctypes.byref(out)))
         return {name: (float(v) if isinstance(v, float) else int(v))
                 for name, v in ((n, getattr(out, n)) for n, _ in _abi.Tuning._fields_)}
+
+    def apply_tuning(self, tuning: Dict[str, object]) -> None:
+        """Simulation.apply_tuning on the batch's tick loop."""
+        _check(self.lib, self.lib.snncuda_batch_apply_tuning(self.handle, ctypes.byref(_tuning_struct(tuning))))
 
     def checksums(self) -> List[tuple]:
         """Device-computed (neuron, synapse) checksums of every network, equal

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from snncuda_gb300 import synthetic
-from snncuda_gb300.simulation import Batch, Simulation, default_config
+from snncuda_gb300.simulation import Batch, SNNCudaError, Simulation, default_config
 
 
 def _members():
@@ -207,3 +207,34 @@ def test_slot_capacity_change_keeps_queued_events(gpu_lib, port_lib, members):
     assert sims[0].counters()["fired_spikes"] == sims[1].counters()["fired_spikes"]
     for s in sims:
         s.close()
+
+
+@pytest.mark.gpu
+def test_applied_tuning_keeps_results(gpu_lib, members):
+    """A tuning applied by hand (multi-pass grouping with a tiny pass, the
+    temporal update and post-spike STDP in tick order, other grid sizes)
+    leaves every network's state and raster unchanged; a field outside the
+    autotuner's ranges is refused before anything changes."""
+    def run(tune):
+        b = Batch([c for _, c, _ in members], _config(gpu_lib), gpu_lib, stdp_enabled=RULE)
+        for i, (_, _, d) in enumerate(members):
+            b.inject(i, *d)
+        b.run_until(39)
+        if tune:
+            t = b.autotune(probe_ticks=2)
+            t.update(scatter_pass_events=64, side_serial=1 - t["side_serial"], grid_bucket=7,
+                     ticks_per_graph=5)
+            b.apply_tuning(t)
+            bad = dict(t, grid_bucket=10 ** 6)
+            with pytest.raises(SNNCudaError):
+                b.apply_tuning(bad)
+        b.run_until(299)
+        out = ([b.digests()[i] for i in range(b.count)], [b.raster(i) for i in range(b.count)], b.checksums())
+        b.close()
+        return out
+
+    plain, tuned = run(False), run(True)
+    assert plain[0] == tuned[0]
+    assert plain[2] == tuned[2]
+    for x, y in zip(plain[1], tuned[1]):
+        assert all(np.array_equal(p, q) for p, q in zip(x, y))
