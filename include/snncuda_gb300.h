@@ -473,9 +473,9 @@ int snncuda_group_events(const uint64_t* events, uint32_t count, uint32_t neuron
  * allocator), and latency-critical loops that must not pay cudaMalloc /
  * cudaFree, which can synchronize the whole device and stall other streams.
  * Same arguments and results as snncuda_group_events; the caller still
- * provides the inputs and outputs, but the scratch (per-neuron counters,
- * scan tiles, the unsorted groups) lives in one static device array compiled
- * into the library (about 11 MB, held on every GPU that loads the library
+ * provides the inputs and outputs, but the scratch (bucket counters, the
+ * events in bucket order) lives in one static device array compiled
+ * into the library (about 17 MB, held on every GPU that loads the library
  * until the process exits).  Limits: count <= SNNCUDA_GROUP_STATIC_MAX_EVENTS
  * and neuron_count <= SNNCUDA_GROUP_STATIC_MAX_NEURONS, otherwise
  * SNNCUDA_ERR_CAPACITY.  The first call on a device looks up the array's

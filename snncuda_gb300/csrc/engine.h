@@ -192,6 +192,16 @@ struct Tables {
 };
 
 // Everything a tick needs, passed by value to the kernels.
+// One due event placed in its bucket by k_bscatter: the due-list word with
+// its due index in the low bits (payload << 32 | due index | external bit)
+// and its target within the bucket.  16 bytes, so the scattered placement is
+// one store per event.
+struct alignas(16) BucketEntry {
+    unsigned long long ev;
+    uint32_t ltgt;
+    uint32_t unused;
+};
+
 struct Engine {
     uint32_t N;
     uint32_t W;             // wheel slots (power of two)
@@ -234,7 +244,7 @@ struct Engine {
     uint32_t grid_bucket;
     // Due-list events per placing pass of k_bscatter (0: one pass): a due
     // list longer than this is placed in passes over disjoint bucket ranges,
-    // so the lines of grp_tmp / grp_ltgt being filled stay in L2 until
+    // so the lines of grp_tmp being filled stay in L2 until
     // complete instead of going to DRAM half-written.
     uint32_t scatter_pass_events;
     // 1: k_temporal and k_post run on the main stream in tick order instead
@@ -249,8 +259,7 @@ struct Engine {
     uint32_t* seg_start;                   // [N + 1] first grouped position of each target
     unsigned long long* grp;               // [slot_cap] due events grouped by target, due order inside
                                            // a target: (payload << 32) | (due index | ext << 31)
-    unsigned long long* grp_tmp;           // [slot_cap] the due events in bucket order (unsorted inside)
-    uint16_t* grp_ltgt;                    // [slot_cap] target of each grp_tmp entry within its bucket
+    BucketEntry* grp_tmp;                  // [slot_cap] the due events in bucket order (unsorted inside)
     EvIn* evin;                            // [slot_cap] per-event inputs of k_process, grouped, due order
     SynPre* ev_a0;                         // [slot_cap] each synaptic event's changing fields before it
     uint32_t* fire_bits;                   // [slot_cap/32] bitmap of due positions that fired
@@ -281,7 +290,7 @@ struct Engine {
 };
 
 constexpr uint32_t kMaxBuckets = 16384;   // target buckets of the grouping (shared-memory counters)
-constexpr uint32_t kScatterPassEvents = 1u << 22;  // default Engine::scatter_pass_events (42 MB of grp_tmp + grp_ltgt)
+constexpr uint32_t kScatterPassEvents = 1u << 22;  // default Engine::scatter_pass_events (64 MB of grp_tmp)
 constexpr uint32_t kMaxBucketShift = 14;  // at most 2^14 targets per bucket: N <= 2^28
 
 // Targets per bucket (log2) for N targets: the smallest 2^s >= 256 with at

@@ -708,24 +708,42 @@ __device__ uint32_t block_scan_shared(uint32_t* a, uint32_t n) {
     return total;
 }
 
-// Moves the far-future injections whose delivery tick t + W - 1 just became
-// addressable into the (empty) slot of that tick.  One block.
-__device__ void move_far_injections(const Engine& e, uint32_t t) {
+// The far-future injections whose delivery tick t + W - 1 becomes
+// addressable at tick t: far_ev[b, en), for wheel slot `slot`.
+__device__ __forceinline__ bool far_range(const Engine& e, uint32_t t, uint32_t& b, uint32_t& en, uint32_t& slot) {
     const uint32_t ft = e.ts->far_ticks;
-    if (ft == 0) return;
+    if (ft == 0) return false;
     const long long rel = static_cast<long long>(t) + e.W - 1 - e.ts->far_first_tick;
-    if (rel < 0 || rel >= ft) return;
-    const uint32_t b = e.far_idx[rel], en = e.far_idx[rel + 1];
-    const uint32_t slot = (t + e.W - 1) & e.wmask;
+    if (rel < 0 || rel >= ft) return false;
+    b = e.far_idx[rel];
+    en = e.far_idx[rel + 1];
+    slot = (t + e.W - 1) & e.wmask;
+    return en > b;
+}
+
+// Copies them behind the slot's current events, spread over the whole grid
+// (k_bcount; the slot is not the one being grouped, and its count changes
+// only in k_bscan, after every block has copied its share).
+__device__ void copy_far_injections(const Engine& e, uint32_t t) {
+    uint32_t b, en, slot;
+    if (!far_range(e, t, b, en, slot)) return;
     const uint32_t base = e.slot_count[slot];
-    if (base + (en - b) > e.slot_cap) {
-        if (threadIdx.x == 0) raise_status(e, kStatusSlotOverflow);
+    if (static_cast<unsigned long long>(base) + (en - b) > e.slot_cap) return;  // k_bscan raises it
+    unsigned long long* dst = e.wheel + static_cast<size_t>(slot) * e.slot_cap + base;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < en - b; i += gridDim.x * blockDim.x)
+        dst[i] = e.far_ev[b + i];
+}
+
+// Their slot's new count (one thread of k_bscan).
+__device__ void count_far_injections(const Engine& e, uint32_t t) {
+    uint32_t b, en, slot;
+    if (!far_range(e, t, b, en, slot)) return;
+    const uint32_t base = e.slot_count[slot];
+    if (static_cast<unsigned long long>(base) + (en - b) > e.slot_cap) {
+        raise_status(e, kStatusSlotOverflow);
         return;
     }
-    unsigned long long* dst = e.wheel + static_cast<size_t>(slot) * e.slot_cap + base;
-    for (uint32_t i = threadIdx.x; i < en - b; i += blockDim.x) dst[i] = e.far_ev[b + i];
-    __syncthreads();
-    if (threadIdx.x == 0) e.slot_count[slot] = base + (en - b);
+    e.slot_count[slot] = base + (en - b);
 }
 
 // This block's chunk [beg, end) of a due list of n events.
@@ -746,7 +764,7 @@ __global__ void __launch_bounds__(kBucketThreads) k_bcount(Engine e) {
     tick_enter();
     extern __shared__ uint32_t s_hist[];  // [nbuckets]
     const uint32_t t = e.ts->tick;
-    if (blockIdx.x == 0) move_far_injections(e, t);
+    copy_far_injections(e, t);
     const uint32_t B = e.nbuckets;
     for (uint32_t b = threadIdx.x; b < B; b += blockDim.x) s_hist[b] = 0;
     __syncthreads();
@@ -827,6 +845,7 @@ __global__ void __launch_bounds__(kThreads) k_bscan(Engine e) {
     if (threadIdx.x == 0) {
         e.bstart[B] = s_carry;
         e.seg_start[e.N] = s_carry;
+        count_far_injections(e, e.ts->tick);
     }
 }
 
@@ -871,8 +890,8 @@ __global__ void __launch_bounds__(kBucketThreads) k_bscatter(Engine e) {
                 const uint32_t b = tgt >> e.bucket_shift;
                 if (b < blo || b >= bhi) continue;
                 const uint32_t pos = atomicAdd(&s_pos[b], 1u);
-                e.grp_tmp[pos] = (v[u] & 0xFFFFFFFF00000000ull) | (i | (lo & kExternalBit));
-                e.grp_ltgt[pos] = static_cast<uint16_t>(tgt & lmask);
+                reinterpret_cast<uint4*>(e.grp_tmp)[pos] =
+                    make_uint4(i | (lo & kExternalBit), static_cast<uint32_t>(v[u] >> 32), tgt & lmask, 0u);
             }
         }
     }
@@ -979,8 +998,7 @@ __global__ void __launch_bounds__(kThreads) k_bsort(Engine e) {
         const uint32_t lo = e.bstart[b], hi = e.bstart[b + 1], m = hi - lo;
         const uint32_t n0 = b << e.bucket_shift;
         const uint32_t nw = e.N - n0 < width ? e.N - n0 : width;
-        const unsigned long long* in = e.grp_tmp + lo;
-        const uint16_t* lt = e.grp_ltgt + lo;
+        const uint4* in = reinterpret_cast<const uint4*>(e.grp_tmp) + lo;
         const bool small = m <= kSortSmemEvents;
         unsigned long long v[kSortPerThread];
         uint32_t t16[kSortPerThread];
@@ -988,8 +1006,9 @@ __global__ void __launch_bounds__(kThreads) k_bsort(Engine e) {
 #pragma unroll
             for (uint32_t k = 0; k < kSortPerThread; ++k) {
                 const uint32_t i = threadIdx.x + k * kThreads;
-                t16[k] = i < m ? lt[i] : 0u;
-                v[k] = i < m ? in[i] : 0ull;
+                const uint4 q = i < m ? in[i] : make_uint4(0u, 0u, 0u, 0u);
+                t16[k] = q.z;
+                v[k] = (static_cast<unsigned long long>(q.y) << 32) | q.x;
             }
         }
         for (uint32_t j = threadIdx.x; j < nw; j += blockDim.x) s_cnt[j] = 0;
@@ -999,7 +1018,7 @@ __global__ void __launch_bounds__(kThreads) k_bsort(Engine e) {
             for (uint32_t k = 0; k < kSortPerThread; ++k)
                 if (threadIdx.x + k * kThreads < m) atomicAdd(&s_cnt[t16[k]], 1u);
         } else {
-            for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) atomicAdd(&s_cnt[lt[i]], 1u);
+            for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) atomicAdd(&s_cnt[in[i].z], 1u);
         }
         __syncthreads();
         uint32_t nz = 0;  // targets with events (statistics)
@@ -1016,7 +1035,10 @@ __global__ void __launch_bounds__(kThreads) k_bsort(Engine e) {
             __syncthreads();
             for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) e.grp[lo + i] = s_sort[i];
         } else {
-            for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) e.grp[lo + atomicAdd(&s_cnt[lt[i]], 1u)] = in[i];
+            for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+                const uint4 q = in[i];
+                e.grp[lo + atomicAdd(&s_cnt[q.z], 1u)] = (static_cast<unsigned long long>(q.y) << 32) | q.x;
+            }
         }
         __syncthreads();
     }
@@ -1039,7 +1061,7 @@ __global__ void __launch_bounds__(kThreads) k_segsort(Engine e) {
             warp_bitonic(v, key);
             if (lane < static_cast<int>(len)) g[lane] = v;
         } else {
-            unsigned long long* tmp = e.grp_tmp + beg;
+            unsigned long long* tmp = reinterpret_cast<unsigned long long*>(e.grp_tmp) + beg;
             warp_merge_sort(g, tmp, len);  // sorted into tmp
             for (uint32_t k = lane; k < len; k += 32) g[k] = tmp[k];
             __syncwarp();
@@ -1220,7 +1242,9 @@ __device__ __forceinline__ void events_of_target(const Engine& e, uint32_t n, ui
         __syncwarp();
         return;
     }
-    unsigned long long* srt = e.grp_tmp + beg;  // grp_tmp is free once the groups are built
+    // grp_tmp is free once the groups are built (16 bytes per event: room for
+    // two 8-byte words each)
+    unsigned long long* srt = reinterpret_cast<unsigned long long*>(e.grp_tmp) + beg;
     warp_merge_sort(e.grp + beg, srt, len);
     const NeuronParam p = e.nparam[n];
     for (uint32_t j = lane; j < len; j += 32) {

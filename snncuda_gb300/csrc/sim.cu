@@ -463,8 +463,7 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.bstart = salloc<uint32_t>(sim, static_cast<size_t>(e.nbuckets) + 1, BufKind::kScratch);
     e.bcur = salloc<uint32_t>(sim, e.nbuckets, BufKind::kScratch);
     e.grp = salloc<unsigned long long>(sim, slot_cap, BufKind::kScratch);
-    e.grp_tmp = salloc<unsigned long long>(sim, slot_cap, BufKind::kScratch);
-    e.grp_ltgt = salloc<uint16_t>(sim, slot_cap, BufKind::kScratch);
+    e.grp_tmp = salloc<BucketEntry>(sim, slot_cap, BufKind::kScratch);
     e.evin = salloc<EvIn>(sim, slot_cap, BufKind::kScratch);
     e.ev_a0 = salloc<SynPre>(sim, slot_cap, BufKind::kScratch);
     e.fire_bits = salloc<uint32_t>(sim, bit_words, BufKind::kZero);
@@ -533,6 +532,10 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
         1, std::min<uint64_t>(std::max<uint64_t>((N + 255) / 256, std::min<uint64_t>(sms * 3ull, (N + 63) / 64)),
                               sms * 8ull)));
     e.grid_fire = static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>(fire_tiles, sms * 8ull)));
+    // large networks: the temporal update and post-spike STDP in tick order
+    // (beside k_events they slowed it by more than their own time on a 1e9-
+    // synapse network; neutral at 1e8 synapses)
+    e.side_serial = e.S >= (1ull << 27) ? 1u : 0u;
     sim->ensure_far(1, 2);
     check(cudaStreamSynchronize(st), "create synchronize");
 }
@@ -564,7 +567,7 @@ void remap_engine(Engine& e, const DeviceBuffers& from, const DeviceBuffers& to)
     fix(e.in_ptr); fix(e.nparam); fix(e.nrec); fix(e.ntp); fix(e.cand); fix(e.refmeta); fix(e.ring); fix(e.syn);
     fix(e.lcode); fix(e.pre_base); fix(e.pre_off); fix(e.pre_ev); fix(e.cls_delta); fix(e.wheel);
     fix(e.slot_count); fix(e.bcnt); fix(e.btot); fix(e.bstart); fix(e.bcur); fix(e.seg_start); fix(e.grp);
-    fix(e.grp_tmp); fix(e.grp_ltgt); fix(e.evin); fix(e.ev_a0); fix(e.fire_bits); fix(e.fire_at);
+    fix(e.grp_tmp); fix(e.evin); fix(e.ev_a0); fix(e.fire_bits); fix(e.fire_at);
     fix(e.fire_tile); fix(e.fire_list); fix(e.fired_tgt); fix(e.fired_cnt); fix(e.xsum); fix(e.xdst);
     fix(e.xdst_ok); fix(e.raster); fix(e.ts); fix(e.tab.decay); fix(e.tab.ltp); fix(e.tab.ltd);
 }
@@ -735,8 +738,7 @@ void resize_slots(snncuda_sim* sim, uint64_t cap) {
     sim->drop_graphs();
     realloc_buf(e.wheel, static_cast<size_t>(e.W) * cap * 8);
     realloc_buf(e.grp, cap * 8);
-    realloc_buf(e.grp_tmp, cap * 8);
-    realloc_buf(e.grp_ltgt, cap * 2);
+    realloc_buf(e.grp_tmp, cap * sizeof(BucketEntry));
     realloc_buf(e.evin, cap * sizeof(EvIn));
     realloc_buf(e.ev_a0, cap * sizeof(SynPre));
     realloc_buf(e.fire_at, cap * 4);
@@ -1571,8 +1573,7 @@ struct GroupScratch {
     uint32_t* btot;       // buckets
     uint32_t* bstart;     // buckets + 1
     uint32_t* bcur;       // buckets
-    unsigned long long* grp_tmp;  // count
-    uint16_t* grp_ltgt;   // count
+    BucketEntry* grp_tmp;  // count
     uint32_t* slot_count;
     TickState* ts;
 };
@@ -1589,7 +1590,7 @@ uint32_t group_buckets(uint32_t neuron_count) {
 // The tick's grouping kernels (k_bcount .. k_bsort) on a caller's event
 // buffer seen as a one-slot wheel.  Scratch sizes: kGroupGrid x
 // group_buckets() counts, group_buckets() (+1) bucket totals, starts and
-// cursors, `count` entries of bucket-ordered events and their targets.
+// cursors, `count` bucket-ordered events (BucketEntry).
 void group_run(const uint64_t* events, uint32_t count, uint32_t neuron_count, uint64_t* grouped,
                uint32_t* segment_start, cudaStream_t st, const GroupScratch& sc) {
     int dev = 0, sms = 0;
@@ -1613,7 +1614,6 @@ void group_run(const uint64_t* events, uint32_t count, uint32_t neuron_count, ui
     e.seg_start = segment_start;
     e.grp = reinterpret_cast<unsigned long long*>(grouped);
     e.grp_tmp = sc.grp_tmp;
-    e.grp_ltgt = sc.grp_ltgt;
     e.ts = sc.ts;
     e.grid_wide = static_cast<uint32_t>(std::max(1, sms * 2));
     configure_kernels();
@@ -1647,8 +1647,7 @@ int snncuda_group_events(const uint64_t* events, uint32_t count, uint32_t neuron
         sc.btot = dalloc<uint32_t>(owned, buckets);
         sc.bstart = dalloc<uint32_t>(owned, static_cast<size_t>(buckets) + 1);
         sc.bcur = dalloc<uint32_t>(owned, buckets);
-        sc.grp_tmp = dalloc<unsigned long long>(owned, count);
-        sc.grp_ltgt = dalloc<uint16_t>(owned, count);
+        sc.grp_tmp = dalloc<BucketEntry>(owned, count);
         sc.slot_count = dalloc<uint32_t>(owned, 1);
         sc.ts = dalloc<TickState>(owned, 1);
         group_run(events, count, neuron_count, grouped, segment_start, st, sc);
@@ -1662,7 +1661,7 @@ namespace {
 
 // Static scratch of snncuda_group_events_static: bucket counters and the
 // bucket-ordered events for at most kStaticEvents events over kStaticNeurons
-// neurons (about 11 MB).
+// neurons (about 17 MB).
 constexpr size_t kStaticEvents = SNNCUDA_GROUP_STATIC_MAX_EVENTS;
 constexpr size_t kStaticNeurons = SNNCUDA_GROUP_STATIC_MAX_NEURONS;
 constexpr size_t kStaticBuckets = (kStaticNeurons + 255) / 256;  // bucket_shift_for(2^18) == 8
@@ -1673,8 +1672,7 @@ constexpr size_t kOffBtot = kOffBcnt + align256(kGroupGrid * kStaticBuckets * 4)
 constexpr size_t kOffBstart = kOffBtot + align256(kStaticBuckets * 4);
 constexpr size_t kOffBcur = kOffBstart + align256((kStaticBuckets + 1) * 4);
 constexpr size_t kOffGrpTmp = kOffBcur + align256(kStaticBuckets * 4);
-constexpr size_t kOffLtgt = kOffGrpTmp + align256(kStaticEvents * 8);
-constexpr size_t kOffSlot = kOffLtgt + align256(kStaticEvents * 2);
+constexpr size_t kOffSlot = kOffGrpTmp + align256(kStaticEvents * sizeof(BucketEntry));
 constexpr size_t kOffTs = kOffSlot + 256;
 constexpr size_t kStaticBytes = kOffTs + align256(sizeof(TickState));
 
@@ -1725,8 +1723,7 @@ int snncuda_group_events_static(const uint64_t* events, uint32_t count, uint32_t
         sc.btot = reinterpret_cast<uint32_t*>(base + kOffBtot);
         sc.bstart = reinterpret_cast<uint32_t*>(base + kOffBstart);
         sc.bcur = reinterpret_cast<uint32_t*>(base + kOffBcur);
-        sc.grp_tmp = reinterpret_cast<unsigned long long*>(base + kOffGrpTmp);
-        sc.grp_ltgt = reinterpret_cast<uint16_t*>(base + kOffLtgt);
+        sc.grp_tmp = reinterpret_cast<BucketEntry*>(base + kOffGrpTmp);
         sc.slot_count = reinterpret_cast<uint32_t*>(base + kOffSlot);
         sc.ts = reinterpret_cast<TickState*>(base + kOffTs);
         group_run(events, count, neuron_count, grouped, segment_start, st, sc);
@@ -2067,7 +2064,7 @@ static uint64_t estimate_bytes_impl(const snncuda_network* net, const snncuda_co
     // grouping: bucket counters of up to 512 chunks
     const uint64_t buckets = (N + 255) / 256 < kMaxBuckets ? (N + 255) / 256 + 1 : kMaxBuckets;
     const uint64_t persistent = 64 * S + 8 * S + 8 * pre_total + neuron_bytes + lcode +
-                                W * slot_cap * 8 + slot_cap * (8 + 8 + 2 + 16 + 16 + 4 + 1) + 512 * 4 * buckets +
+                                W * slot_cap * 8 + slot_cap * (8 + 16 + 16 + 16 + 4 + 1) + 512 * 4 * buckets +
                                 fire_cap * 4 + (fire_cap / 8 + 1) * 12 * std::max<uint64_t>(D, 1) +
                                 16 * cfg.raster_capacity + (16u << 20);
     const uint64_t transient = S * (23 + 8 + 12 + 8) + 4 * (has_codes ? net->code_offset_ptr[S] : 0) +
