@@ -103,9 +103,12 @@ LAYOUT_BYTES = {
     "k_process": (16, 16, 4 + 2 * 52),
 }
 # DRAM bytes (read + write) per synaptic event of a kernel, from one ncu
-# capture of this code on a 20,000-neuron case of the workload (profiles/);
-# roofline.traffic scales it to the events of one full-size launch.
-MEASURED_TRAFFIC_PER_EVENT = {}
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of all 240 k_events
+# launches of the timed steps of a 20,000-neuron case of recog_1m (7.863 GB
+# over 59.87 M synaptic events: 127.2 B read, 4.2 B written; the records'
+# write-back happens after the kernel); roofline.traffic scales it to the
+# events of one full-size launch.
+MEASURED_TRAFFIC_PER_EVENT = {"k_events": 131.3}
 
 
 def load_peaks():
@@ -632,6 +635,51 @@ def sequential_by_size(solo):
             "speedup_if_batched_at_best_single_rate": (best * ms / 1e3) / ev if ev else None}
 
 
+def run_group_bench(args):
+    """`bench.py --group-bench EVENTS,TARGETS`: the tick's grouping kernels
+    alone, through snncuda_group_events, on a seeded random due list (targets
+    uniform, 1 % external inputs): `warmup` untimed calls, then `steps`
+    calls timed with CUDA events.  A device case of the grouping at the
+    recog_1m size (13e6 events, 1e6 targets) in about 0.5 GB, small enough
+    for a multi-pass ncu capture of one kernel."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from snncuda_gb300.simulation import _check, backend
+    lib = backend()
+    count, targets = (int(float(x)) for x in args.group_bench.split(","))
+    rng = np.random.default_rng(3)
+    tgt = rng.integers(0, targets, count, dtype=np.uint64)
+    ext = (rng.random(count) < 0.01).astype(np.uint64)
+    payload = rng.integers(0, 1 << 32, count, dtype=np.uint64)
+    ev = (payload << np.uint64(32)) | tgt | (ext << np.uint64(31))
+    d_ev = torch.from_numpy(ev.view(np.int64)).cuda()
+    d_out = torch.empty_like(d_ev)
+    d_seg = torch.empty(targets + 1, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def call():
+        _check(lib, lib.snncuda_group_events(d_ev.data_ptr(), count, targets, d_out.data_ptr(), d_seg.data_ptr(),
+                                             stream.cuda_stream))
+
+    for _ in range(max(args.warmup, 3)):
+        call()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        call()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    seg = d_seg.cpu().numpy().view(np.uint32)
+    ok = bool(seg[-1] == count and np.all(np.diff(seg.astype(np.int64)) == np.bincount(tgt.astype(np.int64),
+                                                                                    minlength=targets)))
+    return {"metric": "grouping_events_per_s", "value": count / (ms / 1e3), "unit": "events/s",
+            "ms_per_call": ms, "events": count, "targets": targets, "steps": args.steps,
+            "segments_match_counts": ok, "data": "synthetic (seed 3)"}
+
+
 def run_batched(args):
     """`bench.py --batched N`: the batched form on its own (batched_leg)."""
     import torch
@@ -788,6 +836,8 @@ def main():
                     help="time random 64-byte record read-modify-writes (the per-event access floor)")
     ap.add_argument("--rmw-args", default="",
                     help="records events [bands band_len picks rows row_len] for --rmw-floor")
+    ap.add_argument("--group-bench", default="",
+                    help="EVENTS,TARGETS: time snncuda_group_events alone on a random due list of that size")
     ap.add_argument("--serve", action="store_true", help="serving: Poisson arrivals under a memory budget")
     ap.add_argument("--serve-rate", type=float, default=4.0, help="job arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=15.0, help="arrival window")
@@ -811,6 +861,9 @@ def main():
         return
     if args.batched:
         print(json.dumps(run_batched(args)), flush=True)
+        return
+    if args.group_bench:
+        print(json.dumps(run_group_bench(args)), flush=True)
         return
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

@@ -758,41 +758,123 @@ __device__ __forceinline__ void chunk_of(uint32_t n, uint32_t& beg, uint32_t& en
 // thread has in flight per round (independent loads: the kernels stream the
 // due list and would otherwise wait a DRAM latency per entry).
 constexpr int kBucketThreads = 1024;
-constexpr int kBucketUnroll = 4;
+
+// The counting and placing blocks stream their chunk of the due list through
+// shared memory: tiles of kStreamTile entries (16 KB) by bulk copy (TMA),
+// two copies in flight per block, each waited for at most
+// Engine::stage_wait_ns.
+constexpr uint32_t kStreamTile = 2048;
+
+struct DueStream {
+    unsigned long long* buf;  // 2 x kStreamTile entries (shared memory)
+    unsigned long long* bar;  // 2 mbarriers (shared memory)
+    uint32_t parity[2];       // phase each buffer's barrier completes next
+    bool staging;             // false after a copy outlived its wait: no more copies
+};
+
+// Shared memory of k_bcount / k_bscatter: the bucket counters, then the
+// stream's two tiles (16-byte aligned).
+__host__ __device__ inline size_t stream_buf_offset(uint32_t nbuckets) {
+    return (static_cast<size_t>(nbuckets) * sizeof(uint32_t) + 15) & ~static_cast<size_t>(15);
+}
+
+// Calls f(i, src[i]) once for every i in [beg, end), spread over the block's
+// threads (every thread of the block must call it: it has block barriers;
+// the order of the calls is unspecified).  The 16-byte aligned even-length
+// body comes in by bulk copies; an unaligned first entry and an odd last
+// entry are read directly.  If a copy outlives
+// its wait, the block raises kStatusStageTimeout, drains the copies in
+// flight (bounded), and reads the rest from global memory, now and in later
+// calls.  Returns false only if a drain also failed (the block must exit).
+template <typename F>
+__device__ bool stream_due(const Engine& e, const unsigned long long* src, uint32_t beg, uint32_t end, DueStream& s,
+                           F&& f) {
+    uint32_t a0 = beg;
+    if (a0 < end && (reinterpret_cast<uintptr_t>(src + a0) & 15u) != 0) ++a0;
+    const uint32_t a1 = a0 + ((end - a0) & ~1u);
+    if (threadIdx.x == 0 && beg < a0) f(beg, src[beg]);
+    if (threadIdx.x == blockDim.x - 1 && a1 < end) f(a1, src[a1]);
+    // (an array that is not even 8-byte aligned is read directly)
+    if (!s.staging || (reinterpret_cast<uintptr_t>(src + a0) & 15u) != 0) {
+        for (uint32_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) f(i, __ldcs(src + i));
+        return true;
+    }
+    const uint32_t ntiles = (a1 - a0 + kStreamTile - 1) / kStreamTile;
+    auto tile_len = [&](uint32_t k) {
+        const uint32_t st = a0 + k * kStreamTile;
+        return a1 - st < kStreamTile ? a1 - st : kStreamTile;
+    };
+    auto issue = [&](uint32_t k) {
+        bulk_load(s.buf + (k & 1u) * kStreamTile, src + a0 + k * kStreamTile,
+                  tile_len(k) * static_cast<uint32_t>(sizeof(unsigned long long)), &s.bar[k & 1u]);
+    };
+    if (threadIdx.x == 0) {
+        if (ntiles > 0) issue(0);
+        if (ntiles > 1) issue(1);
+    }
+    for (uint32_t k = 0; k < ntiles; ++k) {
+        const uint32_t b = k & 1u;
+        const uint32_t st = a0 + k * kStreamTile;
+        const uint32_t cnt = tile_len(k);
+        if (!__syncthreads_and(mbar_wait(&s.bar[b], s.parity[b], e.stage_wait_ns))) {
+            // tiles k and (if issued) k + 1 are still in flight: drain them
+            // before the block goes on without shared memory
+            if (threadIdx.x == 0) raise_status(e, kStatusStageTimeout);
+            bool drained = mbar_wait(&s.bar[b], s.parity[b], kDrainWaitNs);
+            s.parity[b] ^= 1u;
+            if (k + 1 < ntiles) {
+                drained = mbar_wait(&s.bar[b ^ 1u], s.parity[b ^ 1u], kDrainWaitNs) && drained;
+                s.parity[b ^ 1u] ^= 1u;
+            }
+            if (!__syncthreads_and(drained)) return false;
+            s.staging = false;
+            for (uint32_t i = st + threadIdx.x; i < a1; i += blockDim.x) f(i, __ldcs(src + i));
+            return true;
+        }
+        const unsigned long long* tile = s.buf + b * kStreamTile;
+        for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) f(st + i, tile[i]);
+        s.parity[b] ^= 1u;
+        __syncthreads();  // the buffer is read: it may take tile k + 2
+        if (threadIdx.x == 0 && k + 2 < ntiles) issue(k + 2);
+    }
+    return true;
+}
 
 __global__ void __launch_bounds__(kBucketThreads) k_bcount(Engine e) {
     tick_enter();
-    extern __shared__ uint32_t s_hist[];  // [nbuckets]
+    extern __shared__ __align__(16) uint32_t s_hist[];  // [nbuckets], then the stream's tiles
+    __shared__ unsigned long long s_bar[2];
     const uint32_t t = e.ts->tick;
     copy_far_injections(e, t);
     const uint32_t B = e.nbuckets;
     for (uint32_t b = threadIdx.x; b < B; b += blockDim.x) s_hist[b] = 0;
+    if (threadIdx.x == 0) {
+        mbar_init(&s_bar[0], 1);
+        mbar_init(&s_bar[1], 1);
+    }
     __syncthreads();
     const uint32_t slot = t & e.wmask;
     const uint32_t n = e.slot_count[slot];
     const unsigned long long* ev = e.wheel + static_cast<size_t>(slot) * e.slot_cap;
     uint32_t beg, end;
     chunk_of(n, beg, end);
+    DueStream ds{reinterpret_cast<unsigned long long*>(reinterpret_cast<unsigned char*>(s_hist) + stream_buf_offset(B)),
+                 s_bar, {0u, 0u}, true};
     uint32_t ext = 0;
-    for (uint32_t i0 = beg + threadIdx.x; i0 < end; i0 += blockDim.x * kBucketUnroll) {
-        uint32_t lo[kBucketUnroll];
-#pragma unroll
-        for (int u = 0; u < kBucketUnroll; ++u) {
-            const uint32_t i = i0 + u * blockDim.x;
-            lo[u] = i < end ? static_cast<uint32_t>(__ldcs(ev + i)) : 0xFFFFFFFFu;
+    const bool ok = stream_due(e, ev, beg, end, ds, [&](uint32_t, unsigned long long v) {
+        const uint32_t lo = static_cast<uint32_t>(v);
+        const uint32_t tgt = lo & ~kExternalBit;
+        if (tgt >= e.N) {  // only reachable through snncuda_group_events with bad input
+            raise_status(e, kStatusBadEvent);
+            return;
         }
-#pragma unroll
-        for (int u = 0; u < kBucketUnroll; ++u) {
-            if (i0 + u * blockDim.x >= end) continue;
-            const uint32_t tgt = lo[u] & ~kExternalBit;
-            if (tgt >= e.N) {  // only reachable through snncuda_group_events with bad input
-                raise_status(e, kStatusBadEvent);
-                continue;
-            }
-            atomicAdd(&s_hist[tgt >> e.bucket_shift], 1u);
-            ext += lo[u] >> 31;
-        }
-    }
+        atomicAdd(&s_hist[tgt >> e.bucket_shift], 1u);
+        ext += lo >> 31;
+    });
+    // (if a drain failed the counts are partial and the tick is already
+    // flagged; the row is still written, and k_bscatter / k_bsort keep every
+    // access in bounds whatever the counts)
+    (void)ok;
     ext = __reduce_add_sync(0xffffffffu, ext);
     if ((threadIdx.x & 31) == 0 && ext) atomicAdd(&e.ts->external, static_cast<unsigned long long>(ext));
     __syncthreads();
@@ -851,49 +933,46 @@ __global__ void __launch_bounds__(kThreads) k_bscan(Engine e) {
 
 __global__ void __launch_bounds__(kBucketThreads) k_bscatter(Engine e) {
     tick_enter();
-    extern __shared__ uint32_t s_pos[];  // [nbuckets] next position of this chunk in each bucket
+    extern __shared__ __align__(16) uint32_t s_pos[];  // [nbuckets] next position of this chunk in each bucket
+    __shared__ unsigned long long s_bar[2];
     const uint32_t B = e.nbuckets;
     const uint32_t* row = e.bcnt + static_cast<size_t>(blockIdx.x) * B;
     for (uint32_t b = threadIdx.x; b < B; b += blockDim.x) {
         const uint32_t c = row[b];
         s_pos[b] = c ? atomicAdd(&e.bcur[b], c) : 0u;
     }
+    if (threadIdx.x == 0) {
+        mbar_init(&s_bar[0], 1);
+        mbar_init(&s_bar[1], 1);
+    }
     __syncthreads();
+    DueStream ds{reinterpret_cast<unsigned long long*>(reinterpret_cast<unsigned char*>(s_pos) + stream_buf_offset(B)),
+                 s_bar, {0u, 0u}, true};
     const uint32_t slot = e.ts->tick & e.wmask;
     const uint32_t n = e.ts->n_due;
     const unsigned long long* ev = e.wheel + static_cast<size_t>(slot) * e.slot_cap;
     const uint32_t lmask = (1u << e.bucket_shift) - 1u;
     uint32_t beg, end;
     chunk_of(n, beg, end);
-    // passes over disjoint bucket ranges (Engine::scatter_pass_events); the
-    // due list is re-read per pass with evict-first loads, which keep the
-    // L2 for the lines being filled
+    // passes over disjoint bucket ranges (Engine::scatter_pass_events): the
+    // due list is streamed again per pass
     const uint32_t per = e.scatter_pass_events;
     const uint32_t passes = per != 0 && n > per ? (n + per - 1) / per : 1u;
     for (uint32_t pass = 0; pass < passes; ++pass) {
         const uint32_t blo = static_cast<uint32_t>(static_cast<unsigned long long>(B) * pass / passes);
         const uint32_t bhi = static_cast<uint32_t>(static_cast<unsigned long long>(B) * (pass + 1) / passes);
-        for (uint32_t i0 = beg + threadIdx.x; i0 < end; i0 += blockDim.x * kBucketUnroll) {
-            unsigned long long v[kBucketUnroll];
-#pragma unroll
-            for (int u = 0; u < kBucketUnroll; ++u) {
-                const uint32_t i = i0 + u * blockDim.x;
-                v[u] = i < end ? __ldcs(ev + i) : 0ull;
-            }
-#pragma unroll
-            for (int u = 0; u < kBucketUnroll; ++u) {
-                const uint32_t i = i0 + u * blockDim.x;
-                if (i >= end) continue;
-                const uint32_t lo = static_cast<uint32_t>(v[u]);
-                const uint32_t tgt = lo & ~kExternalBit;
-                if (tgt >= e.N) continue;
-                const uint32_t b = tgt >> e.bucket_shift;
-                if (b < blo || b >= bhi) continue;
-                const uint32_t pos = atomicAdd(&s_pos[b], 1u);
-                reinterpret_cast<uint4*>(e.grp_tmp)[pos] =
-                    make_uint4(i | (lo & kExternalBit), static_cast<uint32_t>(v[u] >> 32), tgt & lmask, 0u);
-            }
-        }
+        const bool ok = stream_due(e, ev, beg, end, ds, [&](uint32_t i, unsigned long long v) {
+            const uint32_t lo = static_cast<uint32_t>(v);
+            const uint32_t tgt = lo & ~kExternalBit;
+            if (tgt >= e.N) return;
+            const uint32_t b = tgt >> e.bucket_shift;
+            if (b < blo || b >= bhi) return;
+            const uint32_t pos = atomicAdd(&s_pos[b], 1u);
+            if (pos >= e.slot_cap) return;  // only after a failed stream (counts partial)
+            reinterpret_cast<uint4*>(e.grp_tmp)[pos] =
+                make_uint4(i | (lo & kExternalBit), static_cast<uint32_t>(v >> 32), tgt & lmask, 0u);
+        });
+        if (!ok) return;
     }
 }
 
@@ -1016,9 +1095,12 @@ __global__ void __launch_bounds__(kThreads) k_bsort(Engine e) {
         if (small) {
 #pragma unroll
             for (uint32_t k = 0; k < kSortPerThread; ++k)
-                if (threadIdx.x + k * kThreads < m) atomicAdd(&s_cnt[t16[k]], 1u);
+                if (threadIdx.x + k * kThreads < m && t16[k] < nw) atomicAdd(&s_cnt[t16[k]], 1u);
         } else {
-            for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) atomicAdd(&s_cnt[in[i].z], 1u);
+            for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+                const uint32_t z = in[i].z;
+                if (z < nw) atomicAdd(&s_cnt[z], 1u);
+            }
         }
         __syncthreads();
         uint32_t nz = 0;  // targets with events (statistics)
@@ -1031,13 +1113,13 @@ __global__ void __launch_bounds__(kThreads) k_bsort(Engine e) {
         if (small) {
 #pragma unroll
             for (uint32_t k = 0; k < kSortPerThread; ++k)
-                if (threadIdx.x + k * kThreads < m) s_sort[atomicAdd(&s_cnt[t16[k]], 1u)] = v[k];
+                if (threadIdx.x + k * kThreads < m && t16[k] < nw) s_sort[atomicAdd(&s_cnt[t16[k]], 1u)] = v[k];
             __syncthreads();
             for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) e.grp[lo + i] = s_sort[i];
         } else {
             for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
                 const uint4 q = in[i];
-                e.grp[lo + atomicAdd(&s_cnt[q.z], 1u)] = (static_cast<unsigned long long>(q.y) << 32) | q.x;
+                if (q.z < nw) e.grp[lo + atomicAdd(&s_cnt[q.z], 1u)] = (static_cast<unsigned long long>(q.y) << 32) | q.x;
             }
         }
         __syncthreads();
@@ -2054,7 +2136,9 @@ static void launch_main(void (*kernel)(Engine), uint32_t grid, uint32_t block, s
 }
 
 // Dynamic shared memory of the grouping kernels.
-static size_t bucket_smem(const Engine& e) { return static_cast<size_t>(e.nbuckets) * sizeof(uint32_t); }
+static size_t bucket_smem(const Engine& e) {
+    return stream_buf_offset(e.nbuckets) + 2 * kStreamTile * sizeof(unsigned long long);
+}
 static size_t bsort_smem(const Engine& e) {
     return kSortSmemBytes + (static_cast<size_t>(1) << e.bucket_shift) * sizeof(uint32_t);
 }
@@ -2141,7 +2225,7 @@ void launch_group(const Engine& e, cudaStream_t stream) {
 void configure_kernels() {
     cudaFuncSetAttribute(k_process, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          static_cast<int>(kProcessSmem));
-    const int bucket_bytes = static_cast<int>(kMaxBuckets * sizeof(uint32_t));
+    const int bucket_bytes = static_cast<int>(stream_buf_offset(kMaxBuckets) + 2 * kStreamTile * sizeof(unsigned long long));
     cudaFuncSetAttribute(k_bcount, cudaFuncAttributeMaxDynamicSharedMemorySize, bucket_bytes);
     cudaFuncSetAttribute(k_bscatter, cudaFuncAttributeMaxDynamicSharedMemorySize, bucket_bytes);
     cudaFuncSetAttribute(k_bsort, cudaFuncAttributeMaxDynamicSharedMemorySize,

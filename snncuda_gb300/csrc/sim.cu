@@ -1607,6 +1607,7 @@ void group_run(const uint64_t* events, uint32_t count, uint32_t neuron_count, ui
     e.nbuckets = group_buckets(neuron_count);
     e.grid_bucket = kGroupGrid;
     e.scatter_pass_events = kScatterPassEvents;
+    e.stage_wait_ns = 100000000ull;  // the bulk copies' wait limit (as snncuda_config's default)
     e.bcnt = sc.bcnt;
     e.btot = sc.btot;
     e.bstart = sc.bstart;

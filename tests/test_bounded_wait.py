@@ -1,10 +1,11 @@
-"""The tick's one bounded device wait: k_process waits for the bulk copy of
-its block's event inputs into shared memory for at most
-snncuda_config.stage_wait_ns.  With a limit of 0 the wait gives up at once in
-every block: the blocks read their inputs from global memory instead, so the
-results stay bit-exact with the oracle, and the run reports
-SNNCUDA_ERR_TIMEOUT and poisons the handle.  Nothing faults or hangs: the
-copy still completes and is drained before its buffer is reused."""
+"""The tick's bounded device waits: k_process waits for the bulk copy of its
+block's event inputs into shared memory, and the grouping's counting and
+placing blocks for the bulk copies of their due-list tiles, each for at most
+snncuda_config.stage_wait_ns.  With a limit of 0 every wait gives up at once:
+the blocks read their inputs from global memory instead, so the results stay
+bit-exact with the oracle, and the run reports SNNCUDA_ERR_TIMEOUT and
+poisons the handle.  Nothing faults or hangs: the copies still complete and
+are drained (with a bounded wait) before their buffers are reused."""
 
 import pytest
 

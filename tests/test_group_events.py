@@ -119,3 +119,28 @@ def test_gpu_grouping_one_hot_target(gpu_lib, fn):
     want_g, want_s = expected_grouping(ev, neurons)
     assert np.array_equal(s, want_s)
     assert np.array_equal(g, want_g)
+
+
+@pytest.mark.gpu
+@pytest.mark.timeout(300)
+def test_gpu_grouping_unaligned_input_two_passes(gpu_lib):
+    """An input array that starts 8 bytes past a 16-byte boundary and has an
+    odd length (the counting and placing blocks stream their chunks with
+    bulk copies, which need 16-byte alignment: the first and last entries of
+    a chunk come in directly), and more than 2^22 events (placed in two
+    passes over the bucket ranges)."""
+    import torch
+    rng = np.random.default_rng(29)
+    count, neurons = (1 << 22) + 400_001, 300_000
+    ev = make_events(rng, count, neurons)
+    d_all = torch.zeros(count + 1, dtype=torch.int64, device="cuda")
+    d_all[1:] = torch.from_numpy(ev.view(np.int64)).cuda()
+    d_g = torch.zeros(count, dtype=torch.int64, device="cuda")
+    d_s = torch.zeros(neurons + 1, dtype=torch.int32, device="cuda")
+    rc = gpu_lib.snncuda_group_events(d_all.data_ptr() + 8, count, neurons, d_g.data_ptr(), d_s.data_ptr(),
+                                      torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert rc == 0
+    want_g, want_s = expected_grouping(ev, neurons)
+    assert np.array_equal(d_s.cpu().numpy().view(np.uint32), want_s)
+    assert np.array_equal(d_g.cpu().numpy().view(np.uint64), want_g)
