@@ -156,7 +156,7 @@ class SynapseState(Structure):
     ]
 
 
-KERNEL_COUNT = 11
+KERNEL_COUNT = 10
 
 
 class Profile(Structure):

@@ -306,7 +306,7 @@ constexpr uint32_t kMaxClasses = 256;    // distinct delivery delays
 // Host-side launchers (kernels.cu).
 // `marks` (optional) holds 2 * kKernelCount events recorded around every
 // kernel (before, after) for profiling graphs.
-constexpr int kKernelCount = 11;
+constexpr int kKernelCount = 10;
 // The streams of a tick: k_temporal and k_post run on `side`, forked from
 // `main` with ev[0] / ev[2] and joined back with ev[1] / ev[3].
 struct TickStreams {

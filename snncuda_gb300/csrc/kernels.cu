@@ -6,32 +6,33 @@
 // stream:
 //
 //  1. k_bcount     count due events per bucket of consecutive targets, per
-//                   chunk of the due list (and move far-future injections
+//                   chunk of the due list (and copy far-future injections
 //                   that become reachable into the wheel)
-//  2. k_bscan      bucket starts
-//  3. k_bscatter   place every event in its bucket
-//  4. k_bsort      per bucket: group by target, segment starts
-//  5. k_events     one warp per target with events: restore due order inside
+//  2. k_bscatter   bucket starts; place every event in its bucket
+//  3. k_bsort      per bucket: group by target, segment starts
+//  4. k_events     one warp per target with events: restore due order inside
 //                  its group, then per synapse (lanes in parallel) the event's
 //                  pre-spike STDP, pre-spike count and spike-code pattern
 //                  (SynapseDendriteProcessor.cpp:104-133, :318-365); writes
 //                  each event's input for the neuron walk
-//  6. k_process    one thread per touched target: the neuron's physics over
+//  5. k_process    one thread per touched target: the neuron's physics over
 //                  its events in due order (:175-229), redoing the STDP of
 //                  events that follow a fire of the target; fires into a
 //                  due-position bitmap
-//  7. k_fire_list  fires in due order (= reference fire order), raster
-//  8. k_fire_count events per (fire block, delay class); the last block scans
+//  6. k_fire_list  fires in due order (= reference fire order), raster
+//  7. k_fire_count events per (fire block, delay class); the last block scans
 //                  destinations and finishes the tick
-//  9. k_expand     copy each fire's pre-expanded (synapse, offset) events into
+//  8. k_expand     copy each fire's pre-expanded (synapse, offset) events into
 //                  their delivery slots, order-preserving
 //
-// and on a second stream (graph fork/join):
+// and two more, on a second stream (graph fork/join) beside the others, or
+// for networks of 2^27+ synapses on the main stream in tick order
+// (Engine::side_serial):
 //
-// 10. k_temporal   the neuron temporal pattern of every touched target, once
-//                  per tick, beside 5-6
-// 11. k_post       post-spike STDP over the in-rows of targets that fired
-//                  (:138-173), beside 7-9
+//  9. k_temporal   the neuron temporal pattern of every touched target, once
+//                  per tick, beside 4-5 (or before 4)
+// 10. k_post       post-spike STDP over the in-rows of targets that fired
+//                  (:138-173), beside 6-8 (or after 5)
 //
 // Main-stream kernels that directly follow another are launched as
 // programmatic dependents (tick_enter), so each is scheduled while the one
@@ -155,23 +156,28 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
 
 // Exclusive block scan of one value per thread (blockDim.x == kThreads).
 // Returns the exclusive prefix; *total receives the block sum.
-__device__ uint32_t block_excl_scan(uint32_t v, uint32_t* total) {
-    __shared__ uint32_t warp_sums[kThreads / 32];
+template <int kBlock>
+__device__ uint32_t block_excl_scan_t(uint32_t v, uint32_t* total) {
+    constexpr int kWarps = kBlock / 32;
+    static_assert(kWarps >= 1 && kWarps <= 32, "block size");
+    __shared__ uint32_t warp_sums[kWarps];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t incl = warp_incl_scan(v);
     if (lane == 31) warp_sums[warp] = incl;
     __syncthreads();
     if (warp == 0) {
-        uint32_t s = lane < kThreads / 32 ? warp_sums[lane] : 0;
+        uint32_t s = lane < kWarps ? warp_sums[lane] : 0;
         s = warp_incl_scan(s);
-        if (lane < kThreads / 32) warp_sums[lane] = s;
+        if (lane < kWarps) warp_sums[lane] = s;
     }
     __syncthreads();
     const uint32_t base = warp > 0 ? warp_sums[warp - 1] : 0;
-    if (total) *total = warp_sums[kThreads / 32 - 1];
+    if (total) *total = warp_sums[kWarps - 1];
     __syncthreads();
     return base + incl - v;
 }
+
+__device__ uint32_t block_excl_scan(uint32_t v, uint32_t* total) { return block_excl_scan_t<kThreads>(v, total); }
 
 // "Last block" hand-off: returns true in exactly one block, after every
 // block's prior global writes are visible.
@@ -673,8 +679,8 @@ __device__ void code_update(SynB& b, const NeuronParam& p, uint32_t t, uint16_t*
 //               bucket of 2^bucket_shift consecutive targets, counted in
 //               shared memory; the block's row of counts goes to bcnt and is
 //               added into the bucket totals (one atomic per nonzero bucket)
-//   k_bscan     one block: bucket starts (exclusive scan of the totals)
-//   k_bscatter  a block per chunk: one reservation per (chunk, bucket), then
+//   k_bscatter  a block per chunk: the bucket starts (every block scans the
+//               totals itself), one reservation per (chunk, bucket), then
 //               every event goes to its bucket's range of grp_tmp (order
 //               inside a bucket arbitrary)
 //   k_bsort     a block per bucket: a counting sort of the bucket's events by
@@ -723,18 +729,18 @@ __device__ __forceinline__ bool far_range(const Engine& e, uint32_t t, uint32_t&
 
 // Copies them behind the slot's current events, spread over the whole grid
 // (k_bcount; the slot is not the one being grouped, and its count changes
-// only in k_bscan, after every block has copied its share).
+// only in k_bscatter, after every block has copied its share).
 __device__ void copy_far_injections(const Engine& e, uint32_t t) {
     uint32_t b, en, slot;
     if (!far_range(e, t, b, en, slot)) return;
     const uint32_t base = e.slot_count[slot];
-    if (static_cast<unsigned long long>(base) + (en - b) > e.slot_cap) return;  // k_bscan raises it
+    if (static_cast<unsigned long long>(base) + (en - b) > e.slot_cap) return;  // k_bscatter raises it
     unsigned long long* dst = e.wheel + static_cast<size_t>(slot) * e.slot_cap + base;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < en - b; i += gridDim.x * blockDim.x)
         dst[i] = e.far_ev[b + i];
 }
 
-// Their slot's new count (one thread of k_bscan).
+// Their slot's new count (one thread of k_bscatter).
 __device__ void count_far_injections(const Engine& e, uint32_t t) {
     uint32_t b, en, slot;
     if (!far_range(e, t, b, en, slot)) return;
@@ -760,15 +766,15 @@ __device__ __forceinline__ void chunk_of(uint32_t n, uint32_t& beg, uint32_t& en
 constexpr int kBucketThreads = 1024;
 
 // The counting and placing blocks stream their chunk of the due list through
-// shared memory: tiles of kStreamTile entries (16 KB) by bulk copy (TMA),
+// shared memory: tiles of kStreamTile entries (32 KB) by bulk copy (TMA),
 // two copies in flight per block, each waited for at most
 // Engine::stage_wait_ns.
-constexpr uint32_t kStreamTile = 2048;
+constexpr uint32_t kStreamTile = 4096;
 
 struct DueStream {
     unsigned long long* buf;  // 2 x kStreamTile entries (shared memory)
     unsigned long long* bar;  // 2 mbarriers (shared memory)
-    uint32_t parity[2];       // phase each buffer's barrier completes next
+    uint32_t parity;          // bit b: phase buffer b's barrier completes next
     bool staging;             // false after a copy outlived its wait: no more copies
 };
 
@@ -816,15 +822,15 @@ __device__ bool stream_due(const Engine& e, const unsigned long long* src, uint3
         const uint32_t b = k & 1u;
         const uint32_t st = a0 + k * kStreamTile;
         const uint32_t cnt = tile_len(k);
-        if (!__syncthreads_and(mbar_wait(&s.bar[b], s.parity[b], e.stage_wait_ns))) {
+        if (!__syncthreads_and(mbar_wait(&s.bar[b], (s.parity >> b) & 1u, e.stage_wait_ns))) {
             // tiles k and (if issued) k + 1 are still in flight: drain them
             // before the block goes on without shared memory
             if (threadIdx.x == 0) raise_status(e, kStatusStageTimeout);
-            bool drained = mbar_wait(&s.bar[b], s.parity[b], kDrainWaitNs);
-            s.parity[b] ^= 1u;
+            bool drained = mbar_wait(&s.bar[b], (s.parity >> b) & 1u, kDrainWaitNs);
+            s.parity ^= 1u << b;
             if (k + 1 < ntiles) {
-                drained = mbar_wait(&s.bar[b ^ 1u], s.parity[b ^ 1u], kDrainWaitNs) && drained;
-                s.parity[b ^ 1u] ^= 1u;
+                drained = mbar_wait(&s.bar[b ^ 1u], (s.parity >> (b ^ 1u)) & 1u, kDrainWaitNs) && drained;
+                s.parity ^= 1u << (b ^ 1u);
             }
             if (!__syncthreads_and(drained)) return false;
             s.staging = false;
@@ -833,7 +839,7 @@ __device__ bool stream_due(const Engine& e, const unsigned long long* src, uint3
         }
         const unsigned long long* tile = s.buf + b * kStreamTile;
         for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) f(st + i, tile[i]);
-        s.parity[b] ^= 1u;
+        s.parity ^= 1u << b;
         __syncthreads();  // the buffer is read: it may take tile k + 2
         if (threadIdx.x == 0 && k + 2 < ntiles) issue(k + 2);
     }
@@ -859,7 +865,7 @@ __global__ void __launch_bounds__(kBucketThreads) k_bcount(Engine e) {
     uint32_t beg, end;
     chunk_of(n, beg, end);
     DueStream ds{reinterpret_cast<unsigned long long*>(reinterpret_cast<unsigned char*>(s_hist) + stream_buf_offset(B)),
-                 s_bar, {0u, 0u}, true};
+                 s_bar, 0u, true};
     uint32_t ext = 0;
     const bool ok = stream_due(e, ev, beg, end, ds, [&](uint32_t, unsigned long long v) {
         const uint32_t lo = static_cast<uint32_t>(v);
@@ -891,55 +897,44 @@ __global__ void __launch_bounds__(kBucketThreads) k_bcount(Engine e) {
     }
 }
 
-// Bucket starts; the totals return to zero for the next tick.  One block.
-__global__ void __launch_bounds__(kThreads) k_bscan(Engine e) {
-    tick_enter();
-    const uint32_t B = e.nbuckets;
-    __shared__ uint32_t s_carry;
-    if (threadIdx.x == 0) s_carry = 0;
-    __syncthreads();
-    // kThreads x 16 buckets per round, 16 consecutive per thread
-    constexpr uint32_t kPer = 16;
-    for (uint32_t base = 0; base < B; base += kThreads * kPer) {
-        const uint32_t b0 = base + threadIdx.x * kPer;
-        uint32_t v[kPer];
-        uint32_t sum = 0;
-#pragma unroll
-        for (uint32_t j = 0; j < kPer; ++j) {
-            v[j] = b0 + j < B ? __ldcg(e.btot + b0 + j) : 0u;
-            sum += v[j];
-        }
-        uint32_t total;
-        uint32_t run = s_carry + block_excl_scan(sum, &total);
-#pragma unroll
-        for (uint32_t j = 0; j < kPer; ++j) {
-            if (b0 + j < B) {
-                e.bstart[b0 + j] = run;
-                e.bcur[b0 + j] = run;
-                e.btot[b0 + j] = 0;
-            }
-            run += v[j];
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) s_carry += total;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        e.bstart[B] = s_carry;
-        e.seg_start[e.N] = s_carry;
-        count_far_injections(e, e.ts->tick);
-    }
-}
-
 __global__ void __launch_bounds__(kBucketThreads) k_bscatter(Engine e) {
     tick_enter();
     extern __shared__ __align__(16) uint32_t s_pos[];  // [nbuckets] next position of this chunk in each bucket
     __shared__ unsigned long long s_bar[2];
     const uint32_t B = e.nbuckets;
+    {
+        // bucket starts: every block scans the bucket totals itself (a run of
+        // consecutive buckets per thread); block 0 publishes them
+        const uint32_t per = (B + blockDim.x - 1) / blockDim.x;
+        const uint32_t b0 = threadIdx.x * per < B ? threadIdx.x * per : B;
+        const uint32_t b1 = b0 + per < B ? b0 + per : B;
+        uint32_t sum = 0;
+        for (uint32_t b = b0; b < b1; ++b) {
+            const uint32_t c = __ldcg(e.btot + b);
+            s_pos[b] = c;
+            sum += c;
+        }
+        uint32_t total;
+        uint32_t run = block_excl_scan_t<kBucketThreads>(sum, &total);
+        for (uint32_t b = b0; b < b1; ++b) {
+            const uint32_t c = s_pos[b];
+            s_pos[b] = run;
+            if (blockIdx.x == 0) e.bstart[b] = run;
+            run += c;
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            e.bstart[B] = total;
+            e.seg_start[e.N] = total;
+            count_far_injections(e, e.ts->tick);
+        }
+        __syncthreads();
+    }
+    // this chunk's place in each bucket: behind the chunks that reserved
+    // before it (the cursors start at zero every tick; k_bsort clears them)
     const uint32_t* row = e.bcnt + static_cast<size_t>(blockIdx.x) * B;
     for (uint32_t b = threadIdx.x; b < B; b += blockDim.x) {
         const uint32_t c = row[b];
-        s_pos[b] = c ? atomicAdd(&e.bcur[b], c) : 0u;
+        if (c) s_pos[b] += atomicAdd(&e.bcur[b], c);
     }
     if (threadIdx.x == 0) {
         mbar_init(&s_bar[0], 1);
@@ -947,7 +942,7 @@ __global__ void __launch_bounds__(kBucketThreads) k_bscatter(Engine e) {
     }
     __syncthreads();
     DueStream ds{reinterpret_cast<unsigned long long*>(reinterpret_cast<unsigned char*>(s_pos) + stream_buf_offset(B)),
-                 s_bar, {0u, 0u}, true};
+                 s_bar, 0u, true};
     const uint32_t slot = e.ts->tick & e.wmask;
     const uint32_t n = e.ts->n_due;
     const unsigned long long* ev = e.wheel + static_cast<size_t>(slot) * e.slot_cap;
@@ -1110,6 +1105,10 @@ __global__ void __launch_bounds__(kThreads) k_bsort(Engine e) {
         block_scan_shared(s_cnt, nw);  // segment starts relative to lo
         for (uint32_t j = threadIdx.x; j < nw; j += blockDim.x) e.seg_start[n0 + j] = lo + s_cnt[j];
         __syncthreads();
+        if (threadIdx.x == 0) {  // the bucket's total and cursor start at zero next tick
+            e.btot[b] = 0;
+            e.bcur[b] = 0;
+        }
         if (small) {
 #pragma unroll
             for (uint32_t k = 0; k < kSortPerThread; ++k)
@@ -2163,20 +2162,19 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     };
     // k_bcount follows a wait on the side stream: a full dependency
     mark(false); launch_main(k_bcount, e.grid_bucket, kBucketThreads, bucket_smem(e), stream, false, e); mark(true);
-    mark(false); launch_main(k_bscan, 1, kThreads, 0, stream, dep, e); mark(true);
     mark(false); launch_main(k_bscatter, e.grid_bucket, kBucketThreads, bucket_smem(e), stream, dep, e); mark(true);
     mark(false); launch_main(k_bsort, bsort_grid(e), kThreads, bsort_smem(e), stream, dep, e); mark(true);
     if (e.side_serial) {
         // everything in tick order on the main stream; k_temporal and k_post
         // take a full dependency (they do not wait on a programmatic launch)
-        side_mark(9, false);
+        side_mark(8, false);
         k_temporal<<<e.grid_process, kThreads, 0, stream>>>(e);
-        side_mark(9, true);
+        side_mark(8, true);
         mark(false); launch_main(k_events, e.grid_events, kThreads, 0, stream, false, e); mark(true);
         mark(false); launch_main(k_process, e.grid_walk, kThreads, kProcessSmem, stream, dep, e); mark(true);
-        side_mark(10, false);
+        side_mark(9, false);
         k_post<<<wide * 4, kThreads, 0, stream>>>(e);
-        side_mark(10, true);
+        side_mark(9, true);
         mark(false); launch_main(k_fire_list, e.grid_fire, kThreads, 0, stream, false, e); mark(true);
         mark(false); launch_main(k_fire_count, e.grid_wide / 4 + 1, kFireCountThreads, 0, stream, false, e); mark(true);
         mark(false); launch_main(k_expand, e.grid_wide * 4, kThreads, 0, stream, dep, e); mark(true);
@@ -2186,9 +2184,9 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     // (it needs only the segment starts)
     cudaEventRecord(s.ev[0], stream);
     cudaStreamWaitEvent(s.side, s.ev[0], 0);
-    side_mark(9, false);
+    side_mark(8, false);
     k_temporal<<<e.grid_process, kThreads, 0, s.side>>>(e);
-    side_mark(9, true);
+    side_mark(8, true);
     cudaEventRecord(s.ev[1], s.side);
     mark(false); launch_main(k_events, e.grid_events, kThreads, 0, stream, dep, e); mark(true);
     mark(false); launch_main(k_process, e.grid_walk, kThreads, kProcessSmem, stream, dep, e); mark(true);
@@ -2196,9 +2194,9 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     // the expansion (synapse records are not touched by those)
     cudaEventRecord(s.ev[2], stream);
     cudaStreamWaitEvent(s.side, s.ev[2], 0);
-    side_mark(10, false);
+    side_mark(9, false);
     k_post<<<wide * 4, kThreads, 0, s.side>>>(e);
-    side_mark(10, true);
+    side_mark(9, true);
     cudaEventRecord(s.ev[3], s.side);
     mark(false); launch_main(k_fire_list, e.grid_fire, kThreads, 0, stream, dep, e); mark(true);
     cudaStreamWaitEvent(stream, s.ev[1], 0);  // k_temporal reads the tick counter k_fire_count advances
@@ -2208,15 +2206,14 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
 }
 
 const char* kernel_name(int index) {
-    static const char* names[kKernelCount] = {"k_bcount",    "k_bscan",      "k_bscatter",  "k_bsort",
-                                              "k_events",    "k_process",    "k_fire_list", "k_fire_count",
-                                              "k_expand",    "k_temporal",   "k_post"};
+    static const char* names[kKernelCount] = {"k_bcount",    "k_bscatter",  "k_bsort",    "k_events",
+                                              "k_process",   "k_fire_list", "k_fire_count", "k_expand",
+                                              "k_temporal",  "k_post"};
     return index >= 0 && index < kKernelCount ? names[index] : "";
 }
 
 void launch_group(const Engine& e, cudaStream_t stream) {
     k_bcount<<<e.grid_bucket, kBucketThreads, bucket_smem(e), stream>>>(e);
-    k_bscan<<<1, kThreads, 0, stream>>>(e);
     k_bscatter<<<e.grid_bucket, kBucketThreads, bucket_smem(e), stream>>>(e);
     k_bsort<<<bsort_grid(e), kThreads, bsort_smem(e), stream>>>(e);
     k_segsort<<<e.grid_wide * 4, kThreads, 0, stream>>>(e);

@@ -436,7 +436,11 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.bucket_shift = bucket_shift_for(N);
     if (e.bucket_shift == 0) throw_fail(SNNCUDA_ERR_UNSUPPORTED, "at most 2^28 neurons");
     e.nbuckets = static_cast<uint32_t>(std::max<uint64_t>(1, (static_cast<uint64_t>(N) + (1u << e.bucket_shift) - 1) >> e.bucket_shift));
-    e.grid_bucket = static_cast<uint32_t>(std::max(1, sms * 2));
+    // counting and placing blocks: two per SM, fewer for small networks (one
+    // per 2^18 synapses), whose grids then leave room for other streams'
+    // kernels (side-by-side jobs of a server)
+    e.grid_bucket = static_cast<uint32_t>(
+        std::max<uint64_t>(1, std::min<uint64_t>(sms * 2ull, (static_cast<uint64_t>(sim->S) + (1u << 18) - 1) >> 18)));
     e.scatter_pass_events = kScatterPassEvents;
     const uint32_t grid_bucket_max = static_cast<uint32_t>(std::max(1, sms * 4));  // the autotuner's largest
 
@@ -461,7 +465,7 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.bcnt = salloc<uint32_t>(sim, static_cast<size_t>(grid_bucket_max) * e.nbuckets, BufKind::kScratch);
     e.btot = salloc<uint32_t>(sim, e.nbuckets, BufKind::kZero);
     e.bstart = salloc<uint32_t>(sim, static_cast<size_t>(e.nbuckets) + 1, BufKind::kScratch);
-    e.bcur = salloc<uint32_t>(sim, e.nbuckets, BufKind::kScratch);
+    e.bcur = salloc<uint32_t>(sim, e.nbuckets, BufKind::kZero);
     e.grp = salloc<unsigned long long>(sim, slot_cap, BufKind::kScratch);
     e.grp_tmp = salloc<BucketEntry>(sim, slot_cap, BufKind::kScratch);
     e.evin = salloc<EvIn>(sim, slot_cap, BufKind::kScratch);
@@ -496,6 +500,7 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     h2d(d_cls, cls_delta.data(), cls_delta.size() * sizeof(uint32_t));
     zero(e.slot_count, sizeof(uint32_t) * W);
     zero(e.btot, sizeof(uint32_t) * e.nbuckets);
+    zero(e.bcur, sizeof(uint32_t) * e.nbuckets);
     zero(e.fire_bits, sizeof(uint32_t) * bit_words);
     zero(e.xsum, sizeof(uint32_t) * xblocks * std::max<uint32_t>(D, 1));
     zero(e.fire_tile, sizeof(uint32_t) * (fire_tiles + 2));
@@ -1619,6 +1624,7 @@ void group_run(const uint64_t* events, uint32_t count, uint32_t neuron_count, ui
     e.grid_wide = static_cast<uint32_t>(std::max(1, sms * 2));
     configure_kernels();
     check(cudaMemsetAsync(sc.btot, 0, sizeof(uint32_t) * e.nbuckets, st), "memset");
+    check(cudaMemsetAsync(sc.bcur, 0, sizeof(uint32_t) * e.nbuckets, st), "memset");
     check(cudaMemsetAsync(sc.ts, 0, sizeof(TickState), st), "memset");
     check(cudaMemcpyAsync(sc.slot_count, &count, sizeof(uint32_t), cudaMemcpyHostToDevice, st), "count");
     launch_group(e, st);
