@@ -800,9 +800,21 @@ __device__ bool stream_due(const Engine& e, const unsigned long long* src, uint3
     const uint32_t a1 = a0 + ((end - a0) & ~1u);
     if (threadIdx.x == 0 && beg < a0) f(beg, src[beg]);
     if (threadIdx.x == blockDim.x - 1 && a1 < end) f(a1, src[a1]);
-    // (an array that is not even 8-byte aligned is read directly)
-    if (!s.staging || (reinterpret_cast<uintptr_t>(src + a0) & 15u) != 0) {
-        for (uint32_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) f(i, __ldcs(src + i));
+    // Read directly (four loads in flight per thread): a chunk shorter than
+    // two tiles, where waiting for a whole tile costs more than it hides, an
+    // array that is not even 8-byte aligned, and after a failed copy.
+    if (!s.staging || a1 - a0 < 2 * kStreamTile || (reinterpret_cast<uintptr_t>(src + a0) & 15u) != 0) {
+        for (uint32_t i0 = a0 + threadIdx.x; i0 < a1; i0 += 4 * blockDim.x) {
+            unsigned long long v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t i = i0 + u * blockDim.x;
+                v[u] = i < a1 ? __ldcs(src + i) : 0ull;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (i0 + u * blockDim.x < a1) f(i0 + u * blockDim.x, v[u]);
+        }
         return true;
     }
     const uint32_t ntiles = (a1 - a0 + kStreamTile - 1) / kStreamTile;
@@ -822,16 +834,22 @@ __device__ bool stream_due(const Engine& e, const unsigned long long* src, uint3
         const uint32_t b = k & 1u;
         const uint32_t st = a0 + k * kStreamTile;
         const uint32_t cnt = tile_len(k);
-        if (!__syncthreads_and(mbar_wait(&s.bar[b], (s.parity >> b) & 1u, e.stage_wait_ns))) {
+        // one thread polls the barrier; the block barrier then orders its
+        // observation of the completed copy before every thread's reads
+        bool ready = true;
+        if (threadIdx.x == 0) ready = mbar_wait(&s.bar[b], (s.parity >> b) & 1u, e.stage_wait_ns);
+        if (!__syncthreads_and(ready)) {
             // tiles k and (if issued) k + 1 are still in flight: drain them
             // before the block goes on without shared memory
-            if (threadIdx.x == 0) raise_status(e, kStatusStageTimeout);
-            bool drained = mbar_wait(&s.bar[b], (s.parity >> b) & 1u, kDrainWaitNs);
-            s.parity ^= 1u << b;
-            if (k + 1 < ntiles) {
-                drained = mbar_wait(&s.bar[b ^ 1u], (s.parity >> (b ^ 1u)) & 1u, kDrainWaitNs) && drained;
-                s.parity ^= 1u << (b ^ 1u);
+            bool drained = true;
+            if (threadIdx.x == 0) {
+                raise_status(e, kStatusStageTimeout);
+                drained = mbar_wait(&s.bar[b], (s.parity >> b) & 1u, kDrainWaitNs);
+                if (k + 1 < ntiles)
+                    drained = mbar_wait(&s.bar[b ^ 1u], (s.parity >> (b ^ 1u)) & 1u, kDrainWaitNs) && drained;
             }
+            s.parity ^= 1u << b;
+            if (k + 1 < ntiles) s.parity ^= 1u << (b ^ 1u);
             if (!__syncthreads_and(drained)) return false;
             s.staging = false;
             for (uint32_t i = st + threadIdx.x; i < a1; i += blockDim.x) f(i, __ldcs(src + i));
