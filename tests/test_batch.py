@@ -210,9 +210,10 @@ def test_slot_capacity_change_keeps_queued_events(gpu_lib, port_lib, members):
 
 
 @pytest.mark.gpu
-def test_applied_tuning_keeps_results(gpu_lib, members):
-    """A tuning applied by hand (multi-pass grouping with a tiny pass, the
-    temporal update and post-spike STDP in tick order, other grid sizes)
+@pytest.mark.parametrize("side", [0, 1, 2])
+def test_applied_tuning_keeps_results(gpu_lib, members, side):
+    """A tuning applied by hand (multi-pass grouping with a tiny pass, each
+    placement of the temporal update and post-spike STDP, other grid sizes)
     leaves every network's state and raster unchanged; a field outside the
     autotuner's ranges is refused before anything changes."""
     def run(tune):
@@ -222,8 +223,7 @@ def test_applied_tuning_keeps_results(gpu_lib, members):
         b.run_until(39)
         if tune:
             t = b.autotune(probe_ticks=2)
-            t.update(scatter_pass_events=64, side_serial=1 - t["side_serial"], grid_bucket=7,
-                     ticks_per_graph=5)
+            t.update(scatter_pass_events=64, side_serial=side, grid_bucket=7, ticks_per_graph=5)
             b.apply_tuning(t)
             bad = dict(t, grid_bucket=10 ** 6)
             with pytest.raises(SNNCudaError):
