@@ -167,7 +167,9 @@ def test_autotuned_batch_keeps_results_and_checksums_match_solo(gpu_lib, port_li
     tuning = b.autotune(probe_ticks=8)
     assert tuning["probes"] >= 5 and tuning["max_slot_events"] > 0
     assert tuning["slot_event_capacity"] >= 2 * tuning["max_slot_events"]
-    b.run_until(299)
+    # the probes run the batch's own ticks: compare at a tick past them
+    last = max(299, b.counters(0)["next_tick"] + 40)
+    b.run_until(last)
     got = [(b.digests()[i], b.counters(i), b.raster(i)) for i in range(b.count)]
     sums = b.checksums()
     b.close()
@@ -176,7 +178,7 @@ def test_autotuned_batch_keeps_results_and_checksums_match_solo(gpu_lib, port_li
         cfg.stdp_enabled = 1 if RULE[i] else 0
         ref = Simulation(c, cfg, port_lib)
         ref.inject(*d)
-        ref.run_until(299)
+        ref.run_until(last)
         assert got[i][0] == ref.digest(), i
         assert got[i][1]["fired_spikes"] == ref.counters()["fired_spikes"], i
         ref.close()
@@ -184,7 +186,7 @@ def test_autotuned_batch_keeps_results_and_checksums_match_solo(gpu_lib, port_li
         cfg.stdp_enabled = 1 if RULE[i] else 0
         solo = Simulation(c, cfg, gpu_lib)
         solo.inject(*d)
-        solo.run_until(299)
+        solo.run_until(last)
         assert solo.checksum() == sums[i], i
         solo.close()
 
@@ -222,7 +224,8 @@ def test_applied_tuning_keeps_results(gpu_lib, members, side):
             b.inject(i, *d)
         b.run_until(39)
         if tune:
-            t = b.autotune(probe_ticks=2)
+            t = b.autotune(probe_ticks=2)  # about 70 ticks of probes: done well before tick 299
+            assert b.counters(0)["next_tick"] < 250
             t.update(scatter_pass_events=64, side_serial=side, grid_bucket=7, ticks_per_graph=5)
             b.apply_tuning(t)
             bad = dict(t, grid_bucket=10 ** 6)
