@@ -247,11 +247,10 @@ struct Engine {
     // so the lines of grp_tmp being filled stay in L2 until
     // complete instead of going to DRAM half-written.
     uint32_t scatter_pass_events;
-    // Where k_temporal and k_post run: 0 on the side stream, beside
-    // k_events / k_process and beside the fire ordering; 1 on the main
-    // stream in tick order (two random-access kernels side by side can take
-    // longer than one after the other); 2 k_temporal on the side stream
-    // beside k_process and the fire ordering only, k_post in tick order.
+    // 1: k_temporal and k_post run on the main stream in tick order instead
+    // of on the side stream beside k_events / k_process and beside the fire
+    // ordering (two random-access kernels side by side can take longer than
+    // one after the other).
     uint32_t side_serial;
     uint32_t* bcnt;                        // [grid_bucket][nbuckets] events of each (chunk, bucket)
     uint32_t* btot;                        // [nbuckets] events per bucket (zero between ticks)

@@ -1747,7 +1747,7 @@ __device__ __forceinline__ void temporal_target(const Engine& e, uint32_t n, uin
     e.ntp[n] = wq;
 }
 
-__global__ void __launch_bounds__(kThreads, 4) k_temporal(Engine e) {
+__global__ void __launch_bounds__(kThreads) k_temporal(Engine e) {
     tick_enter();  // (returns at once unless launched as a programmatic dependent)
     const uint32_t t = e.ts->tick;
     const int temporal = e.ts->temporal_enabled;
@@ -2178,33 +2178,13 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     auto side_mark = [&](int index, bool after) {
         if (marks)
             cudaEventRecordWithFlags(marks[2 * index + (after ? 1 : 0)],
-                                     e.side_serial == 1 || (e.side_serial == 2 && index == 9) ? stream : s.side,
+                                     e.side_serial ? stream : s.side,
                                      cudaEventRecordExternal);
     };
     // k_bcount follows a wait on the side stream: a full dependency
     mark(false); launch_main(k_bcount, e.grid_bucket, kBucketThreads, bucket_smem(e), stream, false, e); mark(true);
     mark(false); launch_main(k_bscatter, e.grid_bucket, kBucketThreads, bucket_smem(e), stream, dep, e); mark(true);
     mark(false); launch_main(k_bsort, bsort_grid(e), kThreads, bsort_smem(e), stream, dep, e); mark(true);
-    if (e.side_serial == 2) {
-        // k_temporal beside the walk and the fire ordering only (it starts
-        // after k_events), k_post in tick order on the main stream
-        mark(false); launch_main(k_events, e.grid_events, kThreads, 0, stream, dep, e); mark(true);
-        cudaEventRecord(s.ev[0], stream);
-        cudaStreamWaitEvent(s.side, s.ev[0], 0);
-        side_mark(8, false);
-        k_temporal<<<e.grid_process, kThreads, 0, s.side>>>(e);
-        side_mark(8, true);
-        cudaEventRecord(s.ev[1], s.side);
-        mark(false); launch_main(k_process, e.grid_walk, kThreads, kProcessSmem, stream, dep, e); mark(true);
-        side_mark(9, false);
-        launch_main(k_post, wide * 4, kThreads, 0, stream, dep, e);
-        side_mark(9, true);
-        mark(false); launch_main(k_fire_list, e.grid_fire, kThreads, 0, stream, dep, e); mark(true);
-        cudaStreamWaitEvent(stream, s.ev[1], 0);  // k_temporal reads the tick counter k_fire_count advances
-        mark(false); launch_main(k_fire_count, e.grid_wide / 4 + 1, kFireCountThreads, 0, stream, false, e); mark(true);
-        mark(false); launch_main(k_expand, e.grid_wide * 4, kThreads, 0, stream, dep, e); mark(true);
-        return;
-    }
     if (e.side_serial) {
         // everything in tick order on the main stream, each kernel a
         // programmatic dependent of the one before
