@@ -1748,7 +1748,6 @@ __device__ __forceinline__ void temporal_target(const Engine& e, uint32_t n, uin
 }
 
 __global__ void __launch_bounds__(kThreads) k_temporal(Engine e) {
-    tick_enter();  // (returns at once unless launched as a programmatic dependent)
     const uint32_t t = e.ts->tick;
     const int temporal = e.ts->temporal_enabled;
     for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < e.N; n += gridDim.x * blockDim.x) {
@@ -1779,7 +1778,6 @@ __global__ void k_init_syn(SynAB* syn, const SynA* a, unsigned long long S) {
 // k_expand (none of which touches synapse records), so it reads the tick
 // from post_tick, not from the tick counter k_fire_count advances.
 __global__ void k_post(Engine e) {
-    tick_enter();  // (returns at once unless launched as a programmatic dependent)
     const uint32_t t = e.ts->post_tick;
     const uint32_t nf = e.ts->n_fired_targets;
     const int stdp = e.ts->stdp_enabled;
@@ -2186,18 +2184,21 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     mark(false); launch_main(k_bscatter, e.grid_bucket, kBucketThreads, bucket_smem(e), stream, dep, e); mark(true);
     mark(false); launch_main(k_bsort, bsort_grid(e), kThreads, bsort_smem(e), stream, dep, e); mark(true);
     if (e.side_serial) {
-        // everything in tick order on the main stream, each kernel a
-        // programmatic dependent of the one before
+        // everything in tick order on the main stream; k_temporal, k_events,
+        // k_post and the fire ordering take full dependencies (as
+        // programmatic dependents they made the tick 7 % slower on recog_1m:
+        // their blocks, launched early, held SM resources the kernel before
+        // them needed)
         side_mark(8, false);
-        launch_main(k_temporal, e.grid_process, kThreads, 0, stream, dep, e);
+        launch_main(k_temporal, e.grid_process, kThreads, 0, stream, false, e);
         side_mark(8, true);
-        mark(false); launch_main(k_events, e.grid_events, kThreads, 0, stream, dep, e); mark(true);
+        mark(false); launch_main(k_events, e.grid_events, kThreads, 0, stream, false, e); mark(true);
         mark(false); launch_main(k_process, e.grid_walk, kThreads, kProcessSmem, stream, dep, e); mark(true);
         side_mark(9, false);
-        launch_main(k_post, wide * 4, kThreads, 0, stream, dep, e);
+        launch_main(k_post, wide * 4, kThreads, 0, stream, false, e);
         side_mark(9, true);
-        mark(false); launch_main(k_fire_list, e.grid_fire, kThreads, 0, stream, dep, e); mark(true);
-        mark(false); launch_main(k_fire_count, e.grid_wide / 4 + 1, kFireCountThreads, 0, stream, dep, e); mark(true);
+        mark(false); launch_main(k_fire_list, e.grid_fire, kThreads, 0, stream, false, e); mark(true);
+        mark(false); launch_main(k_fire_count, e.grid_wide / 4 + 1, kFireCountThreads, 0, stream, false, e); mark(true);
         mark(false); launch_main(k_expand, e.grid_wide * 4, kThreads, 0, stream, dep, e); mark(true);
         return;
     }
