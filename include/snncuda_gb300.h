@@ -381,7 +381,7 @@ int snncuda_sim_estimate_bytes(const snncuda_network* network, const snncuda_con
  * snncuda_sim_run_until, but launches one tick at a time from a graph whose
  * event nodes bracket every kernel, and accumulates device time per kernel
  * plus the work counters of the profiled ticks into *out (zero it first). */
-#define SNNCUDA_KERNEL_COUNT 9
+#define SNNCUDA_KERNEL_COUNT 10
 typedef struct snncuda_profile {
     uint64_t ticks;
     double kernel_ms[SNNCUDA_KERNEL_COUNT];

@@ -156,7 +156,7 @@ class SynapseState(Structure):
     ]
 
 
-KERNEL_COUNT = 9
+KERNEL_COUNT = 10
 
 
 class Profile(Structure):

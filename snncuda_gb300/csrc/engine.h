@@ -173,7 +173,7 @@ struct TickState {
     uint32_t n_touched;       // targets with at least one due event
     uint32_t n_fires;         // fires this tick
     uint32_t n_fired_targets; // distinct targets that fired this tick (reset by k_hist)
-    uint32_t post_tick;       // the tick in progress (set by k_bcount; read by k_post and k_temporal)
+    uint32_t post_tick;       // tick of the pending post-spike STDP (set by k_hist; read by k_post)
     uint32_t expand_fires;    // fires whose events k_expand copies
     uint32_t far_first_tick;  // delivery tick of far_idx[0] for the current run
     uint32_t far_ticks;       // entries of far_idx minus one (0 = none)
@@ -306,7 +306,7 @@ constexpr uint32_t kMaxClasses = 256;    // distinct delivery delays
 // Host-side launchers (kernels.cu).
 // `marks` (optional) holds 2 * kKernelCount events recorded around every
 // kernel (before, after) for profiling graphs.
-constexpr int kKernelCount = 9;
+constexpr int kKernelCount = 10;
 // The streams of a tick: k_temporal and k_post run on `side`, forked from
 // `main` with ev[0] / ev[2] and joined back with ev[1] / ev[3].
 struct TickStreams {

@@ -19,20 +19,20 @@
 //                  its events in due order (:175-229), redoing the STDP of
 //                  events that follow a fire of the target; fires into a
 //                  due-position bitmap
-//  6. k_fire_list  fires in due order (= reference fire order), raster,
-//                  events per (fire block, delay class); the last block scans
+//  6. k_fire_list  fires in due order (= reference fire order), raster
+//  7. k_fire_count events per (fire block, delay class); the last block scans
 //                  destinations and finishes the tick
-//  7. k_expand     copy each fire's pre-expanded (synapse, offset) events into
+//  8. k_expand     copy each fire's pre-expanded (synapse, offset) events into
 //                  their delivery slots, order-preserving
 //
 // and two more, on a second stream (graph fork/join) beside the others, or
 // for networks of 2^27+ synapses on the main stream in tick order
 // (Engine::side_serial):
 //
-//  8. k_temporal   the neuron temporal pattern of every touched target, once
+//  9. k_temporal   the neuron temporal pattern of every touched target, once
 //                  per tick, beside 4-5 (or before 4)
-//  9. k_post       post-spike STDP over the in-rows of targets that fired
-//                  (:138-173), beside 6-7 (or after 5)
+// 10. k_post       post-spike STDP over the in-rows of targets that fired
+//                  (:138-173), beside 6-8 (or after 5)
 //
 // Main-stream kernels that directly follow another are launched as
 // programmatic dependents (tick_enter), so each is scheduled while the one
@@ -57,6 +57,7 @@ constexpr int kThreads = 256;
 constexpr uint32_t kStageEvents = 3584;  // event inputs k_process stages per block (56 KB)
 constexpr uint32_t kLtpShared = 2560;    // longest LTP table k_process copies to shared memory (10 KB)
 constexpr size_t kProcessSmem = kStageEvents * sizeof(EvIn) + kLtpShared * sizeof(float);
+constexpr int kFireCountThreads = 1024;  // k_fire_count's last block scans up to 32 delay classes at once
 
 // Minimum resident blocks per SM requested for k_process and k_events
 // (register budget).
@@ -1747,10 +1748,7 @@ __device__ __forceinline__ void temporal_target(const Engine& e, uint32_t n, uin
 }
 
 __global__ void __launch_bounds__(kThreads) k_temporal(Engine e) {
-    // the tick from post_tick (set at the tick's start), not from the tick
-    // counter k_fire_list advances: on the side stream this kernel may still
-    // run then
-    const uint32_t t = e.ts->post_tick;
+    const uint32_t t = e.ts->tick;
     const int temporal = e.ts->temporal_enabled;
     for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < e.N; n += gridDim.x * blockDim.x) {
         const uint32_t len = e.seg_start[n + 1] - e.seg_start[n];
@@ -1778,7 +1776,7 @@ __global__ void k_init_syn(SynAB* syn, const SynA* a, unsigned long long S) {
 // (NetworkPropagator.cpp:95-102), one block per fired target, coalesced over
 // the target-major row.  Runs on the side stream beside k_fire_list ..
 // k_expand (none of which touches synapse records), so it reads the tick
-// from post_tick, not from the tick counter k_fire_list advances.
+// from post_tick, not from the tick counter k_fire_count advances.
 __global__ void k_post(Engine e) {
     const uint32_t t = e.ts->post_tick;
     const uint32_t nf = e.ts->n_fired_targets;
@@ -1803,15 +1801,10 @@ __global__ void k_post(Engine e) {
 // its tile by adding the counts of the tiles before it.  A fire's rank r is
 // its position in the reference's fire order (due order,
 // NetworkPropagator.cpp:80-93); the fire list and the raster are written here
-// and the bitmap is cleared.  The thread of a fire also adds its events per
-// delay class into the counts of its expansion block (kExpandFires fires).
-// The last block turns the counts into wheel positions (per class an
-// exclusive scan over the expansion blocks, appended behind each delivery
-// slot's current contents) and finishes the tick.
+// and the bitmap is cleared.
 __global__ void k_fire_list(Engine e) {
     tick_enter();
     const uint32_t t = e.ts->tick;
-    const uint32_t D = e.D;
     const uint32_t words = (e.ts->n_due + 31) / 32;
     const uint32_t tiles = (words + kThreads - 1) / kThreads;
     const unsigned long long raster0 = e.ts->raster_count;
@@ -1827,17 +1820,7 @@ __global__ void k_fire_list(Engine e) {
             const uint32_t bit = __ffs(bits) - 1;
             bits &= bits - 1;
             const uint32_t n = e.fire_at[w * 32 + bit];
-            if (r < e.fire_cap) {
-                e.fire_list[r] = n;
-                const uint32_t* row = e.pre_off + static_cast<size_t>(n) * (D + 1);
-                uint32_t* xs = e.xsum + static_cast<size_t>(r / kExpandFires) * D;
-                uint32_t prev = row[0];
-                for (uint32_t d = 0; d < D; ++d) {
-                    const uint32_t next = row[d + 1];
-                    if (next != prev) atomicAdd(xs + d, next - prev);
-                    prev = next;
-                }
-            }
+            if (r < e.fire_cap) e.fire_list[r] = n;
             if (e.raster_cap > 0) {
                 const unsigned long long pos = raster0 + r;
                 if (pos < e.raster_cap) {
@@ -1855,15 +1838,41 @@ __global__ void k_fire_list(Engine e) {
         block_excl_scan(part, &step);
         base += step;
     }
-    if (!last_block(&e.ts->done_fire_list)) return;
-    // the tick's fire count: the sum of k_process's per-tile counts (then
-    // zero for the next tick)
-    part = 0;
+}
+
+// Events per (expansion block of kExpandFires fires, delay class), one warp
+// per fire and one lane per class.  The last block turns the counts into wheel positions
+// (exclusive scan over blocks per class, appended behind each delivery slot's
+// current contents) and finishes the tick.
+__global__ void __launch_bounds__(kFireCountThreads, 1) k_fire_count(Engine e) {
+    tick_enter();
+    const uint32_t t = e.ts->tick;
+    // the tick's fire count: the sum of k_process's per-tile counts
+    const uint32_t tiles = ((e.ts->n_due + 31) / 32 + kThreads - 1) / kThreads;
+    __shared__ uint32_t s_nf;
+    if (threadIdx.x == 0) s_nf = 0;
+    __syncthreads();
+    uint32_t part = 0;
     for (uint32_t i = threadIdx.x; i < tiles; i += blockDim.x) part += __ldcg(e.fire_tile + i);
-    uint32_t nfires;
-    block_excl_scan(part, &nfires);
-    for (uint32_t i = threadIdx.x; i < tiles; i += blockDim.x) e.fire_tile[i] = 0;
+    part = __reduce_add_sync(0xffffffffu, part);
+    if ((threadIdx.x & 31) == 0 && part) atomicAdd(&s_nf, part);
+    __syncthreads();
+    const uint32_t nfires = s_nf;
     const uint32_t nf = nfires < e.fire_cap ? nfires : e.fire_cap;
+    const uint32_t D = e.D;
+    // one warp per fire, one lane per delay class
+    const uint32_t lane0 = threadIdx.x & 31;
+    const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nf; r += nwarps) {
+        const uint32_t* row = e.pre_off + static_cast<size_t>(e.fire_list[r]) * (D + 1);
+        uint32_t* xs = e.xsum + static_cast<size_t>(r / kExpandFires) * D;
+        for (uint32_t d = lane0; d < D; d += 32) {
+            const uint32_t c = row[d + 1] - row[d];
+            if (c) atomicAdd(xs + d, c);
+        }
+    }
+    if (!last_block(&e.ts->done_fire_list)) return;
+    for (uint32_t i = threadIdx.x; i < tiles; i += blockDim.x) e.fire_tile[i] = 0;  // zero for the next tick
     if (nfires > e.fire_cap && threadIdx.x == 0) raise_status(e, kStatusFireOverflow);
     const uint32_t blocks = (nf + kExpandFires - 1) / kExpandFires;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1903,6 +1912,7 @@ __global__ void k_fire_list(Engine e) {
         TickState* ts = e.ts;
         ts->n_fires = nfires;
         const uint32_t due = ts->n_due;
+        const unsigned long long raster0 = ts->raster_count;
         ts->delivered += due;
         ts->fired += nfires;
         ts->touched_total += ts->n_touched;
@@ -1921,7 +1931,7 @@ __global__ void k_fire_list(Engine e) {
 // Spike-code offset expansion (NetworkPropagator.cpp:104-130): one block per
 // fire, one warp per delay class.  A fire's events of one class are
 // contiguous in its pre-expanded list and go to one contiguous range of their
-// delivery slot: the range k_fire_list reserved for the fire's expansion
+// delivery slot: the range k_fire_count reserved for the fire's expansion
 // block, behind the block's earlier fires.  So the wheel ends up in exactly
 // the reference's scheduling order.
 __global__ void __launch_bounds__(kThreads) k_expand(Engine e) {
@@ -2179,15 +2189,16 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
         // programmatic dependents they made the tick 7 % slower on recog_1m:
         // their blocks, launched early, held SM resources the kernel before
         // them needed)
-        side_mark(7, false);
+        side_mark(8, false);
         launch_main(k_temporal, e.grid_process, kThreads, 0, stream, false, e);
-        side_mark(7, true);
+        side_mark(8, true);
         mark(false); launch_main(k_events, e.grid_events, kThreads, 0, stream, false, e); mark(true);
         mark(false); launch_main(k_process, e.grid_walk, kThreads, kProcessSmem, stream, dep, e); mark(true);
-        side_mark(8, false);
+        side_mark(9, false);
         launch_main(k_post, wide * 4, kThreads, 0, stream, false, e);
-        side_mark(8, true);
+        side_mark(9, true);
         mark(false); launch_main(k_fire_list, e.grid_fire, kThreads, 0, stream, false, e); mark(true);
+        mark(false); launch_main(k_fire_count, e.grid_wide / 4 + 1, kFireCountThreads, 0, stream, false, e); mark(true);
         mark(false); launch_main(k_expand, e.grid_wide * 4, kThreads, 0, stream, dep, e); mark(true);
         return;
     }
@@ -2195,9 +2206,9 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     // (it needs only the segment starts)
     cudaEventRecord(s.ev[0], stream);
     cudaStreamWaitEvent(s.side, s.ev[0], 0);
-    side_mark(7, false);
+    side_mark(8, false);
     k_temporal<<<e.grid_process, kThreads, 0, s.side>>>(e);
-    side_mark(7, true);
+    side_mark(8, true);
     cudaEventRecord(s.ev[1], s.side);
     mark(false); launch_main(k_events, e.grid_events, kThreads, 0, stream, dep, e); mark(true);
     mark(false); launch_main(k_process, e.grid_walk, kThreads, kProcessSmem, stream, dep, e); mark(true);
@@ -2205,21 +2216,21 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     // the expansion (synapse records are not touched by those)
     cudaEventRecord(s.ev[2], stream);
     cudaStreamWaitEvent(s.side, s.ev[2], 0);
-    side_mark(8, false);
+    side_mark(9, false);
     k_post<<<wide * 4, kThreads, 0, s.side>>>(e);
-    side_mark(8, true);
+    side_mark(9, true);
     cudaEventRecord(s.ev[3], s.side);
     mark(false); launch_main(k_fire_list, e.grid_fire, kThreads, 0, stream, dep, e); mark(true);
+    cudaStreamWaitEvent(stream, s.ev[1], 0);  // k_temporal reads the tick counter k_fire_count advances
+    mark(false); launch_main(k_fire_count, e.grid_wide / 4 + 1, kFireCountThreads, 0, stream, false, e); mark(true);
     mark(false); launch_main(k_expand, e.grid_wide * 4, kThreads, 0, stream, dep, e); mark(true);
-    // the next tick's grouping rewrites what k_temporal reads; its k_events
-    // reads the synapse records k_post writes
-    cudaStreamWaitEvent(stream, s.ev[1], 0);
-    cudaStreamWaitEvent(stream, s.ev[3], 0);
+    cudaStreamWaitEvent(stream, s.ev[3], 0);  // the next tick's k_events reads the synapse records
 }
 
 const char* kernel_name(int index) {
-    static const char* names[kKernelCount] = {"k_bcount",  "k_bscatter",  "k_bsort",  "k_events",  "k_process",
-                                              "k_fire_list", "k_expand", "k_temporal", "k_post"};
+    static const char* names[kKernelCount] = {"k_bcount",    "k_bscatter",  "k_bsort",    "k_events",
+                                              "k_process",   "k_fire_list", "k_fire_count", "k_expand",
+                                              "k_temporal",  "k_post"};
     return index >= 0 && index < kKernelCount ? names[index] : "";
 }
 
