@@ -172,8 +172,8 @@ struct TickState {
     uint32_t n_due;           // events due this tick
     uint32_t n_touched;       // targets with at least one due event
     uint32_t n_fires;         // fires this tick
-    uint32_t n_fired_targets; // distinct targets that fired this tick (reset by k_hist)
-    uint32_t post_tick;       // tick of the pending post-spike STDP (set by k_hist; read by k_post)
+    uint32_t n_fired_targets; // distinct targets that fired this tick (reset by k_bcount)
+    uint32_t post_tick;       // tick of the pending post-spike STDP (set by k_bcount; read by k_post)
     uint32_t expand_fires;    // fires whose events k_expand copies
     uint32_t far_first_tick;  // delivery tick of far_idx[0] for the current run
     uint32_t far_ticks;       // entries of far_idx minus one (0 = none)

@@ -1703,7 +1703,7 @@ __global__ void __launch_bounds__(kThreads, SNNGB_PROCESS_MIN_BLOCKS) k_process(
 // The temporal pattern update of every touched target (SynapseDendriteProcessor
 // .cpp:294-316), once per tick for all its k events (temporal_tick).  It reads
 // and writes only the neuron's temporal fields, which nothing else in the tick
-// touches, so it runs beside k_scatter / k_events / k_process.
+// touches, so it can run beside k_events / k_process.
 template <bool kOne>
 __device__ __forceinline__ void temporal_target(const Engine& e, uint32_t n, uint32_t k, uint32_t t, int temporal) {
     const NeuronParam p = e.nparam[n];

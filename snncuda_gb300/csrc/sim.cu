@@ -940,7 +940,7 @@ void run_enqueue(snncuda_sim* sim, uint64_t T, snncuda_profile* prof) {
     const uint64_t W = e.W;
     // Injections in (delivery, call order).  Those due within W ticks go into
     // their slots now, behind everything scheduled before this call; later
-    // ones are moved in by k_hist the tick their slot frees up; the rest wait.
+    // ones are copied in by k_bcount the tick their slot frees up; the rest wait.
     auto& pend = sim->pending;
     sort_pending(sim);
     const Pending* base = pend.data() + sim->pend_head;
