@@ -260,8 +260,6 @@ typedef struct snncuda_tuning {
     uint32_t side_serial;           /* 1: the neuron temporal update and post-spike STDP run in
                                        tick order instead of beside the synapse kernels and the
                                        fire ordering */
-    uint32_t two_level;             /* 1: the grouping places the due list in two levels (coarse
-                                       buckets, then buckets) with coalesced writes */
 } snncuda_tuning;
 int snncuda_sim_autotune(snncuda_sim* sim, uint64_t probe_ticks, snncuda_tuning* out);
 /* Applies a tuning found earlier (by snncuda_sim_autotune on this or another

@@ -87,7 +87,7 @@ class Tuning(Structure):
         ("slot_event_capacity", c_uint64), ("max_slot_events", c_uint64),
         ("ms_per_tick_before", ctypes.c_double), ("ms_per_tick_after", ctypes.c_double),
         ("probes", c_uint32), ("probe_ticks", c_uint64), ("scatter_pass_events", c_uint32),
-        ("side_serial", c_uint32), ("two_level", c_uint32),
+        ("side_serial", c_uint32),
     ]
 
 

@@ -256,15 +256,6 @@ struct Engine {
     uint32_t* btot;                        // [nbuckets] events per bucket (zero between ticks)
     uint32_t* bstart;                      // [nbuckets + 1] first grouped position of each bucket
     uint32_t* bcur;                        // [nbuckets] placement cursor of each bucket
-    // Two-level placement (k_bsplit1 / k_bsplit2 instead of k_bscatter):
-    // the due list goes first to ncoarse coarse buckets of coarse_per
-    // consecutive buckets each (grp_tmp), then from each coarse bucket to its
-    // buckets (evin's memory, free until k_events), every tile sorted in
-    // shared memory first so the global writes are runs.
-    uint32_t two_level;
-    uint32_t coarse_per;
-    uint32_t ncoarse;                      // <= kMaxCoarse
-    uint32_t* ccur;                        // [kMaxCoarse] coarse placement cursors (zero between ticks)
     uint32_t* seg_start;                   // [N + 1] first grouped position of each target
     unsigned long long* grp;               // [slot_cap] due events grouped by target, due order inside
                                            // a target: (payload << 32) | (due index | ext << 31)
@@ -299,7 +290,6 @@ struct Engine {
 };
 
 constexpr uint32_t kMaxBuckets = 16384;   // target buckets of the grouping (shared-memory counters)
-constexpr uint32_t kMaxCoarse = 64;          // coarse buckets of the two-level placement
 constexpr uint32_t kScatterPassEvents = 1u << 22;  // default Engine::scatter_pass_events (64 MB of grp_tmp)
 constexpr uint32_t kMaxBucketShift = 14;  // at most 2^14 targets per bucket: N <= 2^28
 

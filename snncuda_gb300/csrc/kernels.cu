@@ -989,200 +989,6 @@ __global__ void __launch_bounds__(kBucketThreads) k_bscatter(Engine e) {
     }
 }
 
-// ---------------------------------------------------------------------------
-// two-level placement (Engine::two_level): k_bsplit1 puts the due list into
-// at most kMaxCoarse coarse buckets, k_bsplit2 each coarse bucket into its
-// buckets; both sort every tile of kSplitTile events by destination in
-// shared memory first and then write each destination's run with
-// consecutive threads, so the global stores are coalesced runs instead of
-// one scattered 16-byte store per event.
-// ---------------------------------------------------------------------------
-
-constexpr uint32_t kSplitTile = 4096;  // events per tile (4 per thread)
-constexpr uint32_t kSplitPer = kSplitTile / kBucketThreads;
-
-// Block-wide: a tile's entries (kSplitPer per thread, key[k] < nbins or
-// 0xFFFFFFFF for none) sorted by key into `stage`, then written out: entry j
-// of bin b goes to out[base[b] + j] (base[] in shared memory, advanced by the
-// bin's count).  hist/scan: nbins counters in shared memory, zero on entry
-// and on return.
-__device__ void split_tile(const uint4 (&v)[kSplitPer], const uint32_t (&key)[kSplitPer], uint32_t nbins,
-                           uint32_t* hist, uint32_t* scan, uint32_t* base, uint4* stage, uint4* out,
-                           unsigned long long cap) {
-    uint32_t off[kSplitPer];
-#pragma unroll
-    for (uint32_t k = 0; k < kSplitPer; ++k) off[k] = key[k] < nbins ? atomicAdd(&hist[key[k]], 1u) : 0u;
-    __syncthreads();
-    if (threadIdx.x < 32) {  // exclusive scan of the bins, 32 lanes x runs
-        const uint32_t per = (nbins + 31) / 32;
-        const uint32_t b0 = threadIdx.x * per < nbins ? threadIdx.x * per : nbins;
-        const uint32_t b1 = b0 + per < nbins ? b0 + per : nbins;
-        uint32_t sum = 0;
-        for (uint32_t b = b0; b < b1; ++b) sum += hist[b];
-        uint32_t run = warp_incl_scan(sum) - sum;
-        for (uint32_t b = b0; b < b1; ++b) {
-            scan[b] = run;
-            run += hist[b];
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (uint32_t k = 0; k < kSplitPer; ++k) {
-        if (key[k] >= nbins) continue;
-        uint4 x = v[k];
-        x.w = key[k];
-        stage[scan[key[k]] + off[k]] = x;
-    }
-    __syncthreads();
-    const uint32_t total = nbins > 0 ? scan[nbins - 1] + hist[nbins - 1] : 0u;
-    for (uint32_t i = threadIdx.x; i < total; i += blockDim.x) {
-        const uint4 x = stage[i];
-        const unsigned long long pos = static_cast<unsigned long long>(base[x.w]) + (i - scan[x.w]);
-        if (pos < cap) out[pos] = x;  // (out of range only after a failed count)
-    }
-    __syncthreads();
-    for (uint32_t b = threadIdx.x; b < nbins; b += blockDim.x) {
-        base[b] += hist[b];
-        hist[b] = 0;
-    }
-    __syncthreads();
-}
-
-// Level 1: a block per chunk of the due list (the chunks k_bcount counted).
-// The bucket starts come from the totals (every block scans them, block 0
-// publishes them, as k_bscatter); the chunk's count in a coarse bucket is the
-// sum of its row over the coarse bucket's buckets.  Entries go to grp_tmp as
-// (due index | external bit, payload, target).
-__global__ void __launch_bounds__(kBucketThreads) k_bsplit1(Engine e) {
-    tick_enter();
-    extern __shared__ __align__(16) uint32_t s_dyn[];  // [nbuckets] starts, then the stage
-    __shared__ uint32_t s_hist[kMaxCoarse], s_scan[kMaxCoarse], s_base[kMaxCoarse];
-    const uint32_t B = e.nbuckets, C = e.ncoarse, F = e.coarse_per;
-    uint32_t* s_start = s_dyn;
-    uint4* stage = reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(s_dyn) + stream_buf_offset(B));
-    {
-        const uint32_t per = (B + blockDim.x - 1) / blockDim.x;
-        const uint32_t b0 = threadIdx.x * per < B ? threadIdx.x * per : B;
-        const uint32_t b1 = b0 + per < B ? b0 + per : B;
-        uint32_t sum = 0;
-        for (uint32_t b = b0; b < b1; ++b) {
-            const uint32_t c = __ldcg(e.btot + b);
-            s_start[b] = c;
-            sum += c;
-        }
-        uint32_t total;
-        uint32_t run = block_excl_scan_t<kBucketThreads>(sum, &total);
-        for (uint32_t b = b0; b < b1; ++b) {
-            const uint32_t c = s_start[b];
-            s_start[b] = run;
-            if (blockIdx.x == 0) e.bstart[b] = run;
-            run += c;
-        }
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            e.bstart[B] = total;
-            e.seg_start[e.N] = total;
-            count_far_injections(e, e.ts->tick);
-        }
-        if (threadIdx.x < kMaxCoarse) s_hist[threadIdx.x] = 0;
-        __syncthreads();
-    }
-    // this chunk's reservation in each coarse bucket
-    const uint32_t* row = e.bcnt + static_cast<size_t>(blockIdx.x) * B;
-    for (uint32_t b = threadIdx.x; b < B; b += blockDim.x) {
-        const uint32_t c = row[b];
-        if (c) atomicAdd(&s_hist[b / F], c);
-    }
-    __syncthreads();
-    if (threadIdx.x < C) {
-        const uint32_t c = s_hist[threadIdx.x];
-        s_base[threadIdx.x] = s_start[threadIdx.x * F] + (c ? atomicAdd(&e.ccur[threadIdx.x], c) : 0u);
-        s_hist[threadIdx.x] = 0;
-    }
-    __syncthreads();
-    const uint32_t slot = e.ts->tick & e.wmask;
-    const uint32_t n = e.ts->n_due;
-    const unsigned long long* ev = e.wheel + static_cast<size_t>(slot) * e.slot_cap;
-    uint32_t beg, end;
-    chunk_of(n, beg, end);
-    for (uint32_t t0 = beg; t0 < end; t0 += kSplitTile) {
-        uint4 v[kSplitPer];
-        uint32_t key[kSplitPer];
-#pragma unroll
-        for (uint32_t k = 0; k < kSplitPer; ++k) {
-            const uint32_t i = t0 + threadIdx.x + k * kBucketThreads;
-            const unsigned long long x = i < end ? __ldcs(ev + i) : 0ull;
-            const uint32_t lo = static_cast<uint32_t>(x);
-            const uint32_t tgt = lo & ~kExternalBit;
-            key[k] = i < end && tgt < e.N ? (tgt >> e.bucket_shift) / F : 0xFFFFFFFFu;
-            v[k] = make_uint4(i | (lo & kExternalBit), static_cast<uint32_t>(x >> 32), tgt, 0u);
-        }
-        split_tile(v, key, C, s_hist, s_scan, s_base, stage, reinterpret_cast<uint4*>(e.grp_tmp), e.slot_cap);
-    }
-}
-
-// Level 2: tiles of the coarse buckets (block-strided over all of them),
-// each tile's entries to their buckets, reserved with the bucket cursors;
-// entries go to evin's memory as (due index | external bit, payload, target
-// within the bucket), k_bsort's input.
-__global__ void __launch_bounds__(kBucketThreads) k_bsplit2(Engine e) {
-    tick_enter();
-    extern __shared__ __align__(16) uint32_t s_dyn[];  // the stage
-    __shared__ uint32_t s_hist[256], s_scan[256], s_base[256];
-    __shared__ uint32_t s_units[kMaxCoarse + 1], s_cstart[kMaxCoarse + 1];
-    const uint32_t B = e.nbuckets, C = e.ncoarse, F = e.coarse_per;
-    uint4* stage = reinterpret_cast<uint4*>(s_dyn);
-    uint4* out = reinterpret_cast<uint4*>(e.evin);
-    if (threadIdx.x == 0) {
-        // tiles per coarse bucket, prefix-summed
-        uint32_t u = 0;
-        for (uint32_t c = 0; c <= C; ++c) {
-            const uint32_t b = c * F < B ? c * F : B;
-            s_cstart[c] = e.bstart[b];
-            s_units[c] = u;
-            if (c < C) {
-                const uint32_t b1 = (c + 1) * F < B ? (c + 1) * F : B;
-                u += (e.bstart[b1] - e.bstart[b] + kSplitTile - 1) / kSplitTile;
-            }
-        }
-        if (blockIdx.x == 0)
-            for (uint32_t c = 0; c < kMaxCoarse; ++c) e.ccur[c] = 0;  // level 1 is done with them
-    }
-    for (uint32_t b = threadIdx.x; b < 256; b += blockDim.x) s_hist[b] = 0;
-    __syncthreads();
-    const uint32_t units = s_units[C];
-    const uint32_t lmask = (1u << e.bucket_shift) - 1u;
-    for (uint32_t u = blockIdx.x; u < units; u += gridDim.x) {
-        uint32_t c = 0;
-        while (c + 1 < C && s_units[c + 1] <= u) ++c;
-        const uint32_t lo = s_cstart[c] + (u - s_units[c]) * kSplitTile;
-        const uint32_t hi = lo + kSplitTile < s_cstart[c + 1] ? lo + kSplitTile : s_cstart[c + 1];
-        const uint32_t f0 = c * F;
-        const uint32_t nb = f0 + F <= B ? F : B - f0;
-        uint4 v[kSplitPer];
-        uint32_t key[kSplitPer];
-#pragma unroll
-        for (uint32_t k = 0; k < kSplitPer; ++k) {
-            const uint32_t i = lo + threadIdx.x + k * kBucketThreads;
-            uint4 x = i < hi ? reinterpret_cast<const uint4*>(e.grp_tmp)[i] : make_uint4(0u, 0u, 0u, 0u);
-            const uint32_t f = (x.z >> e.bucket_shift) - f0;
-            key[k] = i < hi && f < nb ? f : 0xFFFFFFFFu;
-            x.z &= lmask;
-            v[k] = x;
-        }
-        // this tile's places: behind the tiles that reserved before it
-        for (uint32_t k = 0; k < kSplitPer; ++k)
-            if (key[k] < nb) atomicAdd(&s_hist[key[k]], 1u);
-        __syncthreads();
-        for (uint32_t f = threadIdx.x; f < nb; f += blockDim.x) {
-            const uint32_t cnt = s_hist[f];
-            s_base[f] = e.bstart[f0 + f] + (cnt ? atomicAdd(&e.bcur[f0 + f], cnt) : 0u);
-            s_hist[f] = 0;
-        }
-        __syncthreads();
-        split_tile(v, key, nb, s_hist, s_scan, s_base, stage, out, e.slot_cap);
-    }
-}
-
 // Sort key of a grouped entry: its due index (unique within one due list).
 __device__ __forceinline__ uint32_t grp_key(unsigned long long v) { return static_cast<uint32_t>(v) & ~kExternalBit; }
 
@@ -1284,8 +1090,7 @@ __global__ void __launch_bounds__(kThreads) k_bsort(Engine e) {
         const uint32_t lo = e.bstart[b], hi = e.bstart[b + 1], m = hi - lo;
         const uint32_t n0 = b << e.bucket_shift;
         const uint32_t nw = e.N - n0 < width ? e.N - n0 : width;
-        const uint4* in = reinterpret_cast<const uint4*>(e.two_level ? static_cast<const void*>(e.evin)
-                                                                     : static_cast<const void*>(e.grp_tmp)) + lo;
+        const uint4* in = reinterpret_cast<const uint4*>(e.grp_tmp) + lo;
         const bool small = m <= kSortSmemEvents;
         unsigned long long v[kSortPerThread];
         uint32_t t16[kSortPerThread];
@@ -2351,8 +2156,6 @@ static void launch_main(void (*kernel)(Engine), uint32_t grid, uint32_t block, s
 static size_t bucket_smem(const Engine& e) {
     return stream_buf_offset(e.nbuckets) + 2 * kStreamTile * sizeof(unsigned long long);
 }
-static size_t split1_smem(const Engine& e) { return stream_buf_offset(e.nbuckets) + kSplitTile * sizeof(uint4); }
-static size_t split2_smem() { return kSplitTile * sizeof(uint4); }
 static size_t bsort_smem(const Engine& e) {
     return kSortSmemBytes + (static_cast<size_t>(1) << e.bucket_shift) * sizeof(uint32_t);
 }
@@ -2378,14 +2181,7 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     };
     // k_bcount follows a wait on the side stream: a full dependency
     mark(false); launch_main(k_bcount, e.grid_bucket, kBucketThreads, bucket_smem(e), stream, false, e); mark(true);
-    mark(false);
-    if (e.two_level) {
-        launch_main(k_bsplit1, e.grid_bucket, kBucketThreads, split1_smem(e), stream, dep, e);
-        launch_main(k_bsplit2, e.grid_bucket, kBucketThreads, split2_smem(), stream, dep, e);
-    } else {
-        launch_main(k_bscatter, e.grid_bucket, kBucketThreads, bucket_smem(e), stream, dep, e);
-    }
-    mark(true);
+    mark(false); launch_main(k_bscatter, e.grid_bucket, kBucketThreads, bucket_smem(e), stream, dep, e); mark(true);
     mark(false); launch_main(k_bsort, bsort_grid(e), kThreads, bsort_smem(e), stream, dep, e); mark(true);
     if (e.side_serial) {
         // everything in tick order on the main stream; k_temporal, k_events,
@@ -2451,10 +2247,6 @@ void configure_kernels() {
     const int bucket_bytes = static_cast<int>(stream_buf_offset(kMaxBuckets) + 2 * kStreamTile * sizeof(unsigned long long));
     cudaFuncSetAttribute(k_bcount, cudaFuncAttributeMaxDynamicSharedMemorySize, bucket_bytes);
     cudaFuncSetAttribute(k_bscatter, cudaFuncAttributeMaxDynamicSharedMemorySize, bucket_bytes);
-    cudaFuncSetAttribute(k_bsplit1, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         static_cast<int>(stream_buf_offset(kMaxBuckets) + kSplitTile * sizeof(uint4)));
-    cudaFuncSetAttribute(k_bsplit2, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         static_cast<int>(kSplitTile * sizeof(uint4)));
     cudaFuncSetAttribute(k_bsort, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          static_cast<int>(kSortSmemBytes + (1u << kMaxBucketShift) * sizeof(uint32_t)));
 }

@@ -466,11 +466,6 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.btot = salloc<uint32_t>(sim, e.nbuckets, BufKind::kZero);
     e.bstart = salloc<uint32_t>(sim, static_cast<size_t>(e.nbuckets) + 1, BufKind::kScratch);
     e.bcur = salloc<uint32_t>(sim, e.nbuckets, BufKind::kZero);
-    e.ccur = salloc<uint32_t>(sim, kMaxCoarse, BufKind::kZero);
-    e.ncoarse = std::min<uint32_t>(kMaxCoarse, e.nbuckets);
-    e.coarse_per = (e.nbuckets + e.ncoarse - 1) / e.ncoarse;
-    e.ncoarse = (e.nbuckets + e.coarse_per - 1) / e.coarse_per;
-    e.two_level = S >= (1ull << 27) ? 1u : 0u;  // large due lists (the autotuner probes both)
     e.grp = salloc<unsigned long long>(sim, slot_cap, BufKind::kScratch);
     e.grp_tmp = salloc<BucketEntry>(sim, slot_cap, BufKind::kScratch);
     e.evin = salloc<EvIn>(sim, slot_cap, BufKind::kScratch);
@@ -506,7 +501,6 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     zero(e.slot_count, sizeof(uint32_t) * W);
     zero(e.btot, sizeof(uint32_t) * e.nbuckets);
     zero(e.bcur, sizeof(uint32_t) * e.nbuckets);
-    zero(e.ccur, sizeof(uint32_t) * kMaxCoarse);
     zero(e.fire_bits, sizeof(uint32_t) * bit_words);
     zero(e.xsum, sizeof(uint32_t) * xblocks * std::max<uint32_t>(D, 1));
     zero(e.fire_tile, sizeof(uint32_t) * (fire_tiles + 2));
@@ -577,7 +571,7 @@ void remap_engine(Engine& e, const DeviceBuffers& from, const DeviceBuffers& to)
     };
     fix(e.in_ptr); fix(e.nparam); fix(e.nrec); fix(e.ntp); fix(e.cand); fix(e.refmeta); fix(e.ring); fix(e.syn);
     fix(e.lcode); fix(e.pre_base); fix(e.pre_off); fix(e.pre_ev); fix(e.cls_delta); fix(e.wheel);
-    fix(e.slot_count); fix(e.bcnt); fix(e.btot); fix(e.bstart); fix(e.bcur); fix(e.ccur); fix(e.seg_start); fix(e.grp);
+    fix(e.slot_count); fix(e.bcnt); fix(e.btot); fix(e.bstart); fix(e.bcur); fix(e.seg_start); fix(e.grp);
     fix(e.grp_tmp); fix(e.evin); fix(e.ev_a0); fix(e.fire_bits); fix(e.fire_at);
     fix(e.fire_tile); fix(e.fire_list); fix(e.fired_tgt); fix(e.fired_cnt); fix(e.xsum); fix(e.xdst);
     fix(e.xdst_ok); fix(e.raster); fix(e.ts); fix(e.tab.decay); fix(e.tab.ltp); fix(e.tab.ltd);
@@ -825,7 +819,6 @@ void autotune_impl(snncuda_sim* sim, uint64_t probe_ticks, snncuda_tuning* out) 
         {&e.grid_bucket, {sms, sms * 2, sms * 4}},
         {&e.scatter_pass_events, {kScatterPassEvents / 2, kScatterPassEvents * 2, 0u}},
         {&e.side_serial, {0u, 1u}},
-        {&e.two_level, {0u, 1u}},
         {&e.grid_process, {sms * 2, sms * 4, sms * 8}},
         {&sim->ticks_per_graph, {8, 16, 32}},
     };
@@ -857,7 +850,6 @@ void autotune_impl(snncuda_sim* sim, uint64_t probe_ticks, snncuda_tuning* out) 
         out->grid_bucket = e.grid_bucket;
         out->scatter_pass_events = e.scatter_pass_events;
         out->side_serial = e.side_serial;
-        out->two_level = e.two_level;
         out->grid_temporal = e.grid_process;
         out->ticks_per_graph = sim->ticks_per_graph;
         out->block_threads = 256;
@@ -882,7 +874,7 @@ void apply_tuning_impl(snncuda_sim* sim, const snncuda_tuning& t) {
     auto in = [](uint32_t v, uint32_t lo, uint32_t hi) { return v >= lo && v <= hi; };
     if (!in(t.grid_events, 1, sms * 16) || !in(t.grid_walk, 1, std::max(walk_max, sms * 8)) ||
         !in(t.grid_bucket, 1, sms * 4) || !in(t.grid_temporal, 1, sms * 8) || !in(t.ticks_per_graph, 1, 64) ||
-        t.side_serial > 1 || t.two_level > 1 || (t.block_threads != 0 && t.block_threads != 256))
+        t.side_serial > 1 || (t.block_threads != 0 && t.block_threads != 256))
         throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "tuning field outside the autotuner's ranges");
     e.grid_events = t.grid_events;
     e.grid_walk = t.grid_walk;
@@ -890,7 +882,6 @@ void apply_tuning_impl(snncuda_sim* sim, const snncuda_tuning& t) {
     e.grid_process = t.grid_temporal;
     e.scatter_pass_events = t.scatter_pass_events;
     e.side_serial = t.side_serial;
-    e.two_level = t.two_level;
     sim->ticks_per_graph = t.ticks_per_graph;
     sim->drop_graphs();
     if (t.slot_event_capacity != 0 && t.slot_event_capacity != e.slot_cap) {

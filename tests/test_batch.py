@@ -212,8 +212,8 @@ def test_slot_capacity_change_keeps_queued_events(gpu_lib, port_lib, members):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("side,two", [(0, 0), (1, 0), (0, 1), (1, 1)])
-def test_applied_tuning_keeps_results(gpu_lib, members, side, two):
+@pytest.mark.parametrize("side", [0, 1])
+def test_applied_tuning_keeps_results(gpu_lib, members, side):
     """A tuning applied by hand (multi-pass grouping with a tiny pass, each
     placement of the temporal update and post-spike STDP, other grid sizes)
     leaves every network's state and raster unchanged; a field outside the
@@ -226,7 +226,7 @@ def test_applied_tuning_keeps_results(gpu_lib, members, side, two):
         if tune:
             t = b.autotune(probe_ticks=2)  # about 70 ticks of probes: done well before tick 299
             assert b.counters(0)["next_tick"] < 250
-            t.update(scatter_pass_events=64, side_serial=side, two_level=two, grid_bucket=7, ticks_per_graph=5)
+            t.update(scatter_pass_events=64, side_serial=side, grid_bucket=7, ticks_per_graph=5)
             b.apply_tuning(t)
             bad = dict(t, grid_bucket=10 ** 6)
             with pytest.raises(SNNCudaError):

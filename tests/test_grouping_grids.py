@@ -1,9 +1,7 @@
-"""Two-level placement of the tick's due list (coarse buckets, then buckets,
-each tile sorted in shared memory before its coalesced writes): the same
-grouping as the one-level placement, so results stay equal to the oracle.
-The default turns it on only for networks of 2^27+ synapses; here it is
-forced on a network with hundreds of buckets (and so 64 coarse buckets of
-several buckets each), and compared with the one-level run and the oracle."""
+"""The tick's grouping on a network with hundreds of target buckets, with the
+counting and placing grid of its default size and of one block per SM, and
+with the due list placed in one pass or in passes of 4,096 events: every run
+equals the oracle (digest, counters, raster)."""
 
 import numpy as np
 import pytest
@@ -40,16 +38,16 @@ def _run(lib, net, drive, tuning=None):
     return out
 
 
-def test_two_level_placement_matches_one_level_and_oracle(gpu_lib, port_lib, network):
+def test_grouping_grids_and_passes_match_oracle(gpu_lib, port_lib, network):
     w, net, drive = network
     probe = Simulation(net, _config(gpu_lib), gpu_lib)
     base = probe.autotune(probe_ticks=1)
     probe.close()
     base["slot_event_capacity"] = 0
     runs = {}
-    for two in (0, 1):
+    for passes in (0, 4096):
         for grid in (base["grid_bucket"], 152):
-            runs[(two, grid)] = _run(gpu_lib, net, drive, dict(base, two_level=two, grid_bucket=grid))
+            runs[(passes, grid)] = _run(gpu_lib, net, drive, dict(base, scatter_pass_events=passes, grid_bucket=grid))
     ref = _run(port_lib, net, drive)
     assert ref[1]["synaptic_events"] > 100_000
     for key, (digest, counters, raster) in runs.items():
