@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -118,7 +119,41 @@ struct Digest {
 struct Pending {
     uint64_t tick;  // clamped delivery
     uint64_t event;
+    // left uninitialised by resize(): the queue's new entries are written in
+    // parallel right after
+    Pending() {}
+    Pending(uint64_t t, uint64_t ev) : tick(t), event(ev) {}
 };
+
+// f(begin, end) over [0, n) in contiguous chunks on up to 16 host threads
+// (the calling thread takes the first chunk); serial below 2^20 items.  The
+// injection queue's passes (a drive of millions of injections per call) are
+// memory-bound loops that one host thread runs at a fraction of the host's
+// bandwidth.
+template <typename F>
+void parallel_for(size_t n, F&& f) {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t threads = n < (size_t{1} << 20) ? 1 : std::min<size_t>({size_t{16}, hw, n >> 18});
+    if (threads <= 1) {
+        f(size_t{0}, n);
+        return;
+    }
+    std::vector<std::thread> pool;
+    const size_t chunk = (n + threads - 1) / threads;
+    size_t t = 1;
+    try {
+        pool.reserve(threads - 1);
+        for (; t < threads; ++t) {
+            const size_t b = std::min(n, t * chunk), en = std::min(n, b + chunk);
+            pool.emplace_back([&f, b, en] { f(b, en); });
+        }
+    } catch (...) {
+        // a thread that could not start: its chunks run here
+    }
+    f(size_t{0}, std::min(n, chunk));
+    for (; t < threads; ++t) f(std::min(n, t * chunk), std::min(n, std::min(n, t * chunk) + chunk));
+    for (std::thread& th : pool) th.join();
+}
 
 template <typename T>
 T* dalloc(std::vector<void*>& owned, size_t count) {
@@ -922,7 +957,17 @@ void sort_pending(snncuda_sim* sim) {
         const auto mid = pend.begin() + static_cast<std::ptrdiff_t>(sim->pend_sorted);
         // a drive injected in tick order (the common case) needs no sort, and
         // one that starts at or after every queued event needs no merge
-        if (!std::is_sorted(mid, pend.end(), by_tick)) std::stable_sort(mid, pend.end(), by_tick);
+        const Pending* q = &*mid;
+        const size_t m = static_cast<size_t>(pend.end() - mid);
+        std::atomic<bool> sorted{true};
+        parallel_for(m, [&](size_t b, size_t en) {
+            for (size_t i = b == 0 ? 1 : b; i < en; ++i)
+                if (q[i].tick < q[i - 1].tick) {
+                    sorted.store(false, std::memory_order_relaxed);
+                    return;
+                }
+        });
+        if (!sorted.load()) std::stable_sort(mid, pend.end(), by_tick);
         if (sim->pend_sorted > sim->pend_head && by_tick(*mid, *(mid - 1)))
             std::inplace_merge(pend.begin() + static_cast<std::ptrdiff_t>(sim->pend_head), mid, pend.end(), by_tick);
         sim->pend_sorted = pend.size();
@@ -954,18 +999,22 @@ void run_enqueue(snncuda_sim* sim, uint64_t T, snncuda_profile* prof) {
     const size_t b_end = first_at_or_after(T + W);
     cudaStream_t st = sim->stream;
     if (a_end > 0) {
+        // one group per delivery tick with injections (the queue is in tick
+        // order: each tick's injections are one run, found by binary search)
         std::vector<uint32_t> slots, offs;
-        for (size_t i = 0; i < a_end; ++i) {
-            const uint32_t slot = static_cast<uint32_t>(base[i].tick & (W - 1));
-            if (i == 0 || base[i].tick != base[i - 1].tick) {
-                slots.push_back(slot);
-                offs.push_back(static_cast<uint32_t>(i));
-            }
+        for (size_t b = 0; b < a_end;) {
+            const uint64_t tick = base[b].tick;
+            slots.push_back(static_cast<uint32_t>(tick & (W - 1)));
+            offs.push_back(static_cast<uint32_t>(b));
+            b = std::min(a_end, first_at_or_after(tick + 1));
         }
         offs.push_back(static_cast<uint32_t>(a_end));
         sim->ensure_inject(a_end, slots.size());
         sim->ensure_host(a_end, 2 * slots.size() + 1);
-        for (size_t i = 0; i < a_end; ++i) sim->host_ev[i] = base[i].event;
+        unsigned long long* hev = sim->host_ev;
+        parallel_for(a_end, [&](size_t b, size_t en) {
+            for (size_t i = b; i < en; ++i) hev[i] = base[i].event;
+        });
         std::copy(slots.begin(), slots.end(), sim->host_idx);
         std::copy(offs.begin(), offs.end(), sim->host_idx + slots.size());
         check(cudaMemcpyAsync(sim->inj_ev, sim->host_ev, a_end * 8, cudaMemcpyHostToDevice, st), "inject copy");
@@ -984,14 +1033,13 @@ void run_enqueue(snncuda_sim* sim, uint64_t T, snncuda_profile* prof) {
         const size_t n = b_end - a_end;
         sim->ensure_far(n, static_cast<size_t>(far_ticks) + 1);
         sim->ensure_host(n, static_cast<size_t>(far_ticks) + 1);
-        uint32_t* idx = sim->host_idx;
-        std::fill(idx, idx + far_ticks + 1, 0u);
-        for (size_t i = 0; i < n; ++i) {
-            const Pending& q = base[a_end + i];
-            sim->host_ev[i] = q.event;
-            idx[q.tick - far_first + 1] += 1;
-        }
-        for (size_t i = 1; i <= far_ticks; ++i) idx[i] += idx[i - 1];
+        uint32_t* idx = sim->host_idx;  // idx[j]: far injections due before far_first + j
+        for (uint32_t j = 0; j < far_ticks; ++j) idx[j] = static_cast<uint32_t>(first_at_or_after(far_first + j) - a_end);
+        idx[far_ticks] = static_cast<uint32_t>(n);
+        unsigned long long* hev = sim->host_ev;
+        parallel_for(n, [&](size_t b, size_t en) {
+            for (size_t i = b; i < en; ++i) hev[i] = base[a_end + i].event;
+        });
         check(cudaMemcpyAsync(sim->far_ev, sim->host_ev, n * 8, cudaMemcpyHostToDevice, st), "far copy");
         check(cudaMemcpyAsync(sim->far_idx, idx, (static_cast<size_t>(far_ticks) + 1) * 4, cudaMemcpyHostToDevice,
                               st), "far copy");
@@ -1229,16 +1277,28 @@ int snncuda_sim_inject(snncuda_sim* sim, uint64_t count, const uint32_t* neurons
                        const float* weights) {
     if (sim == nullptr) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null sim");
     if (count > 0 && (!neurons || !ticks || !weights)) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "null array");
-    for (uint64_t i = 0; i < count; ++i)
-        if (neurons[i] >= sim->N) return set_error(SNNCUDA_ERR_INVALID_ARGUMENT, "inject neuron out of range");
     return guarded([&] {
-        sim->pending.reserve(sim->pending.size() + count);
-        for (uint64_t i = 0; i < count; ++i) {
-            const uint64_t t = ticks[i] < sim->next_tick ? sim->next_tick : ticks[i];
-            uint32_t wbits;
-            std::memcpy(&wbits, &weights[i], 4);
-            sim->pending.push_back({t, (static_cast<unsigned long long>(wbits) << 32) | neurons[i] | kExternalBit});
-        }
+        std::atomic<bool> in_range{true};
+        parallel_for(count, [&](size_t b, size_t en) {
+            for (size_t i = b; i < en; ++i)
+                if (neurons[i] >= sim->N) {
+                    in_range.store(false, std::memory_order_relaxed);
+                    return;
+                }
+        });
+        if (!in_range.load()) throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "inject neuron out of range");
+        const size_t at = sim->pending.size();
+        sim->pending.resize(at + count);
+        Pending* dst = sim->pending.data() + at;
+        const uint64_t now = sim->next_tick;
+        parallel_for(count, [&](size_t b, size_t en) {
+            for (size_t i = b; i < en; ++i) {
+                uint32_t wbits;
+                std::memcpy(&wbits, &weights[i], 4);
+                dst[i] = Pending(ticks[i] < now ? now : ticks[i],
+                                 (static_cast<unsigned long long>(wbits) << 32) | neurons[i] | kExternalBit);
+            }
+        });
     });
 }
 
