@@ -1049,9 +1049,14 @@ void run_enqueue(snncuda_sim* sim, uint64_t T, snncuda_profile* prof) {
     if (sim->pend_head == pend.size()) {
         pend.clear();
         sim->pend_head = sim->pend_sorted = 0;
-    } else if (sim->pend_head > (1u << 16) && sim->pend_head * 2 > pend.size()) {
-        pend.erase(pend.begin(), pend.begin() + static_cast<std::ptrdiff_t>(sim->pend_head));
-        sim->pend_sorted -= sim->pend_head;
+    } else if (sim->pend_head > (1u << 16) && sim->pend_head > 3 * (pend.size() - sim->pend_head)) {
+        // compaction once three quarters are consumed: the live quarter moves
+        // to the front (no overlap), split across host threads
+        const size_t head = sim->pend_head, live_n = pend.size() - head;
+        Pending* q = pend.data();
+        parallel_for(live_n, [&](size_t b, size_t en) { std::copy(q + head + b, q + head + en, q + b); });
+        pend.resize(live_n);
+        sim->pend_sorted -= head;
         sim->pend_head = 0;
     }
     // run parameters live in device memory so the captured graphs stay valid
