@@ -257,10 +257,9 @@ typedef struct snncuda_tuning {
     uint32_t probes;
     uint64_t probe_ticks;
     uint32_t scatter_pass_events;   /* due-list events per grouping pass (0: one pass) */
-    uint32_t side_serial;           /* 0: the neuron temporal update and post-spike STDP run beside
-                                       the synapse kernels and the fire ordering; 1: both in tick
-                                       order; 2: post-spike STDP in tick order, the temporal update
-                                       after the neuron walk, beside the fire ordering */
+    uint32_t side_serial;           /* 1: the neuron temporal update and post-spike STDP run in
+                                       tick order instead of beside the synapse kernels and the
+                                       fire ordering */
 } snncuda_tuning;
 int snncuda_sim_autotune(snncuda_sim* sim, uint64_t probe_ticks, snncuda_tuning* out);
 /* Applies a tuning found earlier (by snncuda_sim_autotune on this or another

@@ -250,9 +250,7 @@ struct Engine {
     // 1: k_temporal and k_post run on the main stream in tick order instead
     // of on the side stream beside k_events / k_process and beside the fire
     // ordering (two random-access kernels side by side can take longer than
-    // one after the other); 2: k_post in tick order, k_temporal on the side
-    // stream after k_process, beside k_post, the fire ordering and the
-    // expansion.
+    // one after the other).
     uint32_t side_serial;
     uint32_t* bcnt;                        // [grid_bucket][nbuckets] events of each (chunk, bucket)
     uint32_t* btot;                        // [nbuckets] events per bucket (zero between ticks)

@@ -26,7 +26,7 @@
 //                  their delivery slots, order-preserving
 //
 // and two more, on a second stream (graph fork/join) beside the others, or
-// for networks of 2^27+ synapses on the main stream in tick order
+// for networks of 2^26+ synapses on the main stream in tick order
 // (Engine::side_serial):
 //
 //  9. k_temporal   the neuron temporal pattern of every touched target, once
@@ -1748,10 +1748,7 @@ __device__ __forceinline__ void temporal_target(const Engine& e, uint32_t n, uin
 }
 
 __global__ void __launch_bounds__(kThreads) k_temporal(Engine e) {
-    // the tick in progress from post_tick (set at its start): with
-    // side_serial 2 this kernel may still run when k_fire_count advances the
-    // tick counter
-    const uint32_t t = e.ts->post_tick;
+    const uint32_t t = e.ts->tick;
     const int temporal = e.ts->temporal_enabled;
     for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < e.N; n += gridDim.x * blockDim.x) {
         const uint32_t len = e.seg_start[n + 1] - e.seg_start[n];
@@ -2179,34 +2176,13 @@ void launch_tick(const Engine& e, const TickStreams& s, cudaEvent_t* marks) {
     auto side_mark = [&](int index, bool after) {
         if (marks)
             cudaEventRecordWithFlags(marks[2 * index + (after ? 1 : 0)],
-                                     e.side_serial == 1 || (e.side_serial == 2 && index == 9) ? stream : s.side,
+                                     e.side_serial ? stream : s.side,
                                      cudaEventRecordExternal);
     };
     // k_bcount follows a wait on the side stream: a full dependency
     mark(false); launch_main(k_bcount, e.grid_bucket, kBucketThreads, bucket_smem(e), stream, false, e); mark(true);
     mark(false); launch_main(k_bscatter, e.grid_bucket, kBucketThreads, bucket_smem(e), stream, dep, e); mark(true);
     mark(false); launch_main(k_bsort, bsort_grid(e), kThreads, bsort_smem(e), stream, dep, e); mark(true);
-    if (e.side_serial == 2) {
-        // k_temporal after the walk on the side stream, beside post-spike
-        // STDP, the fire ordering and the expansion (bandwidth-bound or short
-        // kernels), joined at the end of the tick
-        mark(false); launch_main(k_events, e.grid_events, kThreads, 0, stream, dep, e); mark(true);
-        mark(false); launch_main(k_process, e.grid_walk, kThreads, kProcessSmem, stream, dep, e); mark(true);
-        cudaEventRecord(s.ev[0], stream);
-        cudaStreamWaitEvent(s.side, s.ev[0], 0);
-        side_mark(8, false);
-        k_temporal<<<e.grid_process, kThreads, 0, s.side>>>(e);
-        side_mark(8, true);
-        cudaEventRecord(s.ev[1], s.side);
-        side_mark(9, false);
-        launch_main(k_post, wide * 4, kThreads, 0, stream, false, e);
-        side_mark(9, true);
-        mark(false); launch_main(k_fire_list, e.grid_fire, kThreads, 0, stream, false, e); mark(true);
-        mark(false); launch_main(k_fire_count, e.grid_wide / 4 + 1, kFireCountThreads, 0, stream, false, e); mark(true);
-        mark(false); launch_main(k_expand, e.grid_wide * 4, kThreads, 0, stream, dep, e); mark(true);
-        cudaStreamWaitEvent(stream, s.ev[1], 0);  // the next tick's grouping rewrites what k_temporal reads
-        return;
-    }
     if (e.side_serial) {
         // everything in tick order on the main stream; k_temporal, k_events,
         // k_post and the fire ordering take full dependencies (as

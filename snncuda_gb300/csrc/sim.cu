@@ -574,8 +574,9 @@ void create_impl(const snncuda_network* net, const snncuda_config& cfg, snncuda_
     e.grid_fire = static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>(fire_tiles, sms * 8ull)));
     // large networks: the temporal update and post-spike STDP in tick order
     // (beside k_events they slowed it by more than their own time on a 1e9-
-    // synapse network; neutral at 1e8 synapses)
-    e.side_serial = e.S >= (1ull << 27) ? 1u : 0u;
+    // synapse network, and by about their own time at 1e8 synapses; on a
+    // 2e7-synapse network the overlap still gains 15 %)
+    e.side_serial = e.S >= (1ull << 26) ? 1u : 0u;
     sim->ensure_far(1, 2);
     check(cudaStreamSynchronize(st), "create synchronize");
 }
@@ -853,7 +854,7 @@ void autotune_impl(snncuda_sim* sim, uint64_t probe_ticks, snncuda_tuning* out) 
                         std::min(walk_max, sms * 6)}},
         {&e.grid_bucket, {sms, sms * 2, sms * 4}},
         {&e.scatter_pass_events, {kScatterPassEvents / 2, kScatterPassEvents * 2, 0u}},
-        {&e.side_serial, {0u, 1u, 2u}},
+        {&e.side_serial, {0u, 1u}},
         {&e.grid_process, {sms * 2, sms * 4, sms * 8}},
         {&sim->ticks_per_graph, {8, 16, 32}},
     };
@@ -909,7 +910,7 @@ void apply_tuning_impl(snncuda_sim* sim, const snncuda_tuning& t) {
     auto in = [](uint32_t v, uint32_t lo, uint32_t hi) { return v >= lo && v <= hi; };
     if (!in(t.grid_events, 1, sms * 16) || !in(t.grid_walk, 1, std::max(walk_max, sms * 8)) ||
         !in(t.grid_bucket, 1, sms * 4) || !in(t.grid_temporal, 1, sms * 8) || !in(t.ticks_per_graph, 1, 64) ||
-        t.side_serial > 2 || (t.block_threads != 0 && t.block_threads != 256))
+        t.side_serial > 1 || (t.block_threads != 0 && t.block_threads != 256))
         throw_fail(SNNCUDA_ERR_INVALID_ARGUMENT, "tuning field outside the autotuner's ranges");
     e.grid_events = t.grid_events;
     e.grid_walk = t.grid_walk;

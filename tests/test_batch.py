@@ -212,7 +212,7 @@ def test_slot_capacity_change_keeps_queued_events(gpu_lib, port_lib, members):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("side", [0, 1, 2])
+@pytest.mark.parametrize("side", [0, 1])
 def test_applied_tuning_keeps_results(gpu_lib, members, side):
     """A tuning applied by hand (multi-pass grouping with a tiny pass, each
     placement of the temporal update and post-spike STDP, other grid sizes)
