@@ -69,7 +69,11 @@ if "--serve" in sys.argv:
 METRIC = "synaptic_events_per_s"
 UNIT = "events/s"
 ORACLE = ROOT / "oracle" / "_build" / "liboracle_port.so"
-KERNELS_PER_TICK = 11   # launch_tick in snncuda_gb300/csrc/kernels.cu
+# kernels per tick (launch_tick in snncuda_gb300/csrc/kernels.cu): the
+# profile API's kernel count; plus one injection kernel per timed step
+def kernels_per_tick():
+    from snncuda_gb300 import _abi
+    return _abi.KERNEL_COUNT
 
 # Minimal algorithmic bytes of a compact structure-of-arrays design of the
 # tick, per fire F, synaptic event E, external event X, touched target U:
@@ -948,7 +952,7 @@ def main():
             "ticks_per_s": steps_ticks / (ms_max / 1e3),
             "fires_per_tick": r["fires"] / steps_ticks,
             "events_per_tick": r["events"] / steps_ticks,
-            "gpu_launches": steps_ticks * KERNELS_PER_TICK,
+            "gpu_launches": steps_ticks * kernels_per_tick() + args.steps,
             "tick_roofline": tick_roofline(w, r["events"], r["fires"], r["ext"], prof, steps_ticks, ms_max),
             "clocks": r["clocks"], "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             **({"recognition": r["recognition"]} if r["recognition"] is not None else {}),
