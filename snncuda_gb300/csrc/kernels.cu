@@ -767,13 +767,14 @@ constexpr int kBucketThreads = 1024;
 
 // The counting and placing blocks stream their chunk of the due list through
 // shared memory: tiles of kStreamTile entries (32 KB) by bulk copy (TMA),
-// two copies in flight per block, each waited for at most
+// kStreamBufs copies in flight per block, each waited for at most
 // Engine::stage_wait_ns.
 constexpr uint32_t kStreamTile = 4096;
+constexpr uint32_t kStreamBufs = 3;
 
 struct DueStream {
-    unsigned long long* buf;  // 2 x kStreamTile entries (shared memory)
-    unsigned long long* bar;  // 2 mbarriers (shared memory)
+    unsigned long long* buf;  // kStreamBufs x kStreamTile entries (shared memory)
+    unsigned long long* bar;  // kStreamBufs mbarriers (shared memory)
     uint32_t parity;          // bit b: phase buffer b's barrier completes next
     bool staging;             // false after a copy outlived its wait: no more copies
 };
@@ -823,15 +824,14 @@ __device__ bool stream_due(const Engine& e, const unsigned long long* src, uint3
         return a1 - st < kStreamTile ? a1 - st : kStreamTile;
     };
     auto issue = [&](uint32_t k) {
-        bulk_load(s.buf + (k & 1u) * kStreamTile, src + a0 + k * kStreamTile,
-                  tile_len(k) * static_cast<uint32_t>(sizeof(unsigned long long)), &s.bar[k & 1u]);
+        const uint32_t b = k % kStreamBufs;
+        bulk_load(s.buf + b * kStreamTile, src + a0 + k * kStreamTile,
+                  tile_len(k) * static_cast<uint32_t>(sizeof(unsigned long long)), &s.bar[b]);
     };
-    if (threadIdx.x == 0) {
-        if (ntiles > 0) issue(0);
-        if (ntiles > 1) issue(1);
-    }
+    if (threadIdx.x == 0)
+        for (uint32_t k = 0; k < kStreamBufs && k < ntiles; ++k) issue(k);
     for (uint32_t k = 0; k < ntiles; ++k) {
-        const uint32_t b = k & 1u;
+        const uint32_t b = k % kStreamBufs;
         const uint32_t st = a0 + k * kStreamTile;
         const uint32_t cnt = tile_len(k);
         // one thread polls the barrier; the block barrier then orders its
@@ -839,17 +839,15 @@ __device__ bool stream_due(const Engine& e, const unsigned long long* src, uint3
         bool ready = true;
         if (threadIdx.x == 0) ready = mbar_wait(&s.bar[b], (s.parity >> b) & 1u, e.stage_wait_ns);
         if (!__syncthreads_and(ready)) {
-            // tiles k and (if issued) k + 1 are still in flight: drain them
-            // before the block goes on without shared memory
+            // tiles k .. k + kStreamBufs - 1 (those that exist) are still in
+            // flight: drain them before the block goes on without shared memory
             bool drained = true;
-            if (threadIdx.x == 0) {
-                raise_status(e, kStatusStageTimeout);
-                drained = mbar_wait(&s.bar[b], (s.parity >> b) & 1u, kDrainWaitNs);
-                if (k + 1 < ntiles)
-                    drained = mbar_wait(&s.bar[b ^ 1u], (s.parity >> (b ^ 1u)) & 1u, kDrainWaitNs) && drained;
+            if (threadIdx.x == 0) raise_status(e, kStatusStageTimeout);
+            for (uint32_t j = 0; j < kStreamBufs && k + j < ntiles; ++j) {
+                const uint32_t bj = (k + j) % kStreamBufs;
+                if (threadIdx.x == 0) drained = mbar_wait(&s.bar[bj], (s.parity >> bj) & 1u, kDrainWaitNs) && drained;
+                s.parity ^= 1u << bj;
             }
-            s.parity ^= 1u << b;
-            if (k + 1 < ntiles) s.parity ^= 1u << (b ^ 1u);
             if (!__syncthreads_and(drained)) return false;
             s.staging = false;
             for (uint32_t i = st + threadIdx.x; i < a1; i += blockDim.x) f(i, __ldcs(src + i));
@@ -858,8 +856,8 @@ __device__ bool stream_due(const Engine& e, const unsigned long long* src, uint3
         const unsigned long long* tile = s.buf + b * kStreamTile;
         for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) f(st + i, tile[i]);
         s.parity ^= 1u << b;
-        __syncthreads();  // the buffer is read: it may take tile k + 2
-        if (threadIdx.x == 0 && k + 2 < ntiles) issue(k + 2);
+        __syncthreads();  // the buffer is read: it may take tile k + kStreamBufs
+        if (threadIdx.x == 0 && k + kStreamBufs < ntiles) issue(k + kStreamBufs);
     }
     return true;
 }
@@ -867,15 +865,13 @@ __device__ bool stream_due(const Engine& e, const unsigned long long* src, uint3
 __global__ void __launch_bounds__(kBucketThreads) k_bcount(Engine e) {
     tick_enter();
     extern __shared__ __align__(16) uint32_t s_hist[];  // [nbuckets], then the stream's tiles
-    __shared__ unsigned long long s_bar[2];
+    __shared__ unsigned long long s_bar[kStreamBufs];
     const uint32_t t = e.ts->tick;
     copy_far_injections(e, t);
     const uint32_t B = e.nbuckets;
     for (uint32_t b = threadIdx.x; b < B; b += blockDim.x) s_hist[b] = 0;
-    if (threadIdx.x == 0) {
-        mbar_init(&s_bar[0], 1);
-        mbar_init(&s_bar[1], 1);
-    }
+    if (threadIdx.x == 0)
+        for (uint32_t j = 0; j < kStreamBufs; ++j) mbar_init(&s_bar[j], 1);
     __syncthreads();
     const uint32_t slot = t & e.wmask;
     const uint32_t n = e.slot_count[slot];
@@ -918,7 +914,7 @@ __global__ void __launch_bounds__(kBucketThreads) k_bcount(Engine e) {
 __global__ void __launch_bounds__(kBucketThreads) k_bscatter(Engine e) {
     tick_enter();
     extern __shared__ __align__(16) uint32_t s_pos[];  // [nbuckets] next position of this chunk in each bucket
-    __shared__ unsigned long long s_bar[2];
+    __shared__ unsigned long long s_bar[kStreamBufs];
     const uint32_t B = e.nbuckets;
     {
         // bucket starts: every block scans the bucket totals itself (a run of
@@ -954,10 +950,8 @@ __global__ void __launch_bounds__(kBucketThreads) k_bscatter(Engine e) {
         const uint32_t c = row[b];
         if (c) s_pos[b] += atomicAdd(&e.bcur[b], c);
     }
-    if (threadIdx.x == 0) {
-        mbar_init(&s_bar[0], 1);
-        mbar_init(&s_bar[1], 1);
-    }
+    if (threadIdx.x == 0)
+        for (uint32_t j = 0; j < kStreamBufs; ++j) mbar_init(&s_bar[j], 1);
     __syncthreads();
     DueStream ds{reinterpret_cast<unsigned long long*>(reinterpret_cast<unsigned char*>(s_pos) + stream_buf_offset(B)),
                  s_bar, 0u, true};
@@ -2154,7 +2148,7 @@ static void launch_main(void (*kernel)(Engine), uint32_t grid, uint32_t block, s
 
 // Dynamic shared memory of the grouping kernels.
 static size_t bucket_smem(const Engine& e) {
-    return stream_buf_offset(e.nbuckets) + 2 * kStreamTile * sizeof(unsigned long long);
+    return stream_buf_offset(e.nbuckets) + kStreamBufs * kStreamTile * sizeof(unsigned long long);
 }
 static size_t bsort_smem(const Engine& e) {
     return kSortSmemBytes + (static_cast<size_t>(1) << e.bucket_shift) * sizeof(uint32_t);
@@ -2244,7 +2238,8 @@ void launch_group(const Engine& e, cudaStream_t stream) {
 void configure_kernels() {
     cudaFuncSetAttribute(k_process, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          static_cast<int>(kProcessSmem));
-    const int bucket_bytes = static_cast<int>(stream_buf_offset(kMaxBuckets) + 2 * kStreamTile * sizeof(unsigned long long));
+    const int bucket_bytes =
+        static_cast<int>(stream_buf_offset(kMaxBuckets) + kStreamBufs * kStreamTile * sizeof(unsigned long long));
     cudaFuncSetAttribute(k_bcount, cudaFuncAttributeMaxDynamicSharedMemorySize, bucket_bytes);
     cudaFuncSetAttribute(k_bscatter, cudaFuncAttributeMaxDynamicSharedMemorySize, bucket_bytes);
     cudaFuncSetAttribute(k_bsort, cudaFuncAttributeMaxDynamicSharedMemorySize,
