@@ -770,7 +770,7 @@ constexpr int kBucketThreads = 1024;
 // kStreamBufs copies in flight per block, each waited for at most
 // Engine::stage_wait_ns.
 constexpr uint32_t kStreamTile = 4096;
-constexpr uint32_t kStreamBufs = 3;
+constexpr uint32_t kStreamBufs = 2;
 
 struct DueStream {
     unsigned long long* buf;  // kStreamBufs x kStreamTile entries (shared memory)
