@@ -794,6 +794,20 @@ def run_serving(args):
     }
 
 
+def serving_leg(args):
+    """A short serving run beside the headline: Poisson arrivals at 2 jobs/s
+    for 8 s (recog_1m distributions, N log-uniform 1e4-1e5), a 16 GB budget
+    with preemption by eviction, so some jobs wait in host memory; p50/p99
+    latency, aggregate events/s, evictions and the solo-vs-mix check."""
+    import copy
+    a = copy.copy(args)
+    a.serve_rate, a.serve_seconds, a.serve_budget_gb, a.serve_evict = 2.0, 8.0, 16.0, True
+    out = run_serving(a)
+    return {"value": out["value"], "unit": out["unit"], "latency_s": out["latency_s"], "events": out["events"],
+            "wall_s": out["wall_s"], "evictions": out["evictions"], "failed_jobs": out["failed_jobs"],
+            "solo_vs_mix_equal": out["solo_vs_mix_equal"], "config": out["config"]}
+
+
 def side_leg(lib, args, stream):
     """stdp_100k beside the headline: 10 timed steps of 400 ticks after the
     headline's warm-up count, plus its per-kernel profile."""
@@ -850,6 +864,8 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=120.0)
     ap.add_argument("--serve-slice", type=int, default=32, help="ticks per job and scheduling round")
     ap.add_argument("--serve-running", type=int, default=32, help="jobs advanced side by side")
+    ap.add_argument("--no-serve-leg", dest="serve_leg", action="store_false",
+                    help="skip the short serving run beside the headline")
     ap.add_argument("--serve-evict", action="store_true",
                     help="queued jobs preempt running jobs with more remaining work (eviction to host memory)")
     args = ap.parse_args()
@@ -939,6 +955,9 @@ def main():
         nmin, nmax = (int(x) for x in args.batch_neurons.split(","))
         batched = batched_leg(lib, args.batch_networks, nmin, nmax, args.batch_ticks, stream,
                               wave_synapses=args.batch_wave_synapses)
+    serving = None
+    if rank == 0 and args.serve_leg and full_size:
+        serving = serving_leg(args)
     if rank == 0 and not args.no_cpu:
         parity, cpu = parity_legs(lib)
 
@@ -959,6 +978,7 @@ def main():
             "parity": parity,
             **({"stdp_100k": side} if side is not None else {}),
             **({"batched": batched} if batched is not None else {}),
+            **({"serving": serving} if serving is not None else {}),
         }
         print(json.dumps(line), flush=True)
     if world > 1:
