@@ -1932,10 +1932,10 @@ __global__ void __launch_bounds__(kThreads) k_expand(Engine e) {
     tick_enter();
     __shared__ uint32_t s_rows[kExpandFires][kMaxClasses + 1];
     __shared__ unsigned long long s_dst[kMaxClasses];
+    __shared__ uint8_t s_ok[kMaxClasses];  // the class's slot had room
     __shared__ unsigned long long s_base;
     const uint32_t nf = e.ts->expand_fires;
     const uint32_t D = e.D;
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (uint32_t r = blockIdx.x; r < nf; r += gridDim.x) {
         const uint32_t first = r - r % kExpandFires;
         const uint32_t m = r - first + 1;  // fires first .. r of the expansion block
@@ -1945,28 +1945,54 @@ __global__ void __launch_bounds__(kThreads) k_expand(Engine e) {
             const uint32_t q = i / (D + 1), d = i - q * (D + 1);
             s_rows[q][d] = e.pre_off[static_cast<size_t>(e.fire_list[first + q]) * (D + 1) + d];
         }
-        for (uint32_t d = threadIdx.x; d < D; d += blockDim.x)
-            s_dst[d] = e.xdst_ok[d] ? __ldcg(e.xdst + static_cast<size_t>(r / kExpandFires) * D + d) : ~0ull;
+        for (uint32_t d = threadIdx.x; d < D; d += blockDim.x) {
+            s_ok[d] = e.xdst_ok[d] ? 1 : 0;
+            s_dst[d] = s_ok[d] ? __ldcg(e.xdst + static_cast<size_t>(r / kExpandFires) * D + d) : 0ull;
+        }
         if (threadIdx.x == 0) s_base = e.pre_base[e.fire_list[r]];
         __syncthreads();
-        const unsigned long long* src = e.pre_ev + s_base;
         const uint32_t* row = s_rows[m - 1];
-        for (uint32_t d = warp; d < D; d += kThreads / 32) {
-            const uint32_t beg = row[d], len = row[d + 1] - beg;
-            if (len == 0 || s_dst[d] == ~0ull) continue;
-            uint32_t before = 0;  // this class's events of the block's earlier fires
+        // this fire's place in each class: the block's destination behind
+        // the class's events of the block's earlier fires
+        for (uint32_t d = threadIdx.x; d < D; d += blockDim.x) {
+            uint32_t before = 0;
             for (uint32_t q = 0; q + 1 < m; ++q) before += s_rows[q][d + 1] - s_rows[q][d];
-            unsigned long long* dst = e.wheel + s_dst[d] + before;
-            const unsigned long long* sp = src + beg;
-            uint32_t i = lane;
-            for (; i + 96 < len; i += 128) {  // four loads in flight per lane
-                const unsigned long long a0 = sp[i], a1 = sp[i + 32], a2 = sp[i + 64], a3 = sp[i + 96];
-                dst[i] = a0;
-                dst[i + 32] = a1;
-                dst[i + 64] = a2;
-                dst[i + 96] = a3;
+            // then event k of class d goes to s_dst[d] + k (64-bit wrap-around
+            // arithmetic: exact once k >= row[d] is added back)
+            s_dst[d] = s_dst[d] + static_cast<unsigned long long>(before) - static_cast<unsigned long long>(row[d]);
+        }
+        __syncthreads();
+        // every event by its own thread (consecutive threads, consecutive
+        // events: coalesced within a class); its class by binary search of
+        // the fire's class offsets
+        const unsigned long long* src = e.pre_ev + s_base;
+        const uint32_t k0 = row[0], k1 = row[D];
+        auto class_of = [&](uint32_t k) {
+            uint32_t lo = 0, hi = D;  // row[lo] <= k < row[hi]
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (row[mid] <= k) {
+                    lo = mid;
+                } else {
+                    hi = mid;
+                }
             }
-            for (; i < len; i += 32) dst[i] = sp[i];
+            return lo;
+        };
+        for (uint32_t k = k0 + threadIdx.x; k < k1; k += 4 * blockDim.x) {
+            unsigned long long v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t kk = k + u * blockDim.x;
+                v[u] = kk < k1 ? src[kk] : 0ull;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t kk = k + u * blockDim.x;
+                if (kk >= k1) continue;
+                const uint32_t d = class_of(kk);
+                if (s_ok[d]) e.wheel[s_dst[d] + kk] = v[u];
+            }
         }
         __syncthreads();
     }
