@@ -409,11 +409,14 @@ def run_reference(args, w):
     sample = {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "same_config": False,
               "sample": f"ticks {CPU_TIMED_FROM}..{T - 1} of recog_100k (recog_1m distributions at 1e5 neurons x "
                         f"1,000: {r['timed_events']} synaptic events, {r['timed_seconds']:.1f} s, single-threaded "
-                        "oracle port; the oracle cannot hold the 1e9-synapse network)"}
+                        "oracle port; the oracle cannot hold the 1e9-synapse network; ms_per_step: "
+                        f"{ticks_per_step(args, w)} ticks of that network)"}
     tps = ticks_per_step(args, w)
+    # one step = tps ticks of the sample network, at the sample's measured pace
+    ms_step = r["timed_seconds"] / (T - CPU_TIMED_FROM) * tps * 1e3
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic", "config": config_block(args, w, tps),
         "cpu_baseline": sample,
