@@ -1963,13 +1963,10 @@ __global__ void __launch_bounds__(kThreads) k_expand(Engine e) {
         }
         __syncthreads();
         // every event by its own thread (consecutive threads, consecutive
-        // events: coalesced within a class); a warp's 32 consecutive events
-        // span few classes, so lane 0 finds its event's class by binary
-        // search of the fire's class offsets and the other lanes step on from
-        // it
+        // events: coalesced within a class); its class by binary search of
+        // the fire's class offsets
         const unsigned long long* src = e.pre_ev + s_base;
         const uint32_t k0 = row[0], k1 = row[D];
-        const uint32_t lane = threadIdx.x & 31;
         auto class_of = [&](uint32_t k) {
             uint32_t lo = 0, hi = D;  // row[lo] <= k < row[hi]
             while (hi - lo > 1) {
@@ -1982,23 +1979,18 @@ __global__ void __launch_bounds__(kThreads) k_expand(Engine e) {
             }
             return lo;
         };
-        // (the loop bound is uniform per warp: k1 and the warp's first event)
-        for (uint32_t k = k0 + (threadIdx.x - lane); k < k1; k += 4 * blockDim.x) {
+        for (uint32_t k = k0 + threadIdx.x; k < k1; k += 4 * blockDim.x) {
             unsigned long long v[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                const uint32_t kk = k + lane + u * blockDim.x;
+                const uint32_t kk = k + u * blockDim.x;
                 v[u] = kk < k1 ? src[kk] : 0ull;
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                const uint32_t first = k + u * blockDim.x;  // the warp's first event this round
-                if (first >= k1) break;                      // (warp-uniform)
-                uint32_t d = lane == 0 ? class_of(first) : 0u;
-                d = __shfl_sync(0xffffffffu, d, 0);
-                const uint32_t kk = first + lane;
+                const uint32_t kk = k + u * blockDim.x;
                 if (kk >= k1) continue;
-                while (row[d + 1] <= kk) ++d;  // kk < row[D]: ends at the class of kk
+                const uint32_t d = class_of(kk);
                 if (s_ok[d]) e.wheel[s_dst[d] + kk] = v[u];
             }
         }
